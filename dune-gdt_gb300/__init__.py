@@ -1,0 +1,697 @@
+"""GB300-native drop-in for dune-gdt's discretize-and-solve path (Python side).
+
+Mirrors the names of the reference's Python bindings (python/dune/gdt/*: spaces, MatrixOperator,
+VectorFunctional, DirichletConstraints, DiscreteFunction, AdvectionFvOperator, ...). DoF vectors
+and coefficients are CUDA torch tensors (float64); all compute goes through the C ABI of
+libgdtgb300.so (include/gdt_gb300.h). There is no CPU fallback: without the library or a GPU every
+compute call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _capi as capi
+from ._capi import GdtError
+
+__all__ = [
+    "Context", "default_context", "make_cube_grid", "Grid", "ContinuousLagrangeSpace",
+    "DiscontinuousLagrangeSpace", "FiniteVolumeSpace", "Stencil", "LocalLaplaceIntegrand",
+    "LocalElementProductIntegrand", "LocalElementIntegralBilinearForm", "LocalElementIntegralFunctional",
+    "LocalLaplaceIPDGInnerCoupling", "LocalLaplaceIPDGDirichletCoupling", "LocalIPDGInnerPenalty",
+    "LocalIPDGBoundaryPenalty", "LocalCouplingIntersectionIntegralBilinearForm",
+    "LocalIntersectionIntegralBilinearForm", "MatrixOperator", "VectorFunctional", "DirichletConstraints",
+    "Walker", "DiscreteFunction", "BurgersFlux", "LinearTransportFlux", "NumericalLaxFriedrichsFlux",
+    "NumericalUpwindFlux", "AdvectionFvOperator", "ExplicitRungeKuttaTimeStepper",
+    "estimate_dt_for_hyperbolic_system", "GdtError",
+]
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("expected a CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _f64(t, n=None, name="vector"):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
+        raise TypeError(f"{name} must be a contiguous float64 CUDA tensor")
+    if n is not None and t.numel() != n:
+        raise ValueError(f"{name} has {t.numel()} entries, expected {n}")
+    return t
+
+
+# ---------------------------------------------------------------------------- context ---
+class Context:
+    """Device + CUDA stream the library works on (the torch current stream by default)."""
+
+    def __init__(self, device=0, stream=None):
+        self.lib = capi.load()
+        self.device = torch.device("cuda", device)
+        self.stream = stream if stream is not None else torch.cuda.current_stream(self.device)
+        h = C.c_void_p()
+        capi.check(self.lib.gdt_context_create(device, C.c_void_p(self.stream.cuda_stream), C.byref(h)))
+        self.handle = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.gdt_context_destroy(self.handle)
+        except Exception:
+            pass
+
+    def call(self, name, *args):
+        capi.check(getattr(self.lib, name)(self.handle, *args), self.handle, name)
+
+    def synchronize(self):
+        self.call("gdt_context_synchronize")
+
+    @property
+    def kernel_launches(self):
+        return int(self.lib.gdt_context_kernel_launches(self.handle))
+
+
+_default = {}
+
+
+def default_context() -> Context:
+    dev = torch.cuda.current_device()
+    if dev not in _default:
+        _default[dev] = Context(dev)
+    return _default[dev]
+
+
+# ------------------------------------------------------------------------------- grid ---
+class Grid:
+    """make_cube_grid: equidistant YaspGrid-like cube grid or its Kuhn simplex split."""
+
+    def __init__(self, lower_left, upper_right, num_elements, simplex=False, periodic=False):
+        dim = len(num_elements)
+        self.dimension = dim
+        self.lower_left = [float(x) for x in lower_left]
+        self.upper_right = [float(x) for x in upper_right]
+        self.num_cells = [int(n) for n in num_elements]
+        self.simplex = bool(simplex)
+        self.periodic = bool(periodic)
+        self.lib = capi.load()
+        h = C.c_void_p()
+        n = (C.c_int64 * 3)(*self.num_cells, *([1] * (3 - dim)))
+        lo = (C.c_double * 3)(*self.lower_left, *([0.0] * (3 - dim)))
+        hi = (C.c_double * 3)(*self.upper_right, *([1.0] * (3 - dim)))
+        capi.check(self.lib.gdt_grid_create_cube(dim, n, lo, hi, int(simplex), int(periodic), C.byref(h)),
+                   what="make_cube_grid")
+        self.handle = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.gdt_grid_destroy(self.handle)
+        except Exception:
+            pass
+
+    @property
+    def num_elements(self):
+        return int(self.lib.gdt_grid_num_elements(self.handle))
+
+    @property
+    def num_vertices(self):
+        return int(self.lib.gdt_grid_num_vertices(self.handle))
+
+    @property
+    def cell_volume(self):
+        v = 1.0
+        for a in range(self.dimension):
+            v *= (self.upper_right[a] - self.lower_left[a]) / self.num_cells[a]
+        if self.simplex:
+            import math
+
+            v /= math.factorial(self.dimension)
+        return v
+
+
+def make_cube_grid(lower_left, upper_right, num_elements, simplex=False, periodic=False) -> Grid:
+    dim = len(num_elements)
+    if not hasattr(lower_left, "__len__"):
+        lower_left = [lower_left] * dim
+    if not hasattr(upper_right, "__len__"):
+        upper_right = [upper_right] * dim
+    return Grid(lower_left, upper_right, num_elements, simplex, periodic)
+
+
+# ----------------------------------------------------------------------------- spaces ---
+class _Space:
+    kind = None
+
+    def __init__(self, grid: Grid, order: int):
+        self.grid = grid
+        self.order = order
+        self.lib = capi.load()
+        h = C.c_void_p()
+        capi.check(self.lib.gdt_space_create(grid.handle, self.kind, order, C.byref(h)), what=type(self).__name__)
+        self.handle = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.gdt_space_destroy(self.handle)
+        except Exception:
+            pass
+
+    @property
+    def num_DoFs(self):
+        return int(self.lib.gdt_space_size(self.handle))
+
+    size = num_DoFs
+
+    @property
+    def max_local_size(self):
+        return int(self.lib.gdt_space_max_local_size(self.handle))
+
+    def global_indices(self, ctx: Context | None = None):
+        """mapper.global_indices of every element: int64 CUDA tensor [num_elements, local_size]."""
+        ctx = ctx or default_context()
+        out = torch.empty((self.grid.num_elements, self.max_local_size), dtype=torch.int64, device=ctx.device)
+        ctx.call("gdt_space_global_indices", self.handle, _ptr(out))
+        return out
+
+
+class ContinuousLagrangeSpace(_Space):
+    kind = capi.SPACE_CG
+
+    def __init__(self, grid, order=1):
+        super().__init__(grid, order)
+
+
+class DiscontinuousLagrangeSpace(_Space):
+    kind = capi.SPACE_DG
+
+    def __init__(self, grid, order=1):
+        super().__init__(grid, order)
+
+
+class FiniteVolumeSpace(_Space):
+    kind = capi.SPACE_FV
+
+    def __init__(self, grid):
+        super().__init__(grid, 0)
+
+
+class Stencil:
+    element = capi.STENCIL_ELEMENT
+    intersection = capi.STENCIL_INTERSECTION
+    element_and_intersection = capi.STENCIL_ELEMENT_AND_INTERSECTION
+
+
+# ------------------------------------------------------------------- local forms (descriptors) ---
+def _coef(c):
+    """A diffusion / source coefficient: a Python number or a per-element float64 CUDA tensor."""
+    if isinstance(c, torch.Tensor):
+        return _f64(c, name="coefficient"), 0.0
+    return None, float(c)
+
+
+class LocalLaplaceIntegrand:
+    def __init__(self, diffusion=1.0):
+        self.diffusion = diffusion
+
+
+class _ProductWithAnsatz:
+    def __init__(self, weight, function):
+        self.weight = weight
+        self.function = function
+
+
+class LocalElementProductIntegrand:
+    def __init__(self, weight=1.0):
+        if weight != 1.0:
+            raise GdtError(capi.EUNSUPPORTED, "only the unit weight is lowered to the GPU library")
+        self.weight = weight
+
+    def with_ansatz(self, function):
+        return _ProductWithAnsatz(self.weight, function)
+
+
+class LocalElementIntegralBilinearForm:
+    def __init__(self, integrand, over_integrate=0):
+        self.integrand = integrand
+
+
+class LocalElementIntegralFunctional:
+    def __init__(self, integrand, over_integrate=0):
+        self.integrand = integrand
+
+
+class _Sum:
+    def __init__(self, *terms):
+        self.terms = list(terms)
+
+    def __add__(self, other):
+        return _Sum(*self.terms, other)
+
+
+class _Term:
+    def __add__(self, other):
+        return _Sum(self, other)
+
+
+class LocalLaplaceIPDGInnerCoupling(_Term):
+    def __init__(self, symmetry_prefactor, diffusion, weight=None):
+        self.symmetry_prefactor, self.diffusion, self.weight = float(symmetry_prefactor), diffusion, weight
+
+
+class LocalLaplaceIPDGDirichletCoupling(_Term):
+    def __init__(self, symmetry_prefactor, diffusion):
+        self.symmetry_prefactor, self.diffusion = float(symmetry_prefactor), diffusion
+
+
+class LocalIPDGInnerPenalty(_Term):
+    def __init__(self, penalty, weight=None):
+        self.penalty, self.weight = float(penalty), weight
+
+
+class LocalIPDGBoundaryPenalty(_Term):
+    def __init__(self, penalty, weight=None):
+        self.penalty, self.weight = float(penalty), weight
+
+
+class LocalCouplingIntersectionIntegralBilinearForm:
+    def __init__(self, integrand):
+        self.integrand = integrand
+
+
+class LocalIntersectionIntegralBilinearForm:
+    def __init__(self, integrand):
+        self.integrand = integrand
+
+
+def _terms(x):
+    return x.terms if isinstance(x, _Sum) else [x]
+
+
+# ---------------------------------------------------------------------------- matrix operator ---
+class MatrixOperator:
+    """make_matrix_operator(space, stencil): CSR matrix on the device + the appended local forms."""
+
+    def __init__(self, grid, source_space, range_space=None, stencil=Stencil.element, ctx: Context | None = None):
+        self.grid = grid
+        self.source_space = source_space
+        self.range_space = range_space or source_space
+        self.ctx = ctx or default_context()
+        self.stencil = stencil
+        h = C.c_void_p()
+        self.ctx.call("gdt_matrix_create", self.range_space.handle, self.source_space.handle, int(stencil),
+                      C.byref(h))
+        self.handle = h
+        self.forms = []
+        self._keep = []
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                capi.load().gdt_matrix_destroy(self.handle)
+        except Exception:
+            pass
+
+    def append(self, local_form):
+        self.forms.append(local_form)
+        return self
+
+    def __iadd__(self, local_form):
+        return self.append(local_form)
+
+    @property
+    def shape(self):
+        L = capi.load()
+        return int(L.gdt_matrix_rows(self.handle)), int(L.gdt_matrix_cols(self.handle))
+
+    @property
+    def nnz(self):
+        return int(capi.load().gdt_matrix_nnz(self.handle))
+
+    def csr(self):
+        """(row_ptr, col, val) as zero-copy CUDA tensors over the library-owned CSR arrays."""
+        rp, col, val = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        capi.check(capi.load().gdt_matrix_device_arrays(self.handle, C.byref(rp), C.byref(col), C.byref(val)))
+        n, nnz = self.shape[0], self.nnz
+        return (_wrap(rp.value, n + 1, torch.int32, self.ctx.device), _wrap(col.value, nnz, torch.int32, self.ctx.device),
+                _wrap(val.value, nnz, torch.float64, self.ctx.device))
+
+    @property
+    def matrix(self):
+        return self.csr()
+
+    def _diffusion_desc(self, rhs_force=None, dirichlet=False):
+        kappa = 1.0
+        for f in self.forms:
+            if isinstance(f, LocalElementIntegralBilinearForm) and isinstance(f.integrand, LocalLaplaceIntegrand):
+                kappa = f.integrand.diffusion
+        kt, kc = _coef(kappa)
+        d = capi.DiffusionDesc()
+        d.kappa = kt.data_ptr() if kt is not None else None
+        d.kappa_const = kc
+        ft, fc = _coef(1.0 if rhs_force is None else rhs_force)
+        d.force = ft.data_ptr() if ft is not None else None
+        d.force_const = fc
+        d.dirichlet = int(dirichlet)
+        return d
+
+    def _ipdg_desc(self, force=0.0):
+        kappa, theta, sig_in, sig_bd, wdiff = 1.0, 1.0, 8.0, 14.0, True
+        for f in self.forms:
+            if isinstance(f, LocalElementIntegralBilinearForm) and isinstance(f.integrand, LocalLaplaceIntegrand):
+                kappa = f.integrand.diffusion
+            for t in _terms(getattr(f, "integrand", None)):
+                if isinstance(t, LocalLaplaceIPDGInnerCoupling):
+                    theta = t.symmetry_prefactor
+                    wdiff = t.weight is not None
+                if isinstance(t, LocalIPDGInnerPenalty):
+                    sig_in = t.penalty
+                if isinstance(t, LocalIPDGBoundaryPenalty):
+                    sig_bd = t.penalty
+        kt, kc = _coef(kappa)
+        ft, fc = _coef(force)
+        d = capi.IpdgDesc()
+        d.kappa = kt.data_ptr() if kt is not None else None
+        d.kappa_const = kc
+        d.force = ft.data_ptr() if ft is not None else None
+        d.force_const = fc
+        d.symmetry_prefactor, d.sigma_inner, d.sigma_boundary, d.weight_is_diffusion = theta, sig_in, sig_bd, int(wdiff)
+        return d
+
+    def assemble(self, parallel=True, rhs=None, force=None, dirichlet=False):
+        """MatrixOperator::assemble; optionally fused with the load vector / Dirichlet constraints."""
+        if isinstance(self.source_space, DiscontinuousLagrangeSpace):
+            d = self._ipdg_desc(0.0 if force is None else force)
+            self.ctx.call("gdt_assemble_swipdg", self.handle, C.byref(d), _ptr(rhs))
+        else:
+            d = self._diffusion_desc(force, dirichlet)
+            self.ctx.call("gdt_assemble_cg_diffusion", self.handle, C.byref(d), _ptr(rhs))
+        return self
+
+    def apply(self, source, range=None):
+        n, m = self.shape
+        _f64(source, m, "source")
+        if range is None:
+            range = torch.empty(n, dtype=torch.float64, device=self.ctx.device)
+        self.ctx.call("gdt_spmv", self.handle, _ptr(source), _ptr(_f64(range, n, "range")))
+        return range
+
+    def apply_inverse(self, range, source=None, opts=None):
+        """Solve A source = range; opts: type ('cg'|'bicgstab'), precond ('jacobi'|'ilu0'|'none'),
+        precision ('fp64'|'mixed'), tol (relative residual), max_iter, check_every, inner_tol."""
+        opts = dict(opts or {})
+        n = self.shape[0]
+        _f64(range, n, "range")
+        if source is None:
+            source = torch.zeros(n, dtype=torch.float64, device=self.ctx.device)
+        o = capi.SolverOpts()
+        o.solver = {"cg": capi.SOLVER_CG, "bicgstab": capi.SOLVER_BICGSTAB}[opts.get("type", "cg")]
+        o.precond = {"none": capi.PREC_NONE, "jacobi": capi.PREC_JACOBI, "ilu0": capi.PREC_ILU0}[
+            opts.get("precond", "jacobi")]
+        o.precision = {"fp64": capi.PRECISION_FP64, "mixed": capi.PRECISION_MIXED}[opts.get("precision", "fp64")]
+        o.tol = float(opts.get("tol", 1e-10))
+        o.max_iter = int(opts.get("max_iter", 100000))
+        o.check_every = int(opts.get("check_every", 0))
+        o.inner_tol = float(opts.get("inner_tol", 0.0))
+        info = capi.SolveInfo()
+        self.ctx.call("gdt_solve", self.handle, _ptr(range), _ptr(_f64(source, n, "source")), C.byref(o),
+                      C.byref(info))
+        self.last_solve_info = {"iterations": info.iterations, "refinements": info.refinements,
+                                "rel_residual": info.rel_residual, "converged": bool(info.converged)}
+        return source
+
+
+def _wrap(ptr, n, dtype, device):
+    """Zero-copy CUDA tensor over library-owned device memory (lifetime: the owning handle)."""
+    if n == 0:
+        return torch.empty(0, dtype=dtype, device=device)
+    itemsize = torch.empty((), dtype=dtype).element_size()
+    cai = {"shape": (n,), "typestr": {torch.int32: "<i4", torch.int64: "<i8", torch.float64: "<f8",
+                                       torch.float32: "<f4"}[dtype],
+           "data": (ptr, False), "version": 3, "strides": (itemsize,)}
+
+    class _Holder:
+        __cuda_array_interface__ = cai
+
+    return torch.as_tensor(_Holder(), device=device)
+
+
+class VectorFunctional:
+    """make_vector_functional(space) with LocalElementIntegralFunctional(product.with_ansatz(f))."""
+
+    def __init__(self, grid, source_space, ctx: Context | None = None):
+        self.grid, self.space = grid, source_space
+        self.ctx = ctx or default_context()
+        self.forms = []
+        self.vector = torch.zeros(source_space.num_DoFs, dtype=torch.float64, device=self.ctx.device)
+
+    def append(self, local_functional):
+        self.forms.append(local_functional)
+        return self
+
+    __iadd__ = append
+
+    def force(self):
+        f = 0.0
+        for lf in self.forms:
+            if isinstance(lf.integrand, _ProductWithAnsatz):
+                f = lf.integrand.function
+        return f
+
+    def assemble(self, parallel=True):
+        ft, fc = _coef(self.force())
+        d = capi.DiffusionDesc()
+        d.kappa, d.kappa_const = None, 1.0
+        d.force = ft.data_ptr() if ft is not None else None
+        d.force_const = fc
+        d.dirichlet = 0
+        self.ctx.call("gdt_assemble_cg_rhs", self.space.handle, C.byref(d), _ptr(self.vector))
+        return self
+
+
+class DirichletConstraints:
+    """make_dirichlet_constraints(space, AllDirichletBoundaryInfo) + apply(M, V)."""
+
+    def __init__(self, boundary_info, space, ctx: Context | None = None):
+        if boundary_info not in ("dirichlet", "all_dirichlet", None):
+            raise GdtError(capi.EUNSUPPORTED, "only the all-Dirichlet boundary info is lowered")
+        self.space = space
+        self.ctx = ctx or default_context()
+        self.applied_in_walk = False
+
+    def apply(self, matrix_operator, vector=None):
+        if self.applied_in_walk:
+            return
+        self.ctx.call("gdt_dirichlet_apply", matrix_operator.handle, _ptr(vector))
+
+
+class Walker:
+    """XT::Grid::Walker over (MatrixOperator, VectorFunctional, DirichletConstraints): one fused kernel."""
+
+    def __init__(self, grid):
+        self.grid = grid
+        self.functors = []
+
+    def append(self, functor):
+        self.functors.append(functor)
+        return self
+
+    def walk(self, thread_parallel=True):
+        ops = [f for f in self.functors if isinstance(f, MatrixOperator)]
+        funcs = [f for f in self.functors if isinstance(f, VectorFunctional)]
+        dcs = [f for f in self.functors if isinstance(f, DirichletConstraints)]
+        if len(ops) == 1 and len(funcs) <= 1 and not isinstance(ops[0].source_space, DiscontinuousLagrangeSpace):
+            rhs = funcs[0].vector if funcs else None
+            force = funcs[0].force() if funcs else None
+            # the Dirichlet constraints are applied by DirichletConstraints.apply in the reference;
+            # here they are fused into the same pass and apply() becomes a no-op
+            ops[0].assemble(rhs=rhs, force=force, dirichlet=bool(dcs))
+            for d in dcs:
+                d.applied_in_walk = True
+            return
+        for o in ops:
+            o.assemble()
+        for f in funcs:
+            f.assemble()
+
+
+class DiscreteFunction:
+    def __init__(self, space, vector=None, name="dune.gdt.discretefunction"):
+        self.space = space
+        self.name = name
+        self._vector = vector if vector is not None else torch.zeros(space.num_DoFs, dtype=torch.float64,
+                                                                     device=default_context().device)
+
+    def dofs(self):
+        return self
+
+    @property
+    def vector(self):
+        return self._vector
+
+
+# ---------------------------------------------------------------------------- finite volumes ---
+class BurgersFlux:
+    """f(u) = u^2/2 (1, ..., 1)"""
+    kind = capi.FLUX_BURGERS
+    velocity = (0.0, 0.0, 0.0)
+
+
+class LinearTransportFlux:
+    """f(u) = v u"""
+    kind = capi.FLUX_TRANSPORT
+
+    def __init__(self, velocity):
+        self.velocity = tuple(float(v) for v in velocity) + (0.0,) * (3 - len(velocity))
+
+
+class NumericalLaxFriedrichsFlux:
+    numflux = capi.NUMFLUX_LAX_FRIEDRICHS
+
+    def __init__(self, flux, lambda_=0.0):
+        self.flux, self.lf_lambda = flux, float(lambda_)
+
+
+class NumericalUpwindFlux:
+    numflux = capi.NUMFLUX_UPWIND
+
+    def __init__(self, flux):
+        self.flux, self.lf_lambda = flux, 0.0
+
+
+def _fv_desc(numerical_flux):
+    d = capi.FvDesc()
+    d.flux = numerical_flux.flux.kind
+    for i, v in enumerate(numerical_flux.flux.velocity[:3]):
+        d.velocity[i] = v
+    d.numflux = numerical_flux.numflux
+    d.lf_lambda = numerical_flux.lf_lambda
+    return d
+
+
+class AdvectionFvOperator:
+    """AdvectionFvOperator(grid_view, numerical_flux, source_space, range_space) on a periodic grid."""
+
+    def __init__(self, grid, numerical_flux, source_space, range_space=None, ctx: Context | None = None):
+        self.grid, self.numerical_flux = grid, numerical_flux
+        self.space = source_space
+        self.ctx = ctx or default_context()
+        self.desc = _fv_desc(numerical_flux)
+
+    def apply(self, source, range=None, param=None):
+        n = self.space.num_DoFs
+        _f64(source, n, "source")
+        if range is None:
+            range = torch.empty(n, dtype=torch.float64, device=self.ctx.device)
+        self.ctx.call("gdt_fv_apply", self.space.handle, C.byref(self.desc), _ptr(source), _ptr(range))
+        return range
+
+
+def estimate_dt_for_hyperbolic_system(grid, state, flux_operator: AdvectionFvOperator):
+    dt = C.c_double()
+    op = flux_operator
+    op.ctx.call("gdt_fv_estimate_dt", op.space.handle, C.byref(op.desc), _ptr(_f64(state, op.space.num_DoFs)),
+                C.byref(dt))
+    return dt.value
+
+
+class ExplicitRungeKuttaTimeStepper:
+    """ExplicitRungeKuttaTimeStepper(op, initial_values, r=-1) with the explicit Euler or SSP2 tableau.
+    `u` may hold a batch of states one after another (independent initial conditions)."""
+
+    def __init__(self, op: AdvectionFvOperator, initial_values, r=-1.0, method="ssp2"):
+        if r != -1.0:
+            raise GdtError(capi.EUNSUPPORTED, "only r = -1 (u_t + L(u) = 0) is lowered")
+        self.op = op
+        self.u = initial_values
+        self.method = {"ssp2": capi.TIMESTEPPER_SSPRK2, "euler": capi.TIMESTEPPER_EXPLICIT_EULER}[method]
+        self.work = torch.empty_like(initial_values)
+        self.t = 0.0
+
+    def step(self, dt, steps=1):
+        n = self.op.space.num_DoFs
+        nbatch = self.u.numel() // n
+        self.op.ctx.call("gdt_fv_timestep", self.op.space.handle, C.byref(self.op.desc), self.method,
+                         C.c_double(dt), C.c_int64(steps), C.c_int64(nbatch), _ptr(self.u), _ptr(self.work))
+        self.t += dt * steps
+        return dt
+
+
+# ---------------------------------------------------------------------------- adjoint / autograd ---
+def dlogkappa(op: MatrixOperator, u, lam, kappa):
+    """out[e] = -d/dlog(kappa_e) [lam^T A(kappa) u] for the operator's Laplace (CG) or SWIPDG (DG) forms:
+    the log-kappa gradient of J(u(kappa)) when lam solves A^T lam = dJ/du."""
+    ne = op.grid.num_elements
+    out = torch.empty(ne, dtype=torch.float64, device=op.ctx.device)
+    n = op.shape[0]
+    _f64(u, n, "u")
+    _f64(lam, n, "lam")
+    _f64(kappa, ne, "kappa")
+    if isinstance(op.source_space, DiscontinuousLagrangeSpace):
+        d = op._ipdg_desc()
+        d.kappa = kappa.data_ptr()
+        op.ctx.call("gdt_swipdg_dlogkappa", op.source_space.handle, C.byref(d), _ptr(u), _ptr(lam), _ptr(out))
+    else:
+        op.ctx.call("gdt_cg_dlogkappa", op.source_space.handle, _ptr(kappa), _ptr(u), _ptr(lam), _ptr(out))
+    return out
+
+
+class DiffusionProblem:
+    """-div(kappa grad u) = f with kappa = exp(log_kappa) per element: continuous P1/Q1 with homogeneous
+    Dirichlet constraints, or SWIPDG P1 (sigma_inner, sigma_boundary, theta = 1, weight = kappa)."""
+
+    def __init__(self, grid, dg=False, force=1.0, sigma_inner=8.0, sigma_boundary=14.0, solver_opts=None):
+        self.grid = grid
+        self.dg = dg
+        self.force = force
+        self.sigma = (sigma_inner, sigma_boundary)
+        self.solver_opts = dict(solver_opts or {"tol": 1e-12})
+        if dg:
+            self.space = DiscontinuousLagrangeSpace(grid, 1)
+            self.op = MatrixOperator(grid, self.space, stencil=Stencil.element_and_intersection)
+        else:
+            self.space = ContinuousLagrangeSpace(grid, 1)
+            self.op = MatrixOperator(grid, self.space)
+        self.rhs = torch.zeros(self.space.num_DoFs, dtype=torch.float64, device=self.op.ctx.device)
+
+    def assemble(self, kappa):
+        op = self.op
+        op.forms = [LocalElementIntegralBilinearForm(LocalLaplaceIntegrand(kappa))]
+        if self.dg:
+            op.forms += [
+                LocalCouplingIntersectionIntegralBilinearForm(
+                    LocalLaplaceIPDGInnerCoupling(1.0, kappa, kappa) + LocalIPDGInnerPenalty(self.sigma[0], kappa)),
+                LocalIntersectionIntegralBilinearForm(
+                    LocalLaplaceIPDGDirichletCoupling(1.0, kappa) + LocalIPDGBoundaryPenalty(self.sigma[1], kappa)),
+            ]
+            op.assemble(rhs=self.rhs, force=self.force)
+        else:
+            op.assemble(rhs=self.rhs, force=self.force, dirichlet=True)
+
+    def solve(self, kappa, rhs=None):
+        self.assemble(kappa)
+        return self.op.apply_inverse(self.rhs if rhs is None else rhs, opts=self.solver_opts)
+
+
+class DiffusionSolve(torch.autograd.Function):
+    """u = solve(A(exp(log_kappa)) u = f). Backward: one adjoint solve A^T lam = grad_u (A is symmetric
+    for CG Laplace and SWIPDG with theta = 1) and the element kernel -lam^T dA/dlog(kappa_e) u."""
+
+    @staticmethod
+    def forward(ctx, log_kappa, problem: DiffusionProblem):
+        kappa = torch.exp(log_kappa.detach()).contiguous()
+        u = problem.solve(kappa).clone()
+        ctx.problem = problem
+        ctx.save_for_backward(kappa, u)
+        return u
+
+    @staticmethod
+    def backward(ctx, grad_u):
+        kappa, u = ctx.saved_tensors
+        problem = ctx.problem
+        problem.assemble(kappa)  # the operator may have been reassembled since forward
+        lam = problem.op.apply_inverse(grad_u.contiguous().to(torch.float64), opts=problem.solver_opts)
+        return dlogkappa(problem.op, u, lam, kappa), None

@@ -1,0 +1,307 @@
+// Continuous P1/Q1 assembly on structured grids: stiffness of LocalLaplaceIntegrand(kappa)
+// (local/integrands/laplace.hh:81-102 under LocalElementIntegralBilinearForm,
+// local/bilinear-forms/integrals.hh:97-134), load vector of LocalElementProductIntegrand().with_ansatz(f)
+// (local/functionals/integrals.hh:72-98) and DirichletConstraints::apply (tools/dirichlet-constraints.hh:153-184).
+//
+// Design: output-stationary. One thread owns one matrix row (one vertex); it visits the <= 2^d cells
+// around its vertex, adds kappa_e * K_t[li][lj] of every element containing it into a register
+// accumulator laid out over the 3^d vertex stencil, applies the Dirichlet unit row/column rule and
+// writes its CSR row exactly once. No atomics and no colouring passes: each value is produced by
+// exactly one thread, so the result is deterministic and the HBM traffic is one write per nonzero.
+// Elements of one type t share their geometry on an equidistant grid, so the per-type local matrices
+// K_t (exact integrals, equal to the reference's exact quadrature up to rounding) are kernel parameters.
+#include <cmath>
+
+#include "structured.cuh"
+
+namespace gdt {
+namespace {
+
+constexpr int kMaxSub = 6, kMaxLoc = 8;
+// per-type local matrices, passed by value (kernel parameter space) so that contexts on
+// different grids never share mutable device state
+struct LocalTables {
+  double K[kMaxSub * kMaxLoc * kMaxLoc];
+  double B[kMaxSub * kMaxLoc];
+};
+
+// host: exact local stiffness / load of element type t (P1 simplex or Q1 cube) on cells of size h
+void local_matrices(const GridDesc& g, double* K, double* B) {
+  const int d = g.dim, ns = g.nsub, nl = g.simplex ? d + 1 : (1 << d);
+  for (int t = 0; t < ns; ++t) {
+    double* Kt = K + t * kMaxLoc * kMaxLoc;
+    double* Bt = B + t * kMaxLoc;
+    if (g.simplex) {
+      // vertices X_j = h * corner(t, j); J = [X_1 - X_0, ..., X_d - X_0]
+      double X[4][3] = {};
+      for (int j = 0; j < nl; ++j) {
+        int c = local_corner(d, true, t, j);
+        for (int a = 0; a < d; ++a) X[j][a] = ((c >> a) & 1) * g.h[a];
+      }
+      double J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+      for (int k = 0; k < d; ++k)
+        for (int a = 0; a < d; ++a) J[a][k] = X[k + 1][a] - X[0][a];
+      double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                   J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      double inv[3][3];
+      inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+      inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+      inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+      inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+      inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+      inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+      inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+      inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+      inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+      // reference gradients: phi_0 = 1 - sum x, phi_j = x_{j-1}; physical = J^{-T} grad_ref
+      double G[4][3] = {};
+      for (int j = 0; j < nl; ++j)
+        for (int a = 0; a < d; ++a) {
+          double s = 0;
+          for (int k = 0; k < d; ++k) {
+            double gr = (j == 0) ? -1.0 : (k == j - 1 ? 1.0 : 0.0);
+            s += inv[k][a] * gr;
+          }
+          G[j][a] = s;
+        }
+      double fact = 1;
+      for (int i = 2; i <= d; ++i) fact *= i;
+      double vol = std::fabs(det) / fact;
+      for (int i = 0; i < nl; ++i) {
+        for (int j = 0; j < nl; ++j) {
+          double s = 0;
+          for (int a = 0; a < d; ++a) s += G[i][a] * G[j][a];
+          Kt[i * kMaxLoc + j] = vol * s;
+        }
+        Bt[i] = vol / (d + 1);
+      }
+    } else {
+      // Q1 tensor product: int dpsi_p dpsi_q = +-1/h, int psi_p psi_q = h/3 or h/6
+      double vol = 1;
+      for (int a = 0; a < d; ++a) vol *= g.h[a];
+      for (int i = 0; i < nl; ++i) {
+        for (int j = 0; j < nl; ++j) {
+          double s = 0;
+          for (int a = 0; a < d; ++a) {
+            int pa = (i >> a) & 1, qa = (j >> a) & 1;
+            double term = (pa == qa ? 1.0 : -1.0) / g.h[a];
+            for (int b = 0; b < d; ++b) {
+              if (b == a) continue;
+              int pb = (i >> b) & 1, qb = (j >> b) & 1;
+              term *= g.h[b] * (pb == qb ? 1.0 / 3.0 : 1.0 / 6.0);
+            }
+            s += term;
+          }
+          Kt[i * kMaxLoc + j] = s;
+        }
+        Bt[i] = vol / nl;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ bool on_boundary(const GridDesc& g, const long long* vi, int dim) {
+  bool b = false;
+  for (int a = 0; a < dim; ++a) b = b || vi[a] == 0 || vi[a] == g.n[a];
+  return b;
+}
+
+template <int DIM, bool SIMPLEX>
+__global__ void __launch_bounds__(256) assemble_cg_rows(GridDesc g, const int* __restrict__ rp, double* __restrict__ val,
+                                                        double* __restrict__ rhs, const LocalTables tab,
+                                                        const double* __restrict__ kappa,
+                                                        double kappa_const, const double* __restrict__ force,
+                                                        double force_const, int dirichlet) {
+  constexpr int NS = pow3(DIM), NSUB = num_sub(DIM, SIMPLEX), NLOC = num_local(DIM, SIMPLEX);
+  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (v >= g.nvert) return;
+  long long vi[3];
+  vertex_multi(g, v, vi);
+  double acc[NS];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) acc[k] = 0.0;
+  double b = 0.0;
+#pragma unroll
+  for (int cv = 0; cv < (1 << DIM); ++cv) {
+    // v is corner cv of cell vi - bits(cv)
+    long long ci[3] = {0, 0, 0};
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      ci[a] = vi[a] - ((cv >> a) & 1);
+      inside = inside && ci[a] >= 0 && ci[a] < g.n[a];
+    }
+    if (!inside) continue;
+    const long long cell = cell_index(g, ci);
+#pragma unroll
+    for (int t = 0; t < NSUB; ++t) {
+#pragma unroll
+      for (int li = 0; li < NLOC; ++li) {
+        if (local_corner(DIM, SIMPLEX, t, li) != cv) continue;
+        const long long e = cell * NSUB + t;
+        const double kap = kappa ? kappa[e] : kappa_const;
+#pragma unroll
+        for (int lj = 0; lj < NLOC; ++lj)
+          acc[slot_between(DIM, cv, local_corner(DIM, SIMPLEX, t, lj))] += kap * tab.K[(t * kMaxLoc + li) * kMaxLoc + lj];
+        if (rhs) b += (force ? force[e] : force_const) * tab.B[t * kMaxLoc + li];
+      }
+    }
+  }
+  const bool bnd = dirichlet && on_boundary(g, vi, DIM);
+  if (rhs) rhs[v] = bnd ? 0.0 : b;
+  if (!val) return;
+  long long pos = rp[v];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    if (!slot_in_stencil(DIM, SIMPLEX, k)) continue;
+    long long w[3] = {0, 0, 0};
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      w[a] = vi[a] + slot_offset(k, a);
+      ok = ok && w[a] >= 0 && w[a] <= g.n[a];
+    }
+    if (!ok) continue;
+    double value = acc[k];
+    if (dirichlet) {
+      if (bnd) value = (k == center_slot(DIM)) ? 1.0 : 0.0;  // unit_row
+      else if (on_boundary(g, w, DIM)) value = 0.0;          // unit_col
+    }
+    val[pos++] = value;
+  }
+}
+
+// DirichletConstraints::apply(M, V) as a separate pass over an assembled matrix: unit rows for
+// boundary DoFs, zero boundary columns elsewhere (pattern is symmetric), rhs[D] = 0.
+template <int DIM>
+__global__ void dirichlet_rows(GridDesc g, const int* __restrict__ rp, const int* __restrict__ col,
+                               double* __restrict__ val, double* __restrict__ rhs) {
+  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (v >= g.nvert) return;
+  long long vi[3];
+  vertex_multi(g, v, vi);
+  const bool bnd = on_boundary(g, vi, DIM);
+  for (int k = rp[v]; k < rp[v + 1]; ++k) {
+    const long long w = col[k];
+    if (bnd) {
+      val[k] = (w == v) ? 1.0 : 0.0;
+    } else {
+      long long wi[3];
+      vertex_multi(g, w, wi);
+      if (on_boundary(g, wi, DIM)) val[k] = 0.0;
+    }
+  }
+  if (rhs && bnd) rhs[v] = 0.0;
+}
+
+// -lam_e^T (dA_e / dlog kappa_e) u_e = -kappa_e lam_e^T K_t u_e, Dirichlet rows and columns excluded
+template <int DIM, bool SIMPLEX>
+__global__ void cg_dlogkappa_kernel(GridDesc g, const LocalTables tab, const double* __restrict__ kappa, const double* __restrict__ u,
+                                    const double* __restrict__ lam, double* __restrict__ out) {
+  constexpr int NSUB = num_sub(DIM, SIMPLEX), NLOC = num_local(DIM, SIMPLEX);
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= g.nelem) return;
+  const long long cell = e / NSUB;
+  const int t = int(e % NSUB);
+  long long ci[3];
+  cell_multi(g, cell, ci);
+  double ul[NLOC], ll[NLOC];
+#pragma unroll
+  for (int j = 0; j < NLOC; ++j) {
+    int c = 0;
+#pragma unroll
+    for (int tt = 0; tt < NSUB; ++tt)
+      if (tt == t) c = local_corner(DIM, SIMPLEX, tt, j);
+    long long vi[3] = {0, 0, 0}, vidx = 0, stride = 1;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      vi[a] = ci[a] + ((c >> a) & 1);
+      vidx += vi[a] * stride;
+      stride *= g.vn[a];
+    }
+    const bool bnd = on_boundary(g, vi, DIM);
+    ul[j] = bnd ? 0.0 : u[vidx];
+    ll[j] = bnd ? 0.0 : lam[vidx];
+  }
+  double acc = 0.0;
+#pragma unroll
+  for (int i = 0; i < NLOC; ++i) {
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < NLOC; ++j) s += tab.K[(t * kMaxLoc + i) * kMaxLoc + j] * ul[j];
+    acc += ll[i] * s;
+  }
+  out[e] = -kappa[e] * acc;
+}
+
+LocalTables make_tables(const GridDesc& g) {
+  LocalTables tab = {};
+  local_matrices(g, tab.K, tab.B);
+  return tab;
+}
+
+}  // namespace
+
+gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs) {
+  const GridDesc& g = m->test.g;
+  const LocalTables tab = make_tables(g);
+  const int th = 256;
+  const int bl = grid_blocks(g.nvert, th);
+  cudaStream_t s = ctx->stream;
+#define GDT_LAUNCH_ASM(D, S)                                                                                   \
+  assemble_cg_rows<D, S><<<bl, th, 0, s>>>(g, m->rp, m->val, rhs, tab, d->kappa, d->kappa_const, d->force, d->force_const, \
+                                           d->dirichlet)
+  if (g.dim == 1) GDT_LAUNCH_ASM(1, false);
+  else if (g.dim == 2 && !g.simplex) GDT_LAUNCH_ASM(2, false);
+  else if (g.dim == 2) GDT_LAUNCH_ASM(2, true);
+  else if (!g.simplex) GDT_LAUNCH_ASM(3, false);
+  else GDT_LAUNCH_ASM(3, true);
+#undef GDT_LAUNCH_ASM
+  return check_launch(ctx, "assemble_cg_rows");
+}
+
+gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& sp, const gdt_diffusion_desc* d, double* rhs) {
+  const GridDesc& g = sp.g;
+  const LocalTables tab = make_tables(g);
+  const int th = 256;
+  const int bl = grid_blocks(g.nvert, th);
+  cudaStream_t s = ctx->stream;
+#define GDT_LAUNCH_RHS(D, S)                                                                                  \
+  assemble_cg_rows<D, S><<<bl, th, 0, s>>>(g, nullptr, nullptr, rhs, tab, d->kappa, d->kappa_const, d->force, \
+                                           d->force_const, d->dirichlet)
+  if (g.dim == 1) GDT_LAUNCH_RHS(1, false);
+  else if (g.dim == 2 && !g.simplex) GDT_LAUNCH_RHS(2, false);
+  else if (g.dim == 2) GDT_LAUNCH_RHS(2, true);
+  else if (!g.simplex) GDT_LAUNCH_RHS(3, false);
+  else GDT_LAUNCH_RHS(3, true);
+#undef GDT_LAUNCH_RHS
+  return check_launch(ctx, "assemble_cg_rhs");
+}
+
+gdt_status dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
+  const GridDesc& g = m->test.g;
+  const int th = 256;
+  const int bl = grid_blocks(g.nvert, th);
+  cudaStream_t s = ctx->stream;
+  if (g.dim == 1) dirichlet_rows<1><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs);
+  else if (g.dim == 2) dirichlet_rows<2><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs);
+  else dirichlet_rows<3><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs);
+  return check_launch(ctx, "dirichlet_rows");
+}
+
+gdt_status cg_dlogkappa(gdt_context ctx, const gdt_space_s& sp, const double* kappa, const double* u,
+                        const double* lam, double* out) {
+  const GridDesc& g = sp.g;
+  const LocalTables tab = make_tables(g);
+  const int th = 256;
+  const int bl = grid_blocks(g.nelem, th);
+  cudaStream_t s = ctx->stream;
+  if (g.dim == 1) cg_dlogkappa_kernel<1, false><<<bl, th, 0, s>>>(g, tab, kappa, u, lam, out);
+  else if (g.dim == 2 && !g.simplex) cg_dlogkappa_kernel<2, false><<<bl, th, 0, s>>>(g, tab, kappa, u, lam, out);
+  else if (g.dim == 2) cg_dlogkappa_kernel<2, true><<<bl, th, 0, s>>>(g, tab, kappa, u, lam, out);
+  else if (!g.simplex) cg_dlogkappa_kernel<3, false><<<bl, th, 0, s>>>(g, tab, kappa, u, lam, out);
+  else cg_dlogkappa_kernel<3, true><<<bl, th, 0, s>>>(g, tab, kappa, u, lam, out);
+  return check_launch(ctx, "cg_dlogkappa");
+}
+
+}  // namespace gdt

@@ -1,0 +1,389 @@
+// C ABI entry points: handle management, argument validation and dispatch to the kernels.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "internal.cuh"
+
+namespace gdt {
+
+gdt_status fail(gdt_context ctx, gdt_status s, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return s;
+}
+
+gdt_status check_launch(gdt_context ctx, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  if (ctx) ctx->launches++;
+  return GDT_OK;
+}
+
+void timing_begin(gdt_context ctx, cudaStream_t s, int kind) {
+  if (!ctx->timing) return;
+  if (ctx->events_used + 2 > ctx->events.size()) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    ctx->events.push_back(a);
+    ctx->events.push_back(b);
+    ctx->event_kind.push_back(kind);
+  }
+  ctx->event_kind[ctx->events_used / 2] = kind;
+  cudaEventRecord(ctx->events[ctx->events_used], s);
+}
+
+void timing_end(gdt_context ctx, cudaStream_t s) {
+  if (!ctx->timing) return;
+  cudaEventRecord(ctx->events[ctx->events_used + 1], s);
+  ctx->events_used += 2;
+}
+
+void timing_harvest(gdt_context ctx) {
+  for (size_t k = 0; k + 1 < ctx->events_used; k += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->events[k], ctx->events[k + 1]) == cudaSuccess) {
+      const int kind = ctx->event_kind[k / 2];
+      ctx->spmv_ms[kind] += ms;
+      ctx->spmv_launches[kind] += 1;
+    }
+  }
+  ctx->events_used = 0;
+}
+
+}  // namespace gdt
+
+using namespace gdt;
+
+extern "C" {
+
+const char* gdt_status_string(gdt_status s) {
+  switch (s) {
+    case GDT_OK: return "ok";
+    case GDT_EINVAL: return "invalid argument";
+    case GDT_ESHAPE: return "shape mismatch";
+    case GDT_ENOCONV: return "linear solver did not converge";
+    case GDT_ETIMEOUT: return "device wait exceeded its iteration budget";
+    case GDT_ENAN: return "non-finite value";
+    case GDT_EUNSUPPORTED: return "not supported by the GPU library";
+    case GDT_ECUDA: return "CUDA error";
+    case GDT_ENOMEM: return "out of device memory";
+  }
+  return "unknown status";
+}
+
+gdt_status gdt_context_create(int device, void* stream, gdt_context* out) {
+  if (!out) return GDT_EINVAL;
+  *out = nullptr;
+  gdt_context ctx = new (std::nothrow) gdt_context_s;
+  if (!ctx) return GDT_ENOMEM;
+  ctx->device = device;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->scratch, sizeof(double) * kScratchDoubles);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->counters, sizeof(unsigned int) * kCounters);
+  if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, sizeof(unsigned int) * kCounters);
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->host_pinned, sizeof(double) * 64);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    gdt_context_destroy(ctx);
+    return GDT_ECUDA;
+  }
+  *out = ctx;
+  return GDT_OK;
+}
+
+gdt_status gdt_context_set_timing(gdt_context ctx, int enable) {
+  if (!ctx) return GDT_EINVAL;
+  ctx->timing = enable ? 1 : 0;
+  return GDT_OK;
+}
+
+gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp64_launches, double* fp32_ms,
+                                   int64_t* fp32_launches, int reset) {
+  if (!ctx) return GDT_EINVAL;
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  timing_harvest(ctx);
+  if (fp64_ms) *fp64_ms = ctx->spmv_ms[0];
+  if (fp64_launches) *fp64_launches = ctx->spmv_launches[0];
+  if (fp32_ms) *fp32_ms = ctx->spmv_ms[1];
+  if (fp32_launches) *fp32_launches = ctx->spmv_launches[1];
+  if (reset) {
+    ctx->spmv_ms[0] = ctx->spmv_ms[1] = 0.0;
+    ctx->spmv_launches[0] = ctx->spmv_launches[1] = 0;
+  }
+  return GDT_OK;
+}
+
+gdt_status gdt_context_destroy(gdt_context ctx) {
+  if (!ctx) return GDT_EINVAL;
+  for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
+  if (ctx->scratch) cudaFree(ctx->scratch);
+  if (ctx->counters) cudaFree(ctx->counters);
+  if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
+  delete ctx;
+  return GDT_OK;
+}
+
+gdt_status gdt_context_set_stream(gdt_context ctx, void* stream) {
+  if (!ctx) return GDT_EINVAL;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return GDT_OK;
+}
+
+gdt_status gdt_context_synchronize(gdt_context ctx) {
+  if (!ctx) return GDT_EINVAL;
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GDT_OK;
+}
+
+const char* gdt_context_last_error(gdt_context ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int64_t gdt_context_kernel_launches(gdt_context ctx) { return ctx ? ctx->launches : 0; }
+
+// ---------------------------------------------------------------------- grid ---
+gdt_status gdt_grid_create_cube(int dim, const int64_t* num_elements, const double* lower_left,
+                                const double* upper_right, int simplex, int periodic, gdt_grid* out) {
+  if (!out || !num_elements || !lower_left || !upper_right) return GDT_EINVAL;
+  *out = nullptr;
+  if (dim < 1 || dim > 3) return GDT_EINVAL;
+  if (simplex && periodic) return GDT_EUNSUPPORTED;
+  gdt_grid g = new (std::nothrow) gdt_grid_s;
+  if (!g) return GDT_ENOMEM;
+  GridDesc& d = g->d;
+  d.dim = dim;
+  d.simplex = (simplex && dim >= 2) ? 1 : 0;
+  d.periodic = periodic ? 1 : 0;
+  d.ncells = 1;
+  d.nvert = 1;
+  for (int i = 0; i < 3; ++i) {
+    if (i < dim) {
+      if (num_elements[i] < 1 || !(upper_right[i] > lower_left[i])) {
+        delete g;
+        return GDT_EINVAL;
+      }
+      d.n[i] = num_elements[i];
+      d.lo[i] = lower_left[i];
+      d.hi[i] = upper_right[i];
+    } else {
+      d.n[i] = 1;
+      d.lo[i] = 0.0;
+      d.hi[i] = 1.0;
+    }
+    d.h[i] = (d.hi[i] - d.lo[i]) / double(d.n[i]);
+    d.vn[i] = i < dim ? d.n[i] + 1 : 1;
+    d.ncells *= d.n[i];
+    d.nvert *= d.vn[i];
+  }
+  d.nsub = 1;
+  if (d.simplex)
+    for (int i = 2; i <= dim; ++i) d.nsub *= i;
+  d.nelem = d.ncells * d.nsub;
+  if (d.nvert >= (1LL << 31) || d.nelem >= (1LL << 31)) {
+    delete g;
+    return GDT_EUNSUPPORTED;
+  }
+  *out = g;
+  return GDT_OK;
+}
+
+gdt_status gdt_grid_destroy(gdt_grid g) {
+  if (!g) return GDT_EINVAL;
+  delete g;
+  return GDT_OK;
+}
+
+int64_t gdt_grid_num_elements(gdt_grid g) { return g ? g->d.nelem : -1; }
+int64_t gdt_grid_num_vertices(gdt_grid g) { return g ? g->d.nvert : -1; }
+
+// --------------------------------------------------------------------- space ---
+gdt_status gdt_space_create(gdt_grid g, int kind, int order, gdt_space* out) {
+  if (!g || !out) return GDT_EINVAL;
+  *out = nullptr;
+  const GridDesc& d = g->d;
+  gdt_space_s s;
+  s.g = d;
+  s.kind = kind;
+  s.order = order;
+  if (kind == GDT_SPACE_CG) {
+    if (order != 1) return GDT_EUNSUPPORTED;
+    if (d.periodic) return GDT_EUNSUPPORTED;
+    s.lsize = d.simplex ? d.dim + 1 : (1 << d.dim);
+    s.size = d.nvert;
+  } else if (kind == GDT_SPACE_DG) {
+    if (order != 1 || d.periodic) return GDT_EUNSUPPORTED;
+    s.lsize = d.simplex ? d.dim + 1 : (1 << d.dim);
+    s.size = d.nelem * s.lsize;
+  } else if (kind == GDT_SPACE_FV) {
+    if (order != 0) return GDT_EINVAL;
+    if (d.simplex) return GDT_EUNSUPPORTED;
+    s.lsize = 1;
+    s.size = d.nelem;
+  } else {
+    return GDT_EINVAL;
+  }
+  if (s.size >= (1LL << 31)) return GDT_EUNSUPPORTED;
+  gdt_space sp = new (std::nothrow) gdt_space_s(s);
+  if (!sp) return GDT_ENOMEM;
+  *out = sp;
+  return GDT_OK;
+}
+
+gdt_status gdt_space_destroy(gdt_space s) {
+  if (!s) return GDT_EINVAL;
+  delete s;
+  return GDT_OK;
+}
+
+int64_t gdt_space_size(gdt_space s) { return s ? s->size : -1; }
+int gdt_space_max_local_size(gdt_space s) { return s ? s->lsize : -1; }
+
+// -------------------------------------------------------------------- matrix ---
+gdt_status gdt_matrix_create(gdt_context ctx, gdt_space test, gdt_space ansatz, int stencil, gdt_matrix* out) {
+  if (!ctx || !test || !ansatz || !out) return GDT_EINVAL;
+  *out = nullptr;
+  if (stencil < GDT_STENCIL_ELEMENT || stencil > GDT_STENCIL_ELEMENT_AND_INTERSECTION)
+    return fail(ctx, GDT_EINVAL, "unknown stencil");
+  if (test->kind != ansatz->kind || test->order != ansatz->order ||
+      std::memcmp(test->g.n, ansatz->g.n, sizeof(test->g.n)) != 0 || test->g.simplex != ansatz->g.simplex)
+    return fail(ctx, GDT_EUNSUPPORTED, "test and ansatz space must coincide");
+  if (test->kind == GDT_SPACE_FV) return fail(ctx, GDT_EUNSUPPORTED, "no matrix for finite-volume spaces");
+  if (test->kind == GDT_SPACE_CG && stencil != GDT_STENCIL_ELEMENT)
+    return fail(ctx, GDT_EUNSUPPORTED, "continuous spaces use the element stencil");
+  gdt_matrix m = new (std::nothrow) gdt_matrix_s;
+  if (!m) return GDT_ENOMEM;
+  m->ctx = ctx;
+  m->test = *test;
+  m->ansatz = *ansatz;
+  m->stencil = stencil;
+  m->rows = test->size;
+  m->cols = ansatz->size;
+  gdt_status st = build_pattern(ctx, m);
+  if (st != GDT_OK) {
+    gdt_matrix_destroy(m);
+    return st;
+  }
+  *out = m;
+  return GDT_OK;
+}
+
+gdt_status gdt_matrix_destroy(gdt_matrix m) {
+  if (!m) return GDT_EINVAL;
+  if (m->rp) cudaFree(m->rp);
+  if (m->col) cudaFree(m->col);
+  if (m->val) cudaFree(m->val);
+  delete m;
+  return GDT_OK;
+}
+
+int64_t gdt_matrix_rows(gdt_matrix m) { return m ? m->rows : -1; }
+int64_t gdt_matrix_cols(gdt_matrix m) { return m ? m->cols : -1; }
+int64_t gdt_matrix_nnz(gdt_matrix m) { return m ? m->nnz : -1; }
+
+gdt_status gdt_matrix_device_arrays(gdt_matrix m, const int32_t** rp, const int32_t** col, double** val) {
+  if (!m) return GDT_EINVAL;
+  if (rp) *rp = m->rp;
+  if (col) *col = m->col;
+  if (val) *val = m->val;
+  return GDT_OK;
+}
+
+gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m) {
+  if (!ctx || !m) return GDT_EINVAL;
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * m->nnz, ctx->stream));
+  return GDT_OK;
+}
+
+// ------------------------------------------------------------------ assembly ---
+gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs) {
+  if (!ctx || !m || !d) return GDT_EINVAL;
+  if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  return assemble_cg(ctx, m, d, rhs);
+}
+
+gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space s, const gdt_diffusion_desc* d, double* rhs) {
+  if (!ctx || !s || !d || !rhs) return GDT_EINVAL;
+  if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
+  return assemble_cg_rhs(ctx, *s, d, rhs);
+}
+
+gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
+  if (!ctx || !m) return GDT_EINVAL;
+  if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  return dirichlet_apply(ctx, m, rhs);
+}
+
+gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs) {
+  if (!ctx || !m || !d) return GDT_EINVAL;
+  if (m->test.kind != GDT_SPACE_DG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a DG space");
+  if (m->stencil != GDT_STENCIL_ELEMENT_AND_INTERSECTION)
+    return fail(ctx, GDT_ESHAPE, "SWIPDG needs the element_and_intersection stencil");
+  return assemble_swipdg(ctx, m, d, rhs);
+}
+
+gdt_status gdt_spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y) {
+  if (!ctx || !m || !x || !y) return GDT_EINVAL;
+  return spmv(ctx, m, x, y);
+}
+
+gdt_status gdt_solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
+                     gdt_solve_info* info) {
+  if (!ctx || !m || !b || !x || !o) return GDT_EINVAL;
+  if (m->rows != m->cols) return fail(ctx, GDT_ESHAPE, "matrix is not square");
+  if (o->solver != GDT_SOLVER_CG && o->solver != GDT_SOLVER_BICGSTAB) return fail(ctx, GDT_EINVAL, "unknown solver");
+  if (o->precond < GDT_PREC_NONE || o->precond > GDT_PREC_ILU0) return fail(ctx, GDT_EINVAL, "unknown preconditioner");
+  if (o->precision != GDT_PRECISION_FP64 && o->precision != GDT_PRECISION_MIXED)
+    return fail(ctx, GDT_EINVAL, "unknown precision");
+  if (!(o->tol > 0.0) || o->max_iter < 1) return fail(ctx, GDT_EINVAL, "tol must be > 0 and max_iter >= 1");
+  return solve(ctx, m, b, x, o, info);
+}
+
+// ------------------------------------------------------------- finite volume ---
+static gdt_status fv_check(gdt_context ctx, gdt_space s, const gdt_fv_desc* d) {
+  if (!ctx || !s || !d) return GDT_EINVAL;
+  if (s->kind != GDT_SPACE_FV) return fail(ctx, GDT_ESHAPE, "not a finite-volume space");
+  if (!s->g.periodic) return fail(ctx, GDT_EUNSUPPORTED, "finite volumes need a periodic grid");
+  if (d->flux != GDT_FLUX_BURGERS && d->flux != GDT_FLUX_TRANSPORT) return fail(ctx, GDT_EINVAL, "unknown flux");
+  if (d->numflux != GDT_NUMFLUX_LAX_FRIEDRICHS && d->numflux != GDT_NUMFLUX_UPWIND)
+    return fail(ctx, GDT_EINVAL, "unknown numerical flux");
+  return GDT_OK;
+}
+
+gdt_status gdt_fv_apply(gdt_context ctx, gdt_space s, const gdt_fv_desc* d, const double* u, double* range) {
+  GDT_CHECK(ctx, fv_check(ctx, s, d));
+  if (!u || !range) return GDT_EINVAL;
+  return fv_apply(ctx, *s, d, u, range);
+}
+
+gdt_status gdt_fv_estimate_dt(gdt_context ctx, gdt_space s, const gdt_fv_desc* d, const double* u0, double* dt) {
+  GDT_CHECK(ctx, fv_check(ctx, s, d));
+  if (!u0 || !dt) return GDT_EINVAL;
+  return fv_estimate_dt(ctx, *s, d, u0, dt);
+}
+
+gdt_status gdt_fv_timestep(gdt_context ctx, gdt_space s, const gdt_fv_desc* d, int timestepper, double dt,
+                           int64_t steps, int64_t nbatch, double* u, double* work) {
+  GDT_CHECK(ctx, fv_check(ctx, s, d));
+  if (!u || !work || steps < 0 || nbatch < 1) return GDT_EINVAL;
+  if (timestepper != GDT_TIMESTEPPER_EXPLICIT_EULER && timestepper != GDT_TIMESTEPPER_SSPRK2)
+    return fail(ctx, GDT_EINVAL, "unknown time stepper");
+  return fv_timestep(ctx, *s, d, timestepper, dt, steps, nbatch, u, work);
+}
+
+// ------------------------------------------------------------------- adjoint ---
+gdt_status gdt_cg_dlogkappa(gdt_context ctx, gdt_space s, const double* kappa, const double* u, const double* lam,
+                            double* out) {
+  if (!ctx || !s || !kappa || !u || !lam || !out) return GDT_EINVAL;
+  if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
+  return cg_dlogkappa(ctx, *s, kappa, u, lam, out);
+}
+
+gdt_status gdt_swipdg_dlogkappa(gdt_context ctx, gdt_space s, const gdt_ipdg_desc* d, const double* u,
+                                const double* lam, double* out) {
+  if (!ctx || !s || !d || !d->kappa || !u || !lam || !out) return GDT_EINVAL;
+  if (s->kind != GDT_SPACE_DG) return fail(ctx, GDT_ESHAPE, "not a DG space");
+  return swipdg_dlogkappa(ctx, *s, d, u, lam, out);
+}
+
+}  // extern "C"

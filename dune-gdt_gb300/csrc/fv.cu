@@ -1,0 +1,262 @@
+// Finite volumes on periodic structured cube grids (m = 1):
+//   AdvectionFvOperator::apply (operators/advection-fv.hh:66-115) = LocalAdvectionFvCouplingOperator on
+//   every inner/periodic intersection once (local/operators/advection-fv.hh:127-153) with
+//   NumericalLaxFriedrichsFlux (local/numerical-fluxes/lax-friedrichs.hh:61-87) or NumericalUpwindFlux
+//   (upwind.hh:61-73); estimate_dt_for_hyperbolic_system (tools/hyperbolic.hh:38-86); explicit Euler
+//   (test/instationary-eocstudies/base.hh:428-447) and ExplicitRungeKuttaTimeStepper with the SSP2
+//   tableau (tools/timestepper/explicit-rungekutta.hh:82-97, 237-270), r = -1.
+//
+// GB300 design: GB300's FP64 pipe (~0.6e12 instructions/s), not HBM, bounds this update, so the 2D
+// stepper computes every face flux exactly once per stage inside a shared-memory tile (tile + periodic
+// halo staged from global memory), and the second SSP stage fuses u1 = u - dt k0, k1 = L(u1) and
+// u_new = u + (k0 + k1)(-dt/2) into one pass: per step it reads u (twice) and k0 and writes k0 and
+// u_new (40 bytes per cell). LF uses the local speed max(|f'(u)|, |f'(v)|) multiplied in directly
+// (the reference forms 0.5 / (1 / lambda); both agree to rounding).
+#include <cmath>
+#include <limits>
+
+#include <cub/device/device_reduce.cuh>
+
+#include "internal.cuh"
+
+namespace gdt {
+namespace {
+
+struct FvParams {
+  int flux;       // GDT_FLUX_*
+  int numflux;    // GDT_NUMFLUX_*
+  double vel[3];
+  double lf_inv_lambda;  // 0: local LF; else the reference's fixed lambda_ (coefficient 0.5 / lambda_)
+};
+
+__device__ __forceinline__ double f_of(const FvParams& p, double u, int d) {
+  return p.flux == GDT_FLUX_BURGERS ? 0.5 * u * u : p.vel[d] * u;
+}
+__device__ __forceinline__ double df_of(const FvParams& p, double u, int d) {
+  return p.flux == GDT_FLUX_BURGERS ? u : p.vel[d];
+}
+
+// numerical flux across a face with unit normal +e_k, seen from the lower cell (value u) to the upper (v)
+__device__ __forceinline__ double face_flux(const FvParams& p, int dim, int k, double u, double v) {
+  if (p.numflux == GDT_NUMFLUX_LAX_FRIEDRICHS) {
+    double lam;
+    if (p.lf_inv_lambda != 0.0) {
+      lam = 1.0 / p.lf_inv_lambda;  // coefficient (u - v) * 0.5 / lambda_
+    } else if (p.flux == GDT_FLUX_BURGERS) {
+      lam = fmax(fabs(u), fabs(v));
+    } else {
+      lam = 0.0;
+      for (int d = 0; d < dim; ++d) lam = fmax(lam, fabs(p.vel[d]));
+    }
+    const double fsum = f_of(p, u, k) + f_of(p, v, k);
+    return 0.5 * fma(u - v, lam, fsum);
+  }
+  const double w = (u + v) * 0.5;
+  return df_of(p, w, k) > 0.0 ? f_of(p, u, k) : f_of(p, v, k);
+}
+
+// ------------------------------------------------------------------------- generic (any dim) ---
+// range[c] = sum over the 2d faces of c of +-flux * |I| / |E| (periodic neighbours)
+__global__ void fv_apply_kernel(GridDesc g, FvParams p, long long nbatch, const double* __restrict__ u,
+                                double* __restrict__ out, const double* __restrict__ ubase, double a_u1,
+                                int mode, double* __restrict__ u_next, double dt_coef) {
+  // mode 0: out = L(u); mode 1 (Euler): u_next = u - dt L(u); mode 2 (SSP stage 2, u1 = ubase + a_u1 * out):
+  //   u_next = ubase + dt_coef * (k0 + L(u1)) with k0 = out
+  const long long N = g.nelem;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= N * nbatch) return;
+  const long long b = idx / N, c = idx % N;
+  const long long off = b * N;
+  long long ci[3];
+  cell_multi(g, c, ci);
+  auto val = [&](long long cell) -> double {
+    if (mode == 2) return fma(out[off + cell], a_u1, ubase[off + cell]);
+    return u[off + cell];
+  };
+  const double uc = val(c);
+  double acc = 0.0;
+  for (int k = 0; k < g.dim; ++k) {
+    double area = 1.0;
+    for (int j = 0; j < g.dim; ++j)
+      if (j != k) area *= g.h[j];
+    double vol = 1.0;
+    for (int j = 0; j < g.dim; ++j) vol *= g.h[j];
+    const double coef = area / vol;
+    long long cm[3] = {ci[0], ci[1], ci[2]}, cp[3] = {ci[0], ci[1], ci[2]};
+    cm[k] = (ci[k] + g.n[k] - 1) % g.n[k];
+    cp[k] = (ci[k] + 1) % g.n[k];
+    const double um = val(cell_index(g, cm)), up = val(cell_index(g, cp));
+    if (g.n[k] == 1) continue;  // a cell neighbouring itself has no flux
+    acc += coef * (face_flux(p, g.dim, k, uc, up) - face_flux(p, g.dim, k, um, uc));
+  }
+  if (mode == 0) out[off + c] = acc;
+  else if (mode == 1) u_next[off + c] = fma(-dt_coef, acc, u[off + c]);
+  else u_next[off + c] = fma(dt_coef, out[off + c] + acc, ubase[off + c]);
+}
+
+// ------------------------------------------------------------------------------- 2D tiled ---
+constexpr int TX = 32, TY = 32, BY = 8;  // tile TX x TY cells, block TX x BY threads
+
+// STAGE 0: k = L(u) ; STAGE 1 (Euler): u_next = u - dt L(u) ;
+// STAGE 2: u1 = u - dt k0 on the tile + halo, u_next = u + (-dt/2) (k0 + L(u1))
+template <int STAGE>
+__global__ void __launch_bounds__(TX* BY) fv2d_tile(GridDesc g, FvParams p, const double* __restrict__ u,
+                                                    const double* __restrict__ k0, double* __restrict__ out,
+                                                    double dt, double cx, double cy) {
+  __shared__ double s[TY + 2][TX + 3];
+  __shared__ double gx[TY][TX + 1];
+  __shared__ double gy[TY + 1][TX + 1];
+  const long long nx = g.n[0], ny = g.n[1];
+  const long long off = (long long)blockIdx.z * nx * ny;
+  const long long x0 = (long long)blockIdx.x * TX, y0 = (long long)blockIdx.y * TY;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  // stage tile + halo (periodic)
+  for (int j = ty; j < TY + 2; j += BY)
+    for (int i = tx; i < TX + 2; i += TX) {
+      long long gxi = (x0 + i - 1 + nx) % nx, gyj = (y0 + j - 1 + ny) % ny;
+      if (x0 + i - 1 > nx) gxi = nx - 1;  // beyond a partial tile: clamp (values unused)
+      if (y0 + j - 1 > ny) gyj = ny - 1;
+      const long long cidx = off + gyj * nx + gxi;
+      double v = u[cidx];
+      if (STAGE == 2) v = fma(k0[cidx], -dt, v);
+      s[j][i] = v;
+    }
+  __syncthreads();
+  // x faces: between tile columns i-1 and i (i = 0..TX), rows 0..TY-1
+  for (int j = ty; j < TY; j += BY)
+    for (int i = tx; i <= TX; i += TX) gx[j][i] = face_flux(p, 2, 0, s[j + 1][i], s[j + 1][i + 1]);
+  // y faces: between tile rows j-1 and j (j = 0..TY)
+  for (int j = ty; j <= TY; j += BY) gy[j][tx] = face_flux(p, 2, 1, s[j][tx + 1], s[j + 1][tx + 1]);
+  __syncthreads();
+  const long long gxi = x0 + tx;
+  if (gxi >= nx) return;
+  for (int j = ty; j < TY; j += BY) {
+    const long long gyj = y0 + j;
+    if (gyj >= ny) break;
+    const double L = cx * (gx[j][tx + 1] - gx[j][tx]) + cy * (gy[j + 1][tx] - gy[j][tx]);
+    const long long cidx = off + gyj * nx + gxi;
+    if (STAGE == 0) out[cidx] = L;
+    else if (STAGE == 1) out[cidx] = fma(-dt, L, u[cidx]);
+    else out[cidx] = fma(-0.5 * dt, k0[cidx] + L, u[cidx]);
+  }
+}
+
+FvParams make_params(const gdt_fv_desc* d) {
+  FvParams p;
+  p.flux = d->flux;
+  p.numflux = d->numflux;
+  for (int i = 0; i < 3; ++i) p.vel[i] = d->velocity[i];
+  p.lf_inv_lambda = d->lf_lambda;
+  return p;
+}
+
+bool tiled_ok(const GridDesc& g) { return g.dim == 2 && g.n[0] >= 2 && g.n[1] >= 2; }
+
+}  // namespace
+
+gdt_status fv_apply(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc* d, const double* u, double* out) {
+  const GridDesc& g = sp.g;
+  FvParams p = make_params(d);
+  if (tiled_ok(g)) {
+    dim3 grid((unsigned)((g.n[0] + TX - 1) / TX), (unsigned)((g.n[1] + TY - 1) / TY), 1);
+    fv2d_tile<0><<<grid, dim3(TX, BY), 0, ctx->stream>>>(g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
+  } else {
+    fv_apply_kernel<<<grid_blocks(g.nelem, 256), 256, 0, ctx->stream>>>(g, p, 1, u, out, nullptr, 0.0, 0, nullptr,
+                                                                        0.0);
+  }
+  return check_launch(ctx, "fv_apply");
+}
+
+gdt_status fv_estimate_dt(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc* d, const double* u0,
+                          double* dt) {
+  // data range of the (elementwise constant) state, then the reference's formula on the host:
+  // f' sampled at the Gauss points of order flux.order() on [min, max]; dt = 1 / (max |I|/|E| * max |f'|)
+  const GridDesc& g = sp.g;
+  cudaStream_t s = ctx->stream;
+  double* dminmax = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&dminmax, 2 * sizeof(double), s));
+  size_t b1 = 0, b2 = 0;
+  cub::DeviceReduce::Min(nullptr, b1, u0, dminmax, (int)g.nelem, s);
+  cub::DeviceReduce::Max(nullptr, b2, u0, dminmax + 1, (int)g.nelem, s);
+  void* tmp = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&tmp, std::max(b1, b2), s));
+  cub::DeviceReduce::Min(tmp, b1, u0, dminmax, (int)g.nelem, s);
+  cub::DeviceReduce::Max(tmp, b2, u0, dminmax + 1, (int)g.nelem, s);
+  double mm[2];
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(mm, dminmax, sizeof(mm), cudaMemcpyDeviceToHost, s));
+  GDT_TRY_CUDA(ctx, cudaFreeAsync(tmp, s));
+  GDT_TRY_CUDA(ctx, cudaFreeAsync(dminmax, s));
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+  ctx->launches += 4;
+  double data_minimum = std::min(std::numeric_limits<double>::max(), mm[0]);
+  double data_maximum = std::max(std::numeric_limits<double>::min(), mm[1]);
+  if (!(data_minimum < data_maximum)) data_maximum = data_minimum + 1e-6 * data_minimum;
+  double max_df = std::numeric_limits<double>::min();
+  // Gauss points on [0,1]: order 2 (Burgers) -> 2 points, order 1 (transport) -> 1 point
+  const double g2 = 0.5 / std::sqrt(3.0);
+  const double pts2[2] = {0.5 - g2, 0.5 + g2};
+  const double pts1[1] = {0.5};
+  const double* pts = d->flux == GDT_FLUX_BURGERS ? pts2 : pts1;
+  const int npts = d->flux == GDT_FLUX_BURGERS ? 2 : 1;
+  for (int q = 0; q < npts; ++q) {
+    const double uq = data_minimum + (data_maximum - data_minimum) * pts[q];
+    for (int ss = 0; ss < g.dim; ++ss) {
+      const double df = d->flux == GDT_FLUX_BURGERS ? uq : d->velocity[ss];
+      max_df = std::max(max_df, std::fabs(df));
+    }
+  }
+  double vol = 1.0;
+  for (int a = 0; a < g.dim; ++a) vol *= g.h[a];
+  double perimeter = 0.0;
+  for (int k = 0; k < g.dim; ++k) {
+    double area = 1.0;
+    for (int j = 0; j < g.dim; ++j)
+      if (j != k) area *= g.h[j];
+    perimeter += 2 * area;
+  }
+  const double pov = std::max(std::numeric_limits<double>::min(), perimeter / vol);
+  *dt = 1.0 / (pov * max_df);
+  return GDT_OK;
+}
+
+gdt_status fv_timestep(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc* d, int stepper, double dt,
+                       long long steps, long long nbatch, double* u, double* work) {
+  // work holds 2 * nbatch * N doubles for SSP-RK2 (k0 and the next state), nbatch * N for Euler
+  const GridDesc& g = sp.g;
+  const FvParams p = make_params(d);
+  cudaStream_t s = ctx->stream;
+  const long long N = g.nelem * nbatch;
+  double* cur = u;
+  double* nxt = (stepper == GDT_TIMESTEPPER_SSPRK2) ? work + N : work;
+  double* k0 = work;
+  const bool tiled = tiled_ok(g);
+  dim3 grid((unsigned)((g.n[0] + TX - 1) / TX), (unsigned)((g.n[1] + TY - 1) / TY), (unsigned)nbatch);
+  const double cx = 1.0 / g.h[0], cy = g.dim >= 2 ? 1.0 / g.h[1] : 0.0;
+  for (long long st = 0; st < steps; ++st) {
+    if (stepper == GDT_TIMESTEPPER_EXPLICIT_EULER) {
+      if (tiled)
+        fv2d_tile<1><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, nxt, dt, cx, cy);
+      else
+        fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, nullptr, nullptr, 0.0, 1, nxt, dt);
+      ctx->launches++;
+    } else {
+      if (tiled) {
+        fv2d_tile<0><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, k0, dt, cx, cy);
+        fv2d_tile<2><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, k0, nxt, dt, cx, cy);
+      } else {
+        fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, k0, nullptr, 0.0, 0, nullptr, 0.0);
+        fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, nullptr, k0, cur, -dt, 2, nxt, -0.5 * dt);
+      }
+      ctx->launches += 2;
+    }
+    std::swap(cur, nxt);
+  }
+  {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string("fv_timestep: ") + cudaGetErrorString(e));
+  }
+  if (cur != u) GDT_TRY_CUDA(ctx, cudaMemcpyAsync(u, cur, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+  return GDT_OK;
+}
+
+}  // namespace gdt

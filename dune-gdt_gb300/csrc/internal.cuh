@@ -1,0 +1,168 @@
+// Internal declarations of the GB300 discretize-and-solve library (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gdt_gb300.h"
+
+namespace gdt {
+
+constexpr int kMaxDim = 3;
+
+// Structured grid descriptor, passed by value to kernels. Elements: cube index * nsub + sub,
+// cube index and vertex index lexicographic with x fastest (YaspGrid convention).
+struct GridDesc {
+  int dim = 2;
+  int simplex = 0;
+  int periodic = 0;
+  int nsub = 1;  // simplices per cube (d!), 1 for cube grids
+  long long n[3] = {1, 1, 1};
+  long long vn[3] = {1, 1, 1};
+  double lo[3] = {0, 0, 0};
+  double hi[3] = {1, 1, 1};
+  double h[3] = {1, 1, 1};
+  long long ncells = 1, nelem = 1, nvert = 1;
+};
+
+}  // namespace gdt
+
+struct gdt_context_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  long long launches = 0;
+  // small device scratch for reductions and solver scalars
+  double* scratch = nullptr;       // kScratchDoubles doubles
+  unsigned int* counters = nullptr; // kCounters uints (last-block tickets)
+  double* host_pinned = nullptr;   // pinned host mirror for convergence checks
+  int num_sms = 152;
+  // kernel timing: when on, solver iterations run without graph capture and every SpMV launch is
+  // bracketed by CUDA events on the context stream; durations accumulate per precision
+  int timing = 0;
+  std::vector<cudaEvent_t> events;  // pairs (start, stop)
+  std::vector<int> event_kind;      // 0: FP64 SpMV, 1: FP32 SpMV
+  size_t events_used = 0;
+  double spmv_ms[2] = {0, 0};
+  long long spmv_launches[2] = {0, 0};
+};
+
+struct gdt_grid_s {
+  gdt::GridDesc d;
+};
+
+struct gdt_space_s {
+  gdt::GridDesc g;
+  int kind = GDT_SPACE_CG;
+  int order = 1;
+  int lsize = 1;
+  long long size = 0;
+};
+
+struct gdt_matrix_s {
+  gdt_context ctx = nullptr;
+  gdt_space_s test, ansatz;
+  int stencil = GDT_STENCIL_ELEMENT;
+  long long rows = 0, cols = 0, nnz = 0;
+  int* rp = nullptr;
+  int* col = nullptr;
+  double* val = nullptr;
+  int spmv_group = 8;  // lanes per row chosen by the tuner
+};
+
+namespace gdt {
+
+constexpr int kScratchDoubles = 1 << 16;
+constexpr int kCounters = 64;
+
+gdt_status fail(gdt_context ctx, gdt_status s, const std::string& msg);
+gdt_status check_launch(gdt_context ctx, const char* what);
+
+#define GDT_TRY_CUDA(ctx, call)                                                                   \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return ::gdt::fail((ctx), GDT_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define GDT_CHECK(ctx, st)            \
+  do {                                \
+    gdt_status s_ = (st);             \
+    if (s_ != GDT_OK) return s_;      \
+  } while (0)
+
+inline int grid_blocks(long long n, int threads) { return int((n + threads - 1) / threads); }
+
+// kernel timing helpers (capi.cu): bracket one launch; harvest after a stream synchronisation
+void timing_begin(gdt_context ctx, cudaStream_t s, int kind);
+void timing_end(gdt_context ctx, cudaStream_t s);
+void timing_harvest(gdt_context ctx);
+
+// ---------------------------------------------------------------- kernels (host launchers) ---
+// pattern.cu
+gdt_status build_pattern(gdt_context ctx, gdt_matrix m);
+// assemble_cg.cu
+gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs);
+gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& s, const gdt_diffusion_desc* d, double* rhs);
+gdt_status dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs);
+gdt_status cg_dlogkappa(gdt_context ctx, const gdt_space_s& s, const double* kappa, const double* u,
+                        const double* lam, double* out);
+// assemble_ipdg.cu
+gdt_status assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs);
+gdt_status swipdg_dlogkappa(gdt_context ctx, const gdt_space_s& s, const gdt_ipdg_desc* d, const double* u,
+                            const double* lam, double* out);
+// spmv.cu
+gdt_status spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y);
+// krylov.cu
+gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
+                 gdt_solve_info* info);
+// fv.cu
+gdt_status fv_apply(gdt_context ctx, const gdt_space_s& s, const gdt_fv_desc* d, const double* u, double* out);
+gdt_status fv_estimate_dt(gdt_context ctx, const gdt_space_s& s, const gdt_fv_desc* d, const double* u0,
+                          double* dt);
+gdt_status fv_timestep(gdt_context ctx, const gdt_space_s& s, const gdt_fv_desc* d, int stepper, double dt,
+                       long long steps, long long nbatch, double* u, double* work);
+
+// ------------------------------------------------------------------ device helpers ---
+__host__ __device__ inline void vertex_multi(const GridDesc& g, long long v, long long* vi) {
+  vi[0] = v % g.vn[0];
+  vi[1] = (v / g.vn[0]) % g.vn[1];
+  vi[2] = v / (g.vn[0] * g.vn[1]);
+}
+__host__ __device__ inline void cell_multi(const GridDesc& g, long long c, long long* ci) {
+  ci[0] = c % g.n[0];
+  ci[1] = (c / g.n[0]) % g.n[1];
+  ci[2] = c / (g.n[0] * g.n[1]);
+}
+__host__ __device__ inline long long cell_index(const GridDesc& g, const long long* ci) {
+  return ci[0] + g.n[0] * (ci[1] + g.n[1] * ci[2]);
+}
+
+// Deterministic block reduction of NV doubles; result valid in thread 0.
+template <int NV>
+__device__ inline void block_reduce(double (&v)[NV], double* smem /* >= NV * 32 */) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = v[k];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = lane < nw ? smem[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      v[k] = s;
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace gdt

@@ -1,0 +1,827 @@
+// Device-resident Krylov solvers behind ConstMatrixOperator::apply_inverse
+// (operators/matrix-based.hh:131-159). The reference hands this to dune-istl through dune-xt-la
+// (third-party, absent from the reference tree); the algorithms restated here are the published
+// ones: preconditioned CG (Hestenes-Stiefel), BiCGStab (van der Vorst 1992), Jacobi and ILU(0).
+//
+// GB300 design: all scalars (rho, alpha, beta, omega, residual norms, iteration count, converged
+// flag) live in device memory; every reduction finishes in the last block of its kernel (ticketed,
+// fixed summation order: deterministic), so an iteration issues no host synchronisation. Iterations
+// are captured into a CUDA graph in chunks of `check_every`; the host reads the converged flag once
+// per chunk, and kernels of iterations past convergence return immediately.
+// Mixed precision: FP32 inner CG (FP32 CSR values, FP32 vectors, FP32 Jacobi) inside FP64
+// iterative refinement with an FP64 residual r = b - A x from the FP64 matrix.
+#include <cmath>
+#include <vector>
+
+#include "linalg.cuh"
+
+namespace gdt {
+
+template <class T>
+void launch_spmv(int G, int n, const int* rp, const int* col, const T* val, const T* x, T* y, int num_sms,
+                 cudaStream_t s);
+
+namespace {
+
+constexpr int TH = 256;
+
+struct KState {
+  double rho, alpha, beta, omega, rr, rr0, tol2, hden;
+  int iter, max_iter, converged, breakdown;
+};
+
+__device__ __forceinline__ bool stopped(const KState* st) { return *((volatile const int*)&st->converged) != 0; }
+
+// ---------------------------------------------------------------- generic pieces ---
+// y = A x; optional dot(w, y) -> st->hden / alpha (mode 1: CG alpha = rho / (p.Ap); mode 2: BiCGStab
+// alpha = rho / (rt.v); mode 3: two dots (t.s, t.t) -> omega)
+template <int G, class T, int MODE>
+__global__ void __launch_bounds__(TH) k_spmv(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                            const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y,
+                                            const T* __restrict__ w, KState* st, double* partials,
+                                            unsigned int* ticket) {
+  if (stopped(st)) return;
+  const int lane = threadIdx.x & (G - 1);
+  const int rpb = blockDim.x / G;
+  T a0 = T(0), a1 = T(0);
+  for (int row = blockIdx.x * rpb + threadIdx.x / G; row < n; row += gridDim.x * rpb) {
+    T s = csr_row<G, T>(rp[row], rp[row + 1], lane, col, val, x);
+    if (lane == 0) {
+      y[row] = s;
+      if (MODE == 1) a0 = fma(x[row], s, a0);
+      if (MODE == 2) a0 = fma(w[row], s, a0);
+      if (MODE == 3) {
+        a0 = fma(s, w[row], a0);
+        a1 = fma(s, s, a1);
+      }
+    }
+  }
+  if (MODE == 0) return;
+  double v[2] = {double(a0), double(a1)};
+  if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
+    if (MODE == 1) {
+      if (!(v[0] > 0.0) || !isfinite(v[0])) {
+        st->breakdown = 1;
+        st->converged = 1;
+      }
+      st->alpha = st->rho / v[0];
+    } else if (MODE == 2) {
+      if (v[0] == 0.0 || !isfinite(v[0])) {
+        st->breakdown = 1;
+        st->converged = 1;
+      }
+      st->alpha = st->rho / v[0];
+    } else {
+      if (v[1] == 0.0 || !isfinite(v[1])) {
+        st->breakdown = 1;
+        st->converged = 1;
+      }
+      st->omega = v[0] / v[1];
+    }
+  }
+}
+
+// r = b - A x, z = M^{-1} r (Jacobi if dinv, else z = r), p = z (CG start); rho = r.z, rr0 = r.r
+template <int G, class T>
+__global__ void __launch_bounds__(TH) k_residual_init(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                                     const T* __restrict__ val, const T* __restrict__ x,
+                                                     const T* __restrict__ b, T* __restrict__ r,
+                                                     const T* __restrict__ dinv, T* __restrict__ p,
+                                                     KState* st, double* partials, unsigned int* ticket) {
+  const int lane = threadIdx.x & (G - 1);
+  const int rpb = blockDim.x / G;
+  T a0 = T(0), a1 = T(0);
+  for (int row = blockIdx.x * rpb + threadIdx.x / G; row < n; row += gridDim.x * rpb) {
+    T s = csr_row<G, T>(rp[row], rp[row + 1], lane, col, val, x);
+    if (lane == 0) {
+      T ri = b[row] - s;
+      r[row] = ri;
+      T zi = dinv ? dinv[row] * ri : ri;
+      if (p) p[row] = zi;
+      a0 = fma(ri, zi, a0);
+      a1 = fma(ri, ri, a1);
+    }
+  }
+  double v[2] = {double(a0), double(a1)};
+  if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
+    st->rho = v[0];
+    st->rr = v[1];
+    st->rr0 = v[1];
+    st->iter = 0;
+    st->breakdown = 0;
+    st->alpha = st->beta = st->omega = 1.0;
+    st->converged = (v[1] == 0.0 || v[1] <= st->tol2 * v[1]) ? 1 : 0;
+    if (!isfinite(v[1])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
+// x0 = 0 start of the inner FP32 solve: r holds b already; p = dinv r; rho = r.p, rr0 = r.r
+template <class T>
+__global__ void __launch_bounds__(TH) k_init_from_rhs(int n, const T* __restrict__ r, const T* __restrict__ dinv,
+                                                     T* __restrict__ p, KState* st, double* partials,
+                                                     unsigned int* ticket) {
+  T a0 = T(0), a1 = T(0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    T ri = r[i];
+    T zi = dinv[i] * ri;
+    p[i] = zi;
+    a0 = fma(ri, zi, a0);
+    a1 = fma(ri, ri, a1);
+  }
+  double v[2] = {double(a0), double(a1)};
+  if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
+    st->rho = v[0];
+    st->rr = v[1];
+    st->rr0 = v[1];
+    st->iter = 0;
+    st->breakdown = 0;
+    st->alpha = st->beta = st->omega = 1.0;
+    st->converged = (v[1] == 0.0) ? 1 : 0;
+  }
+}
+
+// CG with Jacobi, fused: x += alpha p; r -= alpha q; z = dinv r (not stored); rho' = r.z, rr = r.r
+template <class TX, class T>
+__global__ void __launch_bounds__(TH) k_cg_update_jacobi(int n, TX* __restrict__ x, const T* __restrict__ p,
+                                                        T* __restrict__ r, const T* __restrict__ q,
+                                                        const T* __restrict__ dinv, KState* st, double* partials,
+                                                        unsigned int* ticket) {
+  if (stopped(st)) return;
+  const T alpha = T(st->alpha);
+  T a0 = T(0), a1 = T(0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = TX(fma(alpha, p[i], T(x[i])));
+    T ri = fma(-alpha, q[i], r[i]);
+    r[i] = ri;
+    a0 = fma(ri, dinv[i] * ri, a0);
+    a1 = fma(ri, ri, a1);
+  }
+  double v[2] = {double(a0), double(a1)};
+  if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
+    st->beta = v[0] / st->rho;
+    st->rho = v[0];
+    st->rr = v[1];
+    st->iter += 1;
+    if (v[1] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) st->converged = 1;
+    if (!isfinite(v[1])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(TH) k_cg_p_jacobi(int n, T* __restrict__ p, const T* __restrict__ r,
+                                                   const T* __restrict__ dinv, const KState* st) {
+  if (stopped(st)) return;
+  const T beta = T(st->beta);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = fma(beta, p[i], dinv[i] * r[i]);
+}
+
+// generic CG (any preconditioner): x += alpha p; r -= alpha q; rr = r.r
+__global__ void __launch_bounds__(TH) k_cg_update(int n, double* __restrict__ x, const double* __restrict__ p,
+                                                 double* __restrict__ r, const double* __restrict__ q, KState* st,
+                                                 double* partials, unsigned int* ticket) {
+  if (stopped(st)) return;
+  const double alpha = st->alpha;
+  double a0 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    double ri = fma(-alpha, q[i], r[i]);
+    r[i] = ri;
+    a0 = fma(ri, ri, a0);
+  }
+  double v[1] = {a0};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    st->rr = v[0];
+    st->iter += 1;
+    if (v[0] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) st->converged = 1;
+    if (!isfinite(v[0])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
+// rho' = r.z, beta = rho'/rho (CG)
+__global__ void __launch_bounds__(TH) k_cg_beta(int n, const double* __restrict__ r, const double* __restrict__ z,
+                                               KState* st, double* partials, unsigned int* ticket) {
+  if (stopped(st)) return;
+  double a0 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a0 = fma(r[i], z[i], a0);
+  double v[1] = {a0};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    st->beta = v[0] / st->rho;
+    st->rho = v[0];
+  }
+}
+
+__global__ void __launch_bounds__(TH) k_cg_p(int n, double* __restrict__ p, const double* __restrict__ z,
+                                            const KState* st) {
+  if (stopped(st)) return;
+  const double beta = st->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = fma(beta, p[i], z[i]);
+}
+
+// ---------------------------------------------------------------- BiCGStab pieces ---
+// rho' = rt.r ; beta = (rho'/rho)(alpha/omega) ; p = r + beta (p - omega v) (first iteration: p = r)
+__global__ void __launch_bounds__(TH) k_bicg_rho(int n, const double* __restrict__ rt, const double* __restrict__ r,
+                                                KState* st, double* partials, unsigned int* ticket) {
+  if (stopped(st)) return;
+  double a0 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a0 = fma(rt[i], r[i], a0);
+  double v[1] = {a0};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    if (v[0] == 0.0 || !isfinite(v[0])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+    st->beta = (st->iter == 0) ? 0.0 : (v[0] / st->rho) * (st->alpha / st->omega);
+    st->rho = v[0];
+  }
+}
+
+__global__ void __launch_bounds__(TH) k_bicg_p(int n, double* __restrict__ p, const double* __restrict__ r,
+                                              const double* __restrict__ v, const KState* st) {
+  if (stopped(st)) return;
+  const double beta = st->beta, omega = st->omega;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = fma(beta, fma(-omega, v[i], p[i]), r[i]);
+}
+
+// x += alpha y ; s = r - alpha v ; check ||s|| (if converged: r = s)
+__global__ void __launch_bounds__(TH) k_bicg_s(int n, double* __restrict__ x, const double* __restrict__ y,
+                                              double* __restrict__ r, const double* __restrict__ v, KState* st,
+                                              double* partials, unsigned int* ticket) {
+  if (stopped(st)) return;
+  const double alpha = st->alpha;
+  double a0 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, y[i], x[i]);
+    double si = fma(-alpha, v[i], r[i]);
+    r[i] = si;  // r now holds s
+    a0 = fma(si, si, a0);
+  }
+  double w[1] = {a0};
+  if (grid_reduce<1>(w, partials, ticket) && threadIdx.x == 0) {
+    st->rr = w[0];
+    if (w[0] <= st->tol2 * st->rr0) {
+      st->iter += 1;
+      st->converged = 1;
+    }
+  }
+}
+
+// x += omega z ; r = s - omega t ; rr
+__global__ void __launch_bounds__(TH) k_bicg_r(int n, double* __restrict__ x, const double* __restrict__ z,
+                                              double* __restrict__ r, const double* __restrict__ t, KState* st,
+                                              double* partials, unsigned int* ticket) {
+  if (stopped(st)) return;
+  const double omega = st->omega;
+  double a0 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = fma(omega, z[i], x[i]);
+    double ri = fma(-omega, t[i], r[i]);
+    r[i] = ri;
+    a0 = fma(ri, ri, a0);
+  }
+  double w[1] = {a0};
+  if (grid_reduce<1>(w, partials, ticket) && threadIdx.x == 0) {
+    st->rr = w[0];
+    st->iter += 1;
+    if (w[0] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) st->converged = 1;
+    if (!isfinite(w[0])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
+// ------------------------------------------------------------------- preconditioners ---
+template <class TD, class TS>
+__global__ void k_jacobi_diag(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                              const TS* __restrict__ val, TD* __restrict__ dinv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    TS d = TS(0);
+    for (int k = rp[i]; k < rp[i + 1]; ++k)
+      if (col[k] == i) d = val[k];
+    dinv[i] = TD(1.0 / double(d));
+  }
+}
+
+template <class T>
+__global__ void k_scale(int n, T* __restrict__ z, const T* __restrict__ d, const T* __restrict__ r, const KState* st) {
+  if (stopped(st)) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) z[i] = d ? d[i] * r[i] : r[i];
+}
+
+// ILU(0), level scheduled: rows of one level depend only on rows of earlier levels.
+__global__ void k_ilu_factor_level(const int* __restrict__ rows, int count, const int* __restrict__ rp,
+                                   const int* __restrict__ col, const int* __restrict__ diag, double* __restrict__ lu) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t];
+  const int end_i = rp[i + 1];
+  for (int pk = rp[i]; pk < end_i; ++pk) {
+    const int k = col[pk];
+    if (k >= i) break;
+    const double lik = lu[pk] / lu[diag[k]];
+    lu[pk] = lik;
+    int pi = pk + 1;
+    for (int pj = diag[k] + 1; pj < rp[k + 1]; ++pj) {
+      const int j = col[pj];
+      while (pi < end_i && col[pi] < j) ++pi;
+      if (pi < end_i && col[pi] == j) lu[pi] -= lik * lu[pj];
+    }
+  }
+}
+
+__global__ void k_ilu_lower_level(const int* __restrict__ rows, int count, const int* __restrict__ rp,
+                                  const int* __restrict__ col, const int* __restrict__ diag,
+                                  const double* __restrict__ lu, const double* __restrict__ r, double* __restrict__ z,
+                                  const KState* st) {
+  if (stopped(st)) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t];
+  double s = r[i];
+  for (int p = rp[i]; p < diag[i]; ++p) s -= lu[p] * z[col[p]];
+  z[i] = s;
+}
+
+__global__ void k_ilu_upper_level(const int* __restrict__ rows, int count, const int* __restrict__ rp,
+                                  const int* __restrict__ col, const int* __restrict__ diag,
+                                  const double* __restrict__ lu, double* __restrict__ z, const KState* st) {
+  if (stopped(st)) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = rows[t];
+  double s = z[i];
+  for (int p = diag[i] + 1; p < rp[i + 1]; ++p) s -= lu[p] * z[col[p]];
+  z[i] = s / lu[diag[i]];
+}
+
+__global__ void k_find_diag(int n, const int* __restrict__ rp, const int* __restrict__ col, int* __restrict__ diag) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int d = -1;
+    for (int k = rp[i]; k < rp[i + 1]; ++k)
+      if (col[k] == i) d = k;
+    diag[i] = d;
+  }
+}
+
+// -------------------------------------------------------------- mixed precision helpers ---
+__global__ void k_to_float(long long n, const double* __restrict__ a, float* __restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = float(a[i]);
+}
+
+// r64 = b - A x (FP64) ; rr = r.r ; r32 = r64 * inv_scale where inv_scale = 1/||r|| is applied on the host side
+template <int G>
+__global__ void __launch_bounds__(TH) k_residual64(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                                  const double* __restrict__ val, const double* __restrict__ x,
+                                                  const double* __restrict__ b, double* __restrict__ r,
+                                                  double* out_rr, double* partials, unsigned int* ticket) {
+  const int lane = threadIdx.x & (G - 1);
+  const int rpb = blockDim.x / G;
+  double a0 = 0.0;
+  for (int row = blockIdx.x * rpb + threadIdx.x / G; row < n; row += gridDim.x * rpb) {
+    double s = csr_row<G, double>(rp[row], rp[row + 1], lane, col, val, x);
+    if (lane == 0) {
+      double ri = b[row] - s;
+      r[row] = ri;
+      a0 = fma(ri, ri, a0);
+    }
+  }
+  double v[1] = {a0};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) *out_rr = v[0];
+}
+
+__global__ void k_scale_to_float(int n, const double* __restrict__ r, const double* __restrict__ rr,
+                                 float* __restrict__ r32) {
+  const double inv = 1.0 / sqrt(*rr);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) r32[i] = float(r[i] * inv);
+}
+
+__global__ void k_correct(int n, double* __restrict__ x, const float* __restrict__ d, const double* __restrict__ rr) {
+  const double scale = sqrt(*rr);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = fma(scale, double(d[i]), x[i]);
+}
+
+// ---------------------------------------------------------------------------- host ---
+struct Launch {
+  gdt_context ctx;
+  int n;
+  int G;
+  int vec_blocks;
+  int spmv_blocks;
+  cudaStream_t s;
+  double* partials;
+  unsigned int* ticket;
+};
+
+template <class T, int MODE>
+void spmv_mode(const Launch& L, const int* rp, const int* col, const T* val, const T* x, T* y, const T* w,
+               KState* st) {
+  timing_begin(L.ctx, L.s, sizeof(T) == 8 ? 0 : 1);
+  struct End {
+    const Launch& L;
+    ~End() { timing_end(L.ctx, L.s); }
+  } end{L};
+  switch (L.G) {
+    case 2: k_spmv<2, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
+    case 4: k_spmv<4, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
+    case 8: k_spmv<8, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
+    case 16: k_spmv<16, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
+    default: k_spmv<32, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
+  }
+  L.ctx->launches++;
+}
+
+template <class T>
+void residual_init(const Launch& L, const int* rp, const int* col, const T* val, const T* x, const T* b, T* r,
+                   const T* dinv, T* p, KState* st) {
+  switch (L.G) {
+    case 2: k_residual_init<2, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
+    case 4: k_residual_init<4, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
+    case 8: k_residual_init<8, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
+    case 16: k_residual_init<16, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
+    default: k_residual_init<32, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
+  }
+  L.ctx->launches++;
+}
+
+void residual64(const Launch& L, gdt_matrix m, const double* x, const double* b, double* r, double* rr) {
+  switch (L.G) {
+    case 2: k_residual64<2><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
+    case 4: k_residual64<4><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
+    case 8: k_residual64<8><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
+    case 16: k_residual64<16><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
+    default: k_residual64<32><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
+  }
+  L.ctx->launches++;
+}
+
+// level sets of the lower (U = false) or upper (U = true) triangle, computed on the host from the pattern
+void level_sets(int n, const std::vector<int>& rp, const std::vector<int>& col, bool upper, std::vector<int>& order,
+                std::vector<int>& offsets) {
+  std::vector<int> lev(n, 0);
+  int maxl = 0;
+  if (!upper) {
+    for (int i = 0; i < n; ++i) {
+      int l = 0;
+      for (int k = rp[i]; k < rp[i + 1] && col[k] < i; ++k) l = std::max(l, lev[col[k]] + 1);
+      lev[i] = l;
+      maxl = std::max(maxl, l);
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      int l = 0;
+      for (int k = rp[i + 1] - 1; k >= rp[i] && col[k] > i; --k) l = std::max(l, lev[col[k]] + 1);
+      lev[i] = l;
+      maxl = std::max(maxl, l);
+    }
+  }
+  offsets.assign(maxl + 2, 0);
+  for (int i = 0; i < n; ++i) offsets[lev[i] + 1]++;
+  for (int l = 0; l <= maxl; ++l) offsets[l + 1] += offsets[l];
+  order.resize(n);
+  std::vector<int> fill(offsets.begin(), offsets.end() - 1);
+  for (int i = 0; i < n; ++i) order[fill[lev[i]]++] = i;
+}
+
+struct Ilu {
+  double* lu = nullptr;
+  int* diag = nullptr;
+  int* lorder = nullptr;
+  int* uorder = nullptr;
+  std::vector<int> loff, uoff;
+};
+
+gdt_status ilu_setup(gdt_context ctx, gdt_matrix m, Ilu& f, cudaStream_t s) {
+  const int n = int(m->rows);
+  std::vector<int> rp(n + 1), col(m->nnz);
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(rp.data(), m->rp, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(col.data(), m->col, sizeof(int) * m->nnz, cudaMemcpyDeviceToHost, s));
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+  std::vector<int> lo, uo;
+  level_sets(n, rp, col, false, lo, f.loff);
+  level_sets(n, rp, col, true, uo, f.uoff);
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&f.lu, sizeof(double) * m->nnz, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&f.diag, sizeof(int) * n, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&f.lorder, sizeof(int) * n, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&f.uorder, sizeof(int) * n, s));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(f.lorder, lo.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(f.uorder, uo.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(f.lu, m->val, sizeof(double) * m->nnz, cudaMemcpyDeviceToDevice, s));
+  k_find_diag<<<grid_blocks(n, TH), TH, 0, s>>>(n, m->rp, m->col, f.diag);
+  GDT_CHECK(ctx, check_launch(ctx, "ilu diag"));
+  for (size_t l = 0; l + 1 < f.loff.size(); ++l) {
+    int cnt = f.loff[l + 1] - f.loff[l];
+    k_ilu_factor_level<<<grid_blocks(cnt, 128), 128, 0, s>>>(f.lorder + f.loff[l], cnt, m->rp, m->col, f.diag, f.lu);
+    GDT_CHECK(ctx, check_launch(ctx, "ilu factor"));
+  }
+  // keep the host copies alive until the asynchronous uploads have completed
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+  return GDT_OK;
+}
+
+void ilu_apply(gdt_context ctx, gdt_matrix m, const Ilu& f, const double* r, double* z, const KState* st,
+               cudaStream_t s) {
+  for (size_t l = 0; l + 1 < f.loff.size(); ++l) {
+    int cnt = f.loff[l + 1] - f.loff[l];
+    k_ilu_lower_level<<<grid_blocks(cnt, 128), 128, 0, s>>>(f.lorder + f.loff[l], cnt, m->rp, m->col, f.diag, f.lu, r,
+                                                            z, st);
+    ctx->launches++;
+  }
+  for (size_t l = 0; l + 1 < f.uoff.size(); ++l) {
+    int cnt = f.uoff[l + 1] - f.uoff[l];
+    k_ilu_upper_level<<<grid_blocks(cnt, 128), 128, 0, s>>>(f.uorder + f.uoff[l], cnt, m->rp, m->col, f.diag, f.lu, z,
+                                                            st);
+    ctx->launches++;
+  }
+}
+
+// Runs `body` (one iteration's launches) in graph-captured chunks until the device flag says stop.
+template <class Body>
+gdt_status iterate(gdt_context ctx, cudaStream_t s, KState* st, int chunk, int max_chunks, Body body) {
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  bool use_graph = true;
+  // launches recorded while capturing run once per graph launch: count them there
+  const long long before = ctx->launches;
+  if (ctx->timing) {
+    use_graph = false;  // per-launch events need plain launches
+  } else if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    for (int k = 0; k < chunk; ++k) body();
+    if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
+        cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+      use_graph = false;
+  } else {
+    use_graph = false;
+  }
+  const long long per_chunk = ctx->launches - before;
+  ctx->launches = before;
+  cudaGetLastError();
+  int* flag = reinterpret_cast<int*>(ctx->host_pinned);
+  for (int c = 0; c < max_chunks; ++c) {
+    if (use_graph) {
+      GDT_TRY_CUDA(ctx, cudaGraphLaunch(exec, s));
+      ctx->launches += per_chunk;
+    } else {
+      for (int k = 0; k < chunk; ++k) body();
+    }
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(flag, &st->converged, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+    if (ctx->timing) timing_harvest(ctx);
+    if (*flag) break;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  return GDT_OK;
+}
+
+}  // namespace
+
+gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
+                 gdt_solve_info* info) {
+  cudaStream_t s = ctx->stream;
+  cudaStream_t own = nullptr;
+  if (s == nullptr) {  // the legacy stream cannot be captured; use a blocking stream ordered with it
+    GDT_TRY_CUDA(ctx, cudaStreamCreate(&own));
+    s = own;
+  }
+  struct Cleanup {
+    cudaStream_t st;
+    ~Cleanup() {
+      if (st) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+      }
+    }
+  } cleanup{own};
+  const int n = int(m->rows);
+  Launch L;
+  L.ctx = ctx;
+  L.n = n;
+  L.G = m->spmv_group;
+  L.s = s;
+  L.vec_blocks = std::max(1, std::min(grid_blocks(n, TH), ctx->num_sms * 8));
+  L.spmv_blocks = std::max(1, std::min(grid_blocks((long long)n * L.G, TH), ctx->num_sms * 8));
+  L.partials = ctx->scratch;
+  L.ticket = ctx->counters;
+  const int chunk = o->check_every > 0 ? o->check_every : 32;
+  const bool mixed = o->precision == GDT_PRECISION_MIXED;
+  if (mixed && (o->solver != GDT_SOLVER_CG || o->precond == GDT_PREC_ILU0))
+    return fail(ctx, GDT_EUNSUPPORTED, "mixed precision is provided for CG with Jacobi or no preconditioner");
+  KState* st = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&st, sizeof(KState), s));
+  KState init{};
+  init.tol2 = o->tol * o->tol;
+  init.max_iter = o->max_iter;
+  std::vector<void*> allocs;
+  allocs.push_back(st);
+  auto alloc = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMallocAsync(&p, bytes, s) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return p;
+  };
+  struct Freer {
+    std::vector<void*>* a;
+    cudaStream_t s;
+    ~Freer() {
+      for (void* p : *a) cudaFreeAsync(p, s);
+    }
+  } freer{&allocs, s};
+  gdt_solve_info res{};
+  if (!mixed) {
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(st, &init, sizeof(KState), cudaMemcpyHostToDevice, s));
+    const size_t vb = sizeof(double) * std::max(n, 1);
+    double* r = (double*)alloc(vb);
+    double* p = (double*)alloc(vb);
+    double* q = (double*)alloc(vb);
+    double* dinv = nullptr;
+    if (!r || !p || !q) return fail(ctx, GDT_ENOMEM, "solver vectors");
+    if (o->precond == GDT_PREC_JACOBI) {
+      dinv = (double*)alloc(vb);
+      if (!dinv) return fail(ctx, GDT_ENOMEM, "solver vectors");
+      k_jacobi_diag<double, double><<<L.vec_blocks, TH, 0, s>>>(n, m->rp, m->col, m->val, dinv);
+      GDT_CHECK(ctx, check_launch(ctx, "jacobi"));
+    }
+    Ilu ilu;
+    if (o->precond == GDT_PREC_ILU0) {
+      GDT_CHECK(ctx, ilu_setup(ctx, m, ilu, s));
+      allocs.push_back(ilu.lu);
+      allocs.push_back(ilu.diag);
+      allocs.push_back(ilu.lorder);
+      allocs.push_back(ilu.uorder);
+    }
+    const int chunk_used = (o->precond == GDT_PREC_ILU0) ? std::min(chunk, 2) : chunk;
+    const int max_chunks = o->max_iter / chunk_used + 2;
+    if (o->solver == GDT_SOLVER_CG) {
+      if (o->precond != GDT_PREC_ILU0) {
+        // fused Jacobi (or identity) path
+        double* one = dinv;
+        if (!one) {
+          one = (double*)alloc(vb);
+          if (!one) return fail(ctx, GDT_ENOMEM, "solver vectors");
+          std::vector<double> ones(n, 1.0);
+          GDT_TRY_CUDA(ctx, cudaMemcpyAsync(one, ones.data(), vb, cudaMemcpyHostToDevice, s));
+          GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+        }
+        residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
+        GDT_CHECK(ctx, iterate(ctx, s, st, chunk_used, max_chunks, [&] {
+          spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
+          k_cg_update_jacobi<double, double><<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);
+          k_cg_p_jacobi<double><<<L.vec_blocks, TH, 0, s>>>(n, p, r, one, st);
+          ctx->launches += 2;
+        }));
+      } else {
+        double* z = (double*)alloc(vb);
+        if (!z) return fail(ctx, GDT_ENOMEM, "solver vectors");
+        residual_init<double>(L, m->rp, m->col, m->val, x, b, r, nullptr, nullptr, st);
+        ilu_apply(ctx, m, ilu, r, z, st, s);
+        // rho = r.z, p = z
+        k_cg_beta<<<L.vec_blocks, TH, 0, s>>>(n, r, z, st, L.partials, L.ticket);
+        GDT_TRY_CUDA(ctx, cudaMemcpyAsync(p, z, vb, cudaMemcpyDeviceToDevice, s));
+        ctx->launches++;
+        GDT_CHECK(ctx, iterate(ctx, s, st, chunk_used, max_chunks, [&] {
+          spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
+          k_cg_update<<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, st, L.partials, L.ticket);
+          ilu_apply(ctx, m, ilu, r, z, st, s);
+          k_cg_beta<<<L.vec_blocks, TH, 0, s>>>(n, r, z, st, L.partials, L.ticket);
+          k_cg_p<<<L.vec_blocks, TH, 0, s>>>(n, p, z, st);
+          ctx->launches += 3;
+        }));
+      }
+    } else {
+      // BiCGStab with M = Jacobi / ILU0 / identity
+      double* rt = (double*)alloc(vb);
+      double* v = (double*)alloc(vb);
+      double* y = (double*)alloc(vb);
+      double* t = (double*)alloc(vb);
+      if (!rt || !v || !y || !t) return fail(ctx, GDT_ENOMEM, "solver vectors");
+      GDT_TRY_CUDA(ctx, cudaMemsetAsync(v, 0, vb, s));
+      GDT_TRY_CUDA(ctx, cudaMemsetAsync(p, 0, vb, s));
+      residual_init<double>(L, m->rp, m->col, m->val, x, b, r, nullptr, nullptr, st);
+      GDT_TRY_CUDA(ctx, cudaMemcpyAsync(rt, r, vb, cudaMemcpyDeviceToDevice, s));
+      auto prec = [&](const double* in, double* out) {
+        if (o->precond == GDT_PREC_ILU0) ilu_apply(ctx, m, ilu, in, out, st, s);
+        else {
+          k_scale<double><<<L.vec_blocks, TH, 0, s>>>(n, out, dinv, in, st);
+          ctx->launches++;
+        }
+      };
+      GDT_CHECK(ctx, iterate(ctx, s, st, chunk_used, max_chunks, [&] {
+        k_bicg_rho<<<L.vec_blocks, TH, 0, s>>>(n, rt, r, st, L.partials, L.ticket);
+        k_bicg_p<<<L.vec_blocks, TH, 0, s>>>(n, p, r, v, st);
+        prec(p, y);
+        spmv_mode<double, 2>(L, m->rp, m->col, m->val, y, v, rt, st);
+        k_bicg_s<<<L.vec_blocks, TH, 0, s>>>(n, x, y, r, v, st, L.partials, L.ticket);
+        prec(r, q);  // q = M^{-1} s
+        spmv_mode<double, 3>(L, m->rp, m->col, m->val, q, t, r, st);
+        k_bicg_r<<<L.vec_blocks, TH, 0, s>>>(n, x, q, r, t, st, L.partials, L.ticket);
+        ctx->launches += 4;
+      }));
+    }
+    KState fin;
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fin, st, sizeof(KState), cudaMemcpyDeviceToHost, s));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+    {
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string("krylov: ") + cudaGetErrorString(e));
+    }
+    // report the true FP64 residual of the returned iterate
+    residual64(L, m, x, b, r, L.partials + kScratchDoubles - 1);
+    double rr_true = 0;
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&rr_true, L.partials + kScratchDoubles - 1, sizeof(double),
+                                      cudaMemcpyDeviceToHost, s));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+    res.iterations = fin.iter;
+    res.refinements = 0;
+    res.rel_residual = fin.rr0 > 0 ? std::sqrt(rr_true / fin.rr0) : 0.0;
+    res.converged = (fin.breakdown == 0) && (fin.rr0 == 0 || fin.rr <= fin.tol2 * fin.rr0);
+  } else {
+    // ---------------------------------------------------- FP64 iterative refinement, FP32 inner CG
+    const size_t vb = sizeof(double) * std::max(n, 1), fb = sizeof(float) * std::max(n, 1);
+    double* r = (double*)alloc(vb);
+    float* val32 = (float*)alloc(sizeof(float) * std::max<long long>(m->nnz, 1));
+    float* r32 = (float*)alloc(fb);
+    float* d32 = (float*)alloc(fb);
+    float* p32 = (float*)alloc(fb);
+    float* q32 = (float*)alloc(fb);
+    float* dinv32 = (float*)alloc(fb);
+    double* scal = (double*)alloc(sizeof(double) * 4);
+    if (!r || !val32 || !r32 || !d32 || !p32 || !q32 || !dinv32 || !scal) return fail(ctx, GDT_ENOMEM, "solver vectors");
+    k_to_float<<<ctx->num_sms * 8, TH, 0, s>>>(m->nnz, m->val, val32);
+    ctx->launches++;
+    if (o->precond == GDT_PREC_JACOBI)
+      k_jacobi_diag<float, double><<<L.vec_blocks, TH, 0, s>>>(n, m->rp, m->col, m->val, dinv32);
+    else {
+      std::vector<float> ones(n, 1.0f);
+      GDT_TRY_CUDA(ctx, cudaMemcpyAsync(dinv32, ones.data(), fb, cudaMemcpyHostToDevice, s));
+      GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+    }
+    ctx->launches++;
+    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-3;
+    double rr0 = -1.0, rr = 0.0;
+    int total_iter = 0, refinements = 0;
+    bool ok = false;
+    double* rr_dev = scal;
+    for (int outer = 0; outer < 200; ++outer) {
+      residual64(L, m, x, b, r, rr_dev);
+      GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&rr, rr_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+      if (rr0 < 0) rr0 = rr;
+      if (!std::isfinite(rr)) break;
+      if (rr <= o->tol * o->tol * rr0 || rr == 0.0) {
+        ok = true;
+        break;
+      }
+      if (total_iter >= o->max_iter) break;
+      // inner: A d = r / ||r|| in FP32, d0 = 0
+      k_scale_to_float<<<L.vec_blocks, TH, 0, s>>>(n, r, rr_dev, r32);
+      GDT_TRY_CUDA(ctx, cudaMemsetAsync(d32, 0, fb, s));
+      KState in = init;
+      in.tol2 = inner_tol * inner_tol;
+      in.max_iter = std::max(1, o->max_iter - total_iter);
+      GDT_TRY_CUDA(ctx, cudaMemcpyAsync(st, &in, sizeof(KState), cudaMemcpyHostToDevice, s));
+      k_init_from_rhs<float><<<L.vec_blocks, TH, 0, s>>>(n, r32, dinv32, p32, st, L.partials, L.ticket);
+      ctx->launches += 2;
+      GDT_CHECK(ctx, iterate(ctx, s, st, chunk, in.max_iter / chunk + 2, [&] {
+        spmv_mode<float, 1>(L, m->rp, m->col, val32, p32, q32, nullptr, st);
+        k_cg_update_jacobi<float, float><<<L.vec_blocks, TH, 0, s>>>(n, d32, p32, r32, q32, dinv32, st, L.partials,
+                                                                     L.ticket);
+        k_cg_p_jacobi<float><<<L.vec_blocks, TH, 0, s>>>(n, p32, r32, dinv32, st);
+        ctx->launches += 2;
+      }));
+      KState fin;
+      GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fin, st, sizeof(KState), cudaMemcpyDeviceToHost, s));
+      GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+      total_iter += fin.iter;
+      k_correct<<<L.vec_blocks, TH, 0, s>>>(n, x, d32, rr_dev);
+      ctx->launches++;
+      refinements++;
+      if (fin.breakdown) break;
+    }
+    {
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string("mixed krylov: ") + cudaGetErrorString(e));
+    }
+    res.iterations = total_iter;
+    res.refinements = refinements;
+    res.rel_residual = rr0 > 0 ? std::sqrt(rr / rr0) : 0.0;
+    res.converged = ok ? 1 : 0;
+  }
+  if (info) *info = res;
+  if (!res.converged) return fail(ctx, GDT_ENOCONV, "linear solver did not converge");
+  return GDT_OK;
+}
+
+}  // namespace gdt

@@ -1,0 +1,206 @@
+/* gdt_gb300.h — C ABI of the GB300-native discretize-and-solve library.
+ *
+ * Plain pointers and sizes only. Vectors and coefficient arrays are caller-owned DEVICE pointers
+ * (FP64 unless stated); grids, spaces, matrices and contexts are opaque library-owned handles.
+ * Every entry point returns a gdt_status (the reference's exception classes, exceptions.hh:21-76,
+ * become status codes); gdt_context_last_error() gives the message. The library is
+ * stream-ordered: all work of a context runs on the context's CUDA stream. It is thread-safe
+ * across contexts and not re-entrant per context.
+ *
+ * Reference interfaces replaced (paths inside the dune-gdt tree):
+ *   grid + spaces      make_cube_grid + make_{continuous_lagrange,discontinuous_lagrange,
+ *                      finite_volume}_space  (spaces/h1/continuous-lagrange.hh:189-203,
+ *                      spaces/l2/discontinuous-lagrange.hh:191-205, spaces/l2/finite-volume.hh:209-229)
+ *   mappers            ContinuousMapper::global_indices (spaces/mapper/continuous.hh:139-150),
+ *                      DiscontinuousMapper (spaces/mapper/discontinuous.hh:102-125),
+ *                      FiniteVolumeMapper (spaces/mapper/finite-volume.hh:101-107)
+ *   pattern + matrix   make_sparsity_pattern (tools/sparsity-pattern.hh:162-178),
+ *                      make_matrix_operator(space, Stencil) (operators/matrix-based.hh:650-658)
+ *   assembly           MatrixOperator::append/assemble (operators/matrix-based.hh:346-408, 496-500)
+ *                      with LocalElementIntegralBilinearForm(LocalLaplaceIntegrand)
+ *                      (local/bilinear-forms/integrals.hh:97-134, local/integrands/laplace.hh:81-102),
+ *                      VectorBasedFunctional with LocalElementProductIntegrand().with_ansatz(f)
+ *                      (functionals/vector-based.hh:214-222, local/functionals/integrals.hh:72-98),
+ *                      DirichletConstraints::apply (tools/dirichlet-constraints.hh:153-184),
+ *                      SWIPDG coupling/penalty forms (local/integrands/laplace-ipdg.hh:107-186,
+ *                      331-368; local/integrands/ipdg.hh:113-171, 254-282)
+ *   apply / solve      ConstMatrixOperator::apply / apply_inverse (operators/matrix-based.hh:121-159)
+ *   finite volumes     AdvectionFvOperator::apply (operators/advection-fv.hh:66-115,
+ *                      local/operators/advection-fv.hh:127-153) with NumericalLaxFriedrichsFlux /
+ *                      NumericalUpwindFlux (local/numerical-fluxes/lax-friedrichs.hh:61-87, upwind.hh:61-73),
+ *                      estimate_dt_for_hyperbolic_system (tools/hyperbolic.hh:38-86),
+ *                      ExplicitRungeKuttaTimeStepper::step (tools/timestepper/explicit-rungekutta.hh:237-270)
+ */
+#ifndef GDT_GB300_H
+#define GDT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gdt_status {
+  GDT_OK = 0,
+  GDT_EINVAL = 1,       /* invalid argument (null handle, bad enum, bad size) */
+  GDT_ESHAPE = 2,       /* shape mismatch (cf. operators/matrix-based.hh:73-80) */
+  GDT_ENOCONV = 3,      /* Krylov solver did not converge (cf. operators/matrix-based.hh:155-158) */
+  GDT_ETIMEOUT = 4,     /* a device-side wait ran out of its iteration budget */
+  GDT_ENAN = 5,         /* non-finite value detected */
+  GDT_EUNSUPPORTED = 6, /* form / element / grid combination not provided by the GPU library */
+  GDT_ECUDA = 7,        /* CUDA runtime error */
+  GDT_ENOMEM = 8        /* device allocation failed */
+} gdt_status;
+
+typedef struct gdt_context_s* gdt_context;
+typedef struct gdt_grid_s* gdt_grid;
+typedef struct gdt_space_s* gdt_space;
+typedef struct gdt_matrix_s* gdt_matrix;
+
+enum { GDT_SPACE_CG = 0, GDT_SPACE_DG = 1, GDT_SPACE_FV = 2 };
+enum { GDT_STENCIL_ELEMENT = 0, GDT_STENCIL_INTERSECTION = 1, GDT_STENCIL_ELEMENT_AND_INTERSECTION = 2 };
+enum { GDT_SOLVER_CG = 0, GDT_SOLVER_BICGSTAB = 1 };
+enum { GDT_PREC_NONE = 0, GDT_PREC_JACOBI = 1, GDT_PREC_ILU0 = 2 };
+enum { GDT_PRECISION_FP64 = 0, GDT_PRECISION_MIXED = 1 };
+enum { GDT_FLUX_BURGERS = 0, GDT_FLUX_TRANSPORT = 1 };
+enum { GDT_NUMFLUX_LAX_FRIEDRICHS = 0, GDT_NUMFLUX_UPWIND = 1 };
+enum { GDT_TIMESTEPPER_EXPLICIT_EULER = 0, GDT_TIMESTEPPER_SSPRK2 = 1 };
+
+/* ------------------------------------------------------------------ context --- */
+/* device: CUDA ordinal; stream: a cudaStream_t (NULL = the legacy default stream). */
+gdt_status gdt_context_create(int device, void* stream, gdt_context* out);
+gdt_status gdt_context_destroy(gdt_context ctx);
+gdt_status gdt_context_set_stream(gdt_context ctx, void* stream);
+gdt_status gdt_context_synchronize(gdt_context ctx);
+const char* gdt_context_last_error(gdt_context ctx);
+const char* gdt_status_string(gdt_status s);
+/* number of kernels this library launched on the context since creation */
+int64_t gdt_context_kernel_launches(gdt_context ctx);
+/* kernel timing (tracing aid, no reference counterpart beyond Dune::Timer around solves,
+ * test/stationary-eocstudies/base.hh:221-225): while enabled, solver iterations are launched without
+ * graph capture and every SpMV launch is bracketed by CUDA events on the context stream. */
+gdt_status gdt_context_set_timing(gdt_context ctx, int enable);
+/* accumulated SpMV kernel time (ms) and launch counts since the last reset, FP64 and FP32 separately */
+gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp64_launches, double* fp32_ms,
+                                   int64_t* fp32_launches, int reset);
+
+/* --------------------------------------------------------------------- grid --- */
+/* make_cube_grid(lower_left, upper_right, num_elements): equidistant YaspGrid-like cube grid
+ * (elements and vertices lexicographic, x fastest) or its Kuhn split into d! simplices per cube
+ * (element = cube * d! + permutation in std::next_permutation order). dim in {1,2,3}. */
+gdt_status gdt_grid_create_cube(int dim, const int64_t* num_elements, const double* lower_left,
+                                const double* upper_right, int simplex, int periodic, gdt_grid* out);
+gdt_status gdt_grid_destroy(gdt_grid grid);
+int64_t gdt_grid_num_elements(gdt_grid grid);
+int64_t gdt_grid_num_vertices(gdt_grid grid);
+
+/* -------------------------------------------------------------------- space --- */
+/* kind: GDT_SPACE_CG (order 1), GDT_SPACE_DG (order 1), GDT_SPACE_FV (order 0, m = 1). */
+gdt_status gdt_space_create(gdt_grid grid, int kind, int order, gdt_space* out);
+gdt_status gdt_space_destroy(gdt_space space);
+int64_t gdt_space_size(gdt_space space);
+int gdt_space_max_local_size(gdt_space space);
+/* mapper.global_indices of every element into a DEVICE int64 array [num_elements][local_size] */
+gdt_status gdt_space_global_indices(gdt_context ctx, gdt_space space, int64_t* out_dev);
+
+/* ------------------------------------------------------------------- matrix --- */
+/* builds the sorted CSR sparsity pattern on the device; values start at zero.
+ * row_ptr and col are int32 (nnz < 2^31). */
+gdt_status gdt_matrix_create(gdt_context ctx, gdt_space test_space, gdt_space ansatz_space, int stencil,
+                             gdt_matrix* out);
+gdt_status gdt_matrix_destroy(gdt_matrix m);
+int64_t gdt_matrix_rows(gdt_matrix m);
+int64_t gdt_matrix_cols(gdt_matrix m);
+int64_t gdt_matrix_nnz(gdt_matrix m);
+gdt_status gdt_matrix_device_arrays(gdt_matrix m, const int32_t** row_ptr, const int32_t** col, double** val);
+gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m);
+
+/* ----------------------------------------------------------------- assembly --- */
+typedef struct gdt_diffusion_desc {
+  const double* kappa;   /* device, one scalar diffusion value per element, or NULL */
+  double kappa_const;    /* used when kappa == NULL */
+  const double* force;   /* device, one source value per element, or NULL */
+  double force_const;    /* used when force == NULL */
+  int dirichlet;         /* 1: all-Dirichlet boundary, homogeneous (unit row + col, rhs = 0) */
+} gdt_diffusion_desc;
+
+/* continuous Lagrange: stiffness of LocalLaplaceIntegrand(kappa) into m, and (if rhs != NULL) the
+ * load vector of LocalElementProductIntegrand().with_ansatz(force); Dirichlet constraints fused. */
+gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* desc, double* rhs);
+
+/* load vector only (VectorBasedFunctional::assemble, functionals/vector-based.hh:276-279); with
+ * desc->dirichlet the Dirichlet entries are set to zero (DirichletConstraints::apply(V)). */
+gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space cg, const gdt_diffusion_desc* desc, double* rhs);
+/* DirichletConstraints::apply(M, V) (tools/dirichlet-constraints.hh:153-184) on an assembled
+ * matrix of a continuous space, all-Dirichlet boundary: unit_col + unit_row, rhs[D] = 0 (rhs may be NULL). */
+gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs);
+
+typedef struct gdt_ipdg_desc {
+  const double* kappa;   /* device, per element, or NULL */
+  double kappa_const;
+  const double* force;   /* device, per element, or NULL */
+  double force_const;
+  double symmetry_prefactor; /* 1 SIPDG/SWIPDG, 0 IIPDG, -1 NIPDG */
+  double sigma_inner;        /* inner penalty */
+  double sigma_boundary;     /* Dirichlet penalty */
+  int weight_is_diffusion;   /* 1: SWIPDG (weight = kappa), 0: weight = 1 */
+} gdt_ipdg_desc;
+
+/* DG Lagrange order 1: element Laplace + InnerCoupling/InnerPenalty (inner intersections) +
+ * DirichletCoupling/BoundaryPenalty (homogeneous Dirichlet boundary), penalty length h = |I|. */
+gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* desc, double* rhs);
+
+/* ------------------------------------------------------------ apply / solve --- */
+gdt_status gdt_spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y);
+
+typedef struct gdt_solver_opts {
+  int solver;            /* GDT_SOLVER_* */
+  int precond;           /* GDT_PREC_* */
+  int precision;         /* GDT_PRECISION_FP64 or GDT_PRECISION_MIXED (FP32 inner CG, FP64 refinement) */
+  double tol;            /* stop when ||b - A x|| <= tol * ||b - A x0|| */
+  int max_iter;          /* total inner iterations */
+  int check_every;       /* iterations between host convergence checks (0 = library default) */
+  double inner_tol;      /* mixed: relative reduction per refinement step (0 = default 1e-3) */
+} gdt_solver_opts;
+
+typedef struct gdt_solve_info {
+  int iterations;        /* Krylov iterations done */
+  int refinements;       /* mixed precision: FP64 refinement steps */
+  double rel_residual;   /* final ||b - A x|| / ||b - A x0|| in FP64 */
+  int converged;
+} gdt_solve_info;
+
+/* x holds the initial guess on entry. Returns GDT_ENOCONV (x = last iterate) if not converged. */
+gdt_status gdt_solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* opts,
+                     gdt_solve_info* info);
+
+/* --------------------------------------------------------------- finite volume --- */
+typedef struct gdt_fv_desc {
+  int flux;              /* GDT_FLUX_BURGERS: f(u) = u^2/2 (1,..,1); GDT_FLUX_TRANSPORT: f(u) = v u */
+  double velocity[3];
+  int numflux;           /* GDT_NUMFLUX_* */
+  double lf_lambda;      /* 0: local Lax-Friedrichs (max_d |f_d'|); else the reference's fixed lambda */
+} gdt_fv_desc;
+
+/* range = AdvectionFvOperator(u) on a periodic cube grid (FV space, m = 1) */
+gdt_status gdt_fv_apply(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, const double* u, double* range);
+/* dt of estimate_dt_for_hyperbolic_system for initial data u0 (host result) */
+gdt_status gdt_fv_estimate_dt(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, const double* u0, double* dt);
+/* `steps` explicit steps in place on a batch of `nbatch` states stored one after another
+ * (u[b * N + cell]); work must hold nbatch * N doubles. */
+gdt_status gdt_fv_timestep(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, int timestepper, double dt,
+                           int64_t steps, int64_t nbatch, double* u, double* work);
+
+/* ------------------------------------------------------------------ adjoint --- */
+/* out[e] = -d/dlog(kappa_e) [lam^T A(kappa) u]: the gradient of J(u(kappa)) w.r.t. log kappa when
+ * lam solves A^T lam = dJ/du. CG: Laplace stiffness (Dirichlet rows excluded); DG: SWIPDG. */
+gdt_status gdt_cg_dlogkappa(gdt_context ctx, gdt_space cg, const double* kappa, const double* u,
+                            const double* lam, double* out);
+gdt_status gdt_swipdg_dlogkappa(gdt_context ctx, gdt_space dg, const gdt_ipdg_desc* desc, const double* u,
+                                const double* lam, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

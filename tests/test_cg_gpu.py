@@ -1,0 +1,173 @@
+"""Continuous Lagrange path on the GPU against the CPU oracle: DoF numbering and sparsity pattern
+bit-exact, stiffness/RHS/Dirichlet within 1e-12 relative, SpMV and Krylov solves."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spl
+import torch
+
+from conftest import csr_equal_pattern, rel_err
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = [
+    (1, [7], False),
+    (2, [5, 4], False),
+    (2, [6, 3], True),
+    (3, [4, 3, 5], False),
+    (3, [3, 4, 2], True),
+]
+
+
+def _grid(gdt, oracle, dim, n, simplex, lo=None, hi=None):
+    lo = lo or [0.0] * dim
+    hi = hi or [1.0 + 0.5 * a for a in range(dim)]
+    return gdt.make_cube_grid(lo, hi, n, simplex=simplex), oracle.grid(dim, n, lo, hi, simplex=simplex)
+
+
+@pytest.mark.parametrize("dim,n,simplex", GRIDS)
+def test_global_indices_bit_exact(gdt, oracle, dim, n, simplex):
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    for kind, cls in ((oracle.CG, gdt.ContinuousLagrangeSpace), (oracle.DG, gdt.DiscontinuousLagrangeSpace)):
+        if kind == oracle.DG and simplex and dim == 3:
+            continue
+        sp = cls(g, 1)
+        assert sp.num_DoFs == oracle.space_size(og, kind, 1)
+        gi = sp.global_indices().cpu().numpy()
+        assert np.array_equal(gi, oracle.global_indices(og, kind, 1))
+
+
+@pytest.mark.parametrize("dim,n,simplex", GRIDS)
+def test_pattern_bit_exact(gdt, oracle, dim, n, simplex):
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    op = gdt.MatrixOperator(g, gdt.ContinuousLagrangeSpace(g, 1))
+    ref = oracle.pattern(og, oracle.CG, 1, oracle.STENCIL_ELEMENT)
+    assert op.nnz == ref.nnz
+    assert csr_equal_pattern(op.csr(), ref)
+
+
+@pytest.mark.parametrize("dim,n,simplex", [(2, [5, 4], True), (2, [4, 6], False)])
+def test_dg_pattern_bit_exact(gdt, oracle, dim, n, simplex):
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    sp = gdt.DiscontinuousLagrangeSpace(g, 1)
+    for st, ost in ((gdt.Stencil.element_and_intersection, oracle.STENCIL_ELEMENT_AND_INTERSECTION),
+                    (gdt.Stencil.intersection, oracle.STENCIL_INTERSECTION),
+                    (gdt.Stencil.element, oracle.STENCIL_ELEMENT)):
+        op = gdt.MatrixOperator(g, sp, stencil=st)
+        ref = oracle.pattern(og, oracle.DG, 1, ost)
+        assert csr_equal_pattern(op.csr(), ref)
+
+
+@pytest.mark.parametrize("dim,n,simplex", GRIDS)
+@pytest.mark.parametrize("dirichlet", [True, False])
+def test_assembly_matches_oracle(gdt, oracle, dim, n, simplex, dirichlet):
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    rng = np.random.default_rng(11 + dim)
+    ne = g.num_elements
+    kappa = np.exp(rng.standard_normal(ne))
+    force = rng.uniform(-1, 2, ne)
+    A, b = oracle.assemble_cg(og, 1, kappa=kappa, force=force, dirichlet=dirichlet)
+    space = gdt.ContinuousLagrangeSpace(g, 1)
+    op = gdt.MatrixOperator(g, space)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(torch.tensor(kappa, device="cuda")))
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    op.assemble(rhs=rhs, force=torch.tensor(force, device="cuda"), dirichlet=dirichlet)
+    rp, col, val = op.csr()
+    assert csr_equal_pattern((rp, col, val), A)
+    assert rel_err(val.cpu().numpy(), A.val) < 1e-12
+    assert rel_err(rhs.cpu().numpy(), b) < 1e-12
+
+
+def test_walker_fused_equals_separate_dirichlet(gdt, oracle):
+    # the reference example's walker (examples/stationary-heat-equation.cc:94-110) vs separate passes
+    g = gdt.make_cube_grid([-1, -1], [1, 1], [16, 16])
+    space = gdt.ContinuousLagrangeSpace(g, 1)
+    ops = []
+    for fused in (True, False):
+        lhs = gdt.MatrixOperator(g, space)
+        lhs.append(gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(1.0)))
+        rhs = gdt.VectorFunctional(g, space)
+        rhs.append(gdt.LocalElementIntegralFunctional(gdt.LocalElementProductIntegrand().with_ansatz(1.0)))
+        dc = gdt.DirichletConstraints("all_dirichlet", space)
+        if fused:
+            w = gdt.Walker(g)
+            w.append(lhs).append(rhs).append(dc)
+            w.walk(thread_parallel=True)
+        else:
+            lhs.assemble()
+            rhs.assemble()
+        dc.apply(lhs, rhs.vector)
+        ops.append((lhs.csr()[2].cpu().numpy().copy(), rhs.vector.cpu().numpy().copy()))
+    og = oracle.grid(2, [16, 16], [-1, -1], [1, 1])
+    A, b = oracle.assemble_cg(og, 1)
+    for val, vec in ops:
+        assert rel_err(val, A.val) < 1e-12
+        assert rel_err(vec, b) < 1e-12
+
+
+@pytest.mark.parametrize("dim,n,simplex", [(2, [9, 7], True), (3, [5, 4, 6], False), (1, [9], False)])
+def test_spmv_matches_oracle(gdt, oracle, dim, n, simplex):
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    rng = np.random.default_rng(3)
+    kappa = np.exp(rng.standard_normal(g.num_elements))
+    A, _ = oracle.assemble_cg(og, 1, kappa=kappa, dirichlet=False)
+    space = gdt.ContinuousLagrangeSpace(g, 1)
+    op = gdt.MatrixOperator(g, space)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(torch.tensor(kappa, device="cuda")))
+    op.assemble()
+    x = rng.standard_normal(space.num_DoFs)
+    y = op.apply(torch.tensor(x, device="cuda")).cpu().numpy()
+    assert rel_err(y, oracle.spmv(A, x)) < 1e-13
+
+
+def _heat_problem(gdt, oracle, dim, n, simplex, seed=5):
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    rng = np.random.default_rng(seed)
+    kappa = np.exp(rng.standard_normal(g.num_elements))
+    A, b = oracle.assemble_cg(og, 1, kappa=kappa, force_const=1.0)
+    space = gdt.ContinuousLagrangeSpace(g, 1)
+    op = gdt.MatrixOperator(g, space)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(torch.tensor(kappa, device="cuda")))
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    op.assemble(rhs=rhs, force=1.0, dirichlet=True)
+    return op, rhs, A, b
+
+
+@pytest.mark.parametrize("solver,precond", [("cg", "jacobi"), ("cg", "none"), ("cg", "ilu0"),
+                                            ("bicgstab", "jacobi"), ("bicgstab", "ilu0"), ("bicgstab", "none")])
+def test_solvers_match_direct(gdt, oracle, solver, precond):
+    op, rhs, A, b = _heat_problem(gdt, oracle, 2, [24, 20], True)
+    xd = spl.spsolve(A.to_scipy().tocsc(), b)
+    x = op.apply_inverse(rhs, opts={"type": solver, "precond": precond, "tol": 1e-13})
+    info = op.last_solve_info
+    assert info["converged"]
+    assert rel_err(x.cpu().numpy(), xd) < 1e-10
+    # iteration counts agree with the oracle's restatement of the same algorithm
+    xo, it, rr, st = oracle.solve(A, b, solver={"cg": 0, "bicgstab": 1}[solver],
+                                  prec={"none": 0, "jacobi": 1, "ilu0": 2}[precond], tol=1e-13)
+    assert abs(info["iterations"] - it) <= max(2, 0.05 * it)
+
+
+def test_mixed_precision_refinement_reaches_fp64_accuracy(gdt, oracle):
+    op, rhs, A, b = _heat_problem(gdt, oracle, 3, [12, 10, 14], False)
+    xd = spl.spsolve(A.to_scipy().tocsc(), b)
+    x = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+    info = op.last_solve_info
+    assert info["converged"] and info["refinements"] >= 2
+    assert rel_err(x.cpu().numpy(), xd) < 1e-9
+
+
+def test_solver_reports_non_convergence(gdt, oracle):
+    op, rhs, A, b = _heat_problem(gdt, oracle, 2, [30, 30], False)
+    with pytest.raises(gdt.GdtError) as e:
+        op.apply_inverse(rhs, opts={"tol": 1e-12, "max_iter": 3})
+    assert e.value.status == gdt._capi.ENOCONV
+
+
+def test_shape_errors_are_status_codes(gdt):
+    g = gdt.make_cube_grid([0, 0], [1, 1], [4, 4])
+    op = gdt.MatrixOperator(g, gdt.ContinuousLagrangeSpace(g, 1))
+    with pytest.raises(ValueError):
+        op.apply(torch.zeros(3, dtype=torch.float64, device="cuda"))
+    with pytest.raises(gdt.GdtError) as e:
+        gdt.MatrixOperator(g, gdt.ContinuousLagrangeSpace(g, 1), stencil=gdt.Stencil.element_and_intersection)
+    assert e.value.status == gdt._capi.EUNSUPPORTED

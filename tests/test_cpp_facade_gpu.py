@@ -1,0 +1,24 @@
+"""The reference's stationary-heat-equation driver, written against the C++ facade (same calls as
+examples/stationary-heat-equation.cc:87-110), runs on the GPU and converges to the exact solution."""
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT, import_gdt
+
+pytestmark = pytest.mark.gpu
+
+
+def test_stationary_heat_equation_example(gdt):
+    exes = gdt._build.build_examples()
+    exe = [e for e in exes if e.endswith("stationary_heat_equation")][0]
+    errs = []
+    for cells in (32, 64):
+        out = subprocess.run([exe, str(cells)], capture_output=True, text=True, timeout=300, check=True).stdout
+        fields = out.split()
+        assert int(fields[1]) == (cells + 1) ** 2
+        errs.append(float(fields[-1]))
+    # second-order convergence of the vertex error (element-barycentre source lowering)
+    assert errs[1] < errs[0] / 3.0
+    assert errs[1] < 2e-3

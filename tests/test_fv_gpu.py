@@ -1,0 +1,125 @@
+"""Finite-volume path on the GPU against the oracle: AdvectionFvOperator apply, dt estimate,
+explicit Euler and SSP-RK2 (single and batched), and the reference's Burgers 1D tables."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import fv_cell_average_1d, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _bumps(dim, n, seed, nb=6):
+    rng = np.random.default_rng(seed)
+    axes = [(np.arange(k) + 0.5) / k for k in n]
+    X = np.meshgrid(*axes, indexing="ij")
+    u = np.zeros([k for k in n])
+    for _ in range(nb):
+        c = rng.uniform(0, 1, dim)
+        w = rng.uniform(0.05, 0.2)
+        a = rng.uniform(-1, 1)
+        r2 = sum((X[a_] - c[a_]) ** 2 for a_ in range(dim))
+        u += a * np.exp(-r2 / (2 * w * w))
+    # lexicographic, x fastest
+    return np.ascontiguousarray(u.transpose(list(range(dim))[::-1]).reshape(-1))
+
+
+CASES = [
+    (1, [37]),
+    (2, [40, 33]),
+    (2, [64, 64]),
+    (3, [9, 7, 6]),
+]
+FLUXES = [("burgers", "lf"), ("burgers", "upwind"), ("transport", "lf"), ("transport", "upwind")]
+
+
+def _op(gdt, g, flux, numflux, dim):
+    fl = gdt.BurgersFlux() if flux == "burgers" else gdt.LinearTransportFlux([0.7, -0.4, 0.25][:dim])
+    nf = gdt.NumericalLaxFriedrichsFlux(fl) if numflux == "lf" else gdt.NumericalUpwindFlux(fl)
+    space = gdt.FiniteVolumeSpace(g)
+    return gdt.AdvectionFvOperator(g, nf, space), space
+
+
+def _orc_args(oracle, flux, numflux, dim):
+    return dict(flux=oracle.FLUX_BURGERS if flux == "burgers" else oracle.FLUX_TRANSPORT,
+                numflux=oracle.NUMFLUX_LAX_FRIEDRICHS if numflux == "lf" else oracle.NUMFLUX_UPWIND,
+                velocity=[0.7, -0.4, 0.25][:dim])
+
+
+@pytest.mark.parametrize("dim,n", CASES)
+@pytest.mark.parametrize("flux,numflux", FLUXES)
+def test_fv_apply_matches_oracle(gdt, oracle, dim, n, flux, numflux):
+    g = gdt.make_cube_grid([0] * dim, [1] * dim, n, periodic=True)
+    og = oracle.grid(dim, n, 0.0, 1.0, periodic=True)
+    op, space = _op(gdt, g, flux, numflux, dim)
+    u = _bumps(dim, n, 4)
+    a = _orc_args(oracle, flux, numflux, dim)
+    ref = oracle.fv_apply(og, a["flux"], a["numflux"], u, velocity=a["velocity"])
+    out = op.apply(torch.tensor(u, device="cuda")).cpu().numpy()
+    assert rel_err(out, ref) < 1e-13
+
+
+@pytest.mark.parametrize("dim,n", CASES)
+@pytest.mark.parametrize("flux,numflux", FLUXES)
+@pytest.mark.parametrize("method", ["euler", "ssp2"])
+def test_fv_timesteppers_match_oracle(gdt, oracle, dim, n, flux, numflux, method):
+    g = gdt.make_cube_grid([0] * dim, [1] * dim, n, periodic=True)
+    og = oracle.grid(dim, n, 0.0, 1.0, periodic=True)
+    op, space = _op(gdt, g, flux, numflux, dim)
+    u0 = _bumps(dim, n, 9)
+    a = _orc_args(oracle, flux, numflux, dim)
+    dt_o = oracle.fv_estimate_dt(og, a["flux"], u0, velocity=a["velocity"])
+    ut = torch.tensor(u0, device="cuda")
+    dt_g = gdt.estimate_dt_for_hyperbolic_system(g, ut, op)
+    assert abs(dt_g - dt_o) <= 1e-14 * dt_o
+    dt = 0.5 * dt_o
+    steps = 25
+    stepper = gdt.ExplicitRungeKuttaTimeStepper(op, ut, method=method)
+    stepper.step(dt, steps)
+    if method == "euler":
+        ref = oracle.fv_explicit_euler(og, a["flux"], a["numflux"], u0, dt, steps, velocity=a["velocity"])
+    else:
+        ref = oracle.fv_ssprk2(og, a["flux"], a["numflux"], u0, dt, steps, velocity=a["velocity"])
+    assert rel_err(ut.cpu().numpy(), ref) < 1e-12
+
+
+def test_fv_batched_equals_single(gdt, oracle):
+    n = [48, 40]
+    g = gdt.make_cube_grid([0, 0], [1, 1], n, periodic=True)
+    og = oracle.grid(2, n, 0.0, 1.0, periodic=True)
+    op, space = _op(gdt, g, "burgers", "lf", 2)
+    states = [_bumps(2, n, s) for s in (1, 2, 3)]
+    ut = torch.tensor(np.concatenate(states), device="cuda")
+    dt = 0.4 * min(oracle.fv_estimate_dt(og, oracle.FLUX_BURGERS, s) for s in states)
+    gdt.ExplicitRungeKuttaTimeStepper(op, ut, method="ssp2").step(dt, 30)
+    out = ut.cpu().numpy().reshape(3, -1)
+    for b, s in enumerate(states):
+        ref = oracle.fv_ssprk2(og, oracle.FLUX_BURGERS, oracle.NUMFLUX_LAX_FRIEDRICHS, s, dt, 30)
+        assert rel_err(out[b], ref) < 1e-12
+
+
+@pytest.mark.parametrize("flux", ["numerical_upwind_flux", "numerical_lax_friedrichs_flux"])
+def test_burgers_1d_tables_on_gpu(gdt, oracle, golden, flux):
+    # dune/gdt/test/burgers/burgers__1d__explicit__fv.mini through the GPU path
+    case = golden["burgers_1d"][flux]
+    res = case["results"]
+    for lvl, n in enumerate((16, 32)):
+        g = gdt.make_cube_grid([0.0], [1.0], [n], periodic=True)
+        fl = gdt.BurgersFlux()
+        nf = gdt.NumericalUpwindFlux(fl) if "upwind" in flux else gdt.NumericalLaxFriedrichsFlux(fl)
+        op = gdt.AdvectionFvOperator(g, nf, gdt.FiniteVolumeSpace(g))
+        u0 = fv_cell_average_1d(n, lambda x: np.exp(-(x - 0.33) ** 2 / (2 * 0.075 ** 2)), 3)
+        ut = torch.tensor(u0, device="cuda")
+        fv_dt = gdt.estimate_dt_for_hyperbolic_system(g, ut, op)
+        dt = 0.99 * case["setup"]["use_fixed_dt"]
+        stepper = gdt.ExplicitRungeKuttaTimeStepper(op, ut, method="euler")
+        t, count, masses = 0.0, 1, []
+        while t < 1.0 + dt:
+            stepper.step(dt, 1)
+            t += dt
+            count += 1
+            masses.append(ut.sum().item() / n)
+        assert count == res["quantity.num_timesteps"][lvl]
+        assert float("%.2e" % (dt / fv_dt)) == pytest.approx(res["quantity.CFL"][lvl], rel=1e-12)
+        m0 = u0.sum() / n
+        assert max(abs(m - m0) / m0 for m in masses) < 1e-14
