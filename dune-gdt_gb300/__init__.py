@@ -695,3 +695,55 @@ class DiffusionSolve(torch.autograd.Function):
         problem.assemble(kappa)  # the operator may have been reassembled since forward
         lam = problem.op.apply_inverse(grad_u.contiguous().to(torch.float64), opts=problem.solver_opts)
         return dlogkappa(problem.op, u, lam, kappa), None
+
+
+# ---------------------------------------------------------------------------------- batched ---
+class BatchedDiffusion:
+    """Many parametric problems (-div(kappa_mu grad u) = f on the unit square, P1 on cells[i]^2 squares
+    split into triangles, kappa = mu[i, q] on quadrant q) assembled and solved in one persistent launch."""
+
+    def __init__(self, cells, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.cells = [int(c) for c in cells]
+        arr = (C.c_int64 * len(self.cells))(*self.cells)
+        h = C.c_void_p()
+        self.ctx.call("gdt_batch_create", C.c_int64(len(self.cells)), arr, C.byref(h))
+        self.handle = h
+        L = capi.load()
+        self.total_dofs = int(L.gdt_batch_total_dofs(h))
+        off = (C.c_int64 * (len(self.cells) + 1))()
+        capi.check(L.gdt_batch_dof_offsets(h, off))
+        self.offsets = [int(v) for v in off]
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                capi.load().gdt_batch_destroy(self.handle)
+        except Exception:
+            pass
+
+    def solve(self, mu, force=1.0, precision="fp64", tol=1e-10, max_iter=100000, x=None, keep_stencil=False,
+              wait=True):
+        mu = _f64(mu.contiguous().reshape(-1), 4 * len(self.cells), "mu")
+        if x is None:
+            x = torch.empty(self.total_dofs, dtype=torch.float64, device=self.ctx.device)
+        stencil = torch.empty(self.total_dofs * 7, dtype=torch.float64, device=self.ctx.device) if keep_stencil else None
+        info = capi.BatchInfo()
+        prec = {"fp64": capi.PRECISION_FP64, "mixed": capi.PRECISION_MIXED}[precision]
+        self.ctx.call("gdt_batch_solve", self.handle, _ptr(mu), C.c_double(force), prec, C.c_double(tol), int(max_iter),
+                      _ptr(_f64(x, self.total_dofs, "x")), _ptr(stencil), C.byref(info) if wait else None)
+        self.last_info = {"max_iterations": info.max_iterations, "min_iterations": info.min_iterations,
+                          "max_rel_residual": info.max_rel_residual, "all_converged": bool(info.all_converged)}
+        return (x, stencil) if keep_stencil else x
+
+    def iterations(self):
+        import numpy as np
+
+        n = len(self.cells)
+        it = (C.c_int * n)()
+        rr = (C.c_double * n)()
+        self.ctx.call("gdt_batch_iterations", self.handle, it, rr)
+        return np.array(it[:]), np.array(rr[:])
+
+    def unpack(self, x, i):
+        return x[self.offsets[i]:self.offsets[i + 1]]

@@ -45,6 +45,11 @@ class FvDesc(C.Structure):
     _fields_ = [("flux", C.c_int), ("velocity", C.c_double * 3), ("numflux", C.c_int), ("lf_lambda", C.c_double)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("problems", C.c_int64), ("total_dofs", C.c_int64), ("max_iterations", C.c_int),
+                ("min_iterations", C.c_int), ("max_rel_residual", C.c_double), ("all_converged", C.c_int)]
+
+
 class GdtError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{msg} (status {status})")
@@ -90,6 +95,12 @@ _SIGNATURES = {
     "gdt_fv_apply": (C.c_int, [P, P, C.POINTER(FvDesc), P, P]),
     "gdt_fv_estimate_dt": (C.c_int, [P, P, C.POINTER(FvDesc), P, C.POINTER(C.c_double)]),
     "gdt_fv_timestep": (C.c_int, [P, P, C.POINTER(FvDesc), C.c_int, C.c_double, C.c_int64, C.c_int64, P, P]),
+    "gdt_batch_create": (C.c_int, [P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(P)]),
+    "gdt_batch_destroy": (C.c_int, [P]),
+    "gdt_batch_total_dofs": (C.c_int64, [P]),
+    "gdt_batch_dof_offsets": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "gdt_batch_solve": (C.c_int, [P, P, P, C.c_double, C.c_int, C.c_double, C.c_int, P, P, P]),
+    "gdt_batch_iterations": (C.c_int, [P, P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gdt_cg_dlogkappa": (C.c_int, [P, P, P, P, P, P]),
     "gdt_swipdg_dlogkappa": (C.c_int, [P, P, C.POINTER(IpdgDesc), P, P, P]),
 }

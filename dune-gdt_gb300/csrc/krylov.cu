@@ -41,12 +41,9 @@ __global__ void __launch_bounds__(TH) k_spmv(int n, const int* __restrict__ rp, 
                                             const T* __restrict__ w, KState* st, double* partials,
                                             unsigned int* ticket) {
   if (stopped(st)) return;
-  const int lane = threadIdx.x & (G - 1);
-  const int rpb = blockDim.x / G;
   T a0 = T(0), a1 = T(0);
-  for (int row = blockIdx.x * rpb + threadIdx.x / G; row < n; row += gridDim.x * rpb) {
-    T s = csr_row<G, T>(rp[row], rp[row + 1], lane, col, val, x);
-    if (lane == 0) {
+  for_rows<G, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
+    if (leader) {
       y[row] = s;
       if (MODE == 1) a0 = fma(x[row], s, a0);
       if (MODE == 2) a0 = fma(w[row], s, a0);
@@ -55,7 +52,7 @@ __global__ void __launch_bounds__(TH) k_spmv(int n, const int* __restrict__ rp, 
         a1 = fma(s, s, a1);
       }
     }
-  }
+  });
   if (MODE == 0) return;
   double v[2] = {double(a0), double(a1)};
   if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
@@ -88,12 +85,9 @@ __global__ void __launch_bounds__(TH) k_residual_init(int n, const int* __restri
                                                      const T* __restrict__ b, T* __restrict__ r,
                                                      const T* __restrict__ dinv, T* __restrict__ p,
                                                      KState* st, double* partials, unsigned int* ticket) {
-  const int lane = threadIdx.x & (G - 1);
-  const int rpb = blockDim.x / G;
   T a0 = T(0), a1 = T(0);
-  for (int row = blockIdx.x * rpb + threadIdx.x / G; row < n; row += gridDim.x * rpb) {
-    T s = csr_row<G, T>(rp[row], rp[row + 1], lane, col, val, x);
-    if (lane == 0) {
+  for_rows<G, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
+    if (leader) {
       T ri = b[row] - s;
       r[row] = ri;
       T zi = dinv ? dinv[row] * ri : ri;
@@ -101,7 +95,7 @@ __global__ void __launch_bounds__(TH) k_residual_init(int n, const int* __restri
       a0 = fma(ri, zi, a0);
       a1 = fma(ri, ri, a1);
     }
-  }
+  });
   double v[2] = {double(a0), double(a1)};
   if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
     st->rho = v[0];
@@ -386,17 +380,14 @@ __global__ void __launch_bounds__(TH) k_residual64(int n, const int* __restrict_
                                                   const double* __restrict__ val, const double* __restrict__ x,
                                                   const double* __restrict__ b, double* __restrict__ r,
                                                   double* out_rr, double* partials, unsigned int* ticket) {
-  const int lane = threadIdx.x & (G - 1);
-  const int rpb = blockDim.x / G;
   double a0 = 0.0;
-  for (int row = blockIdx.x * rpb + threadIdx.x / G; row < n; row += gridDim.x * rpb) {
-    double s = csr_row<G, double>(rp[row], rp[row + 1], lane, col, val, x);
-    if (lane == 0) {
+  for_rows<G, double>(n, rp, col, val, x, [&](int row, bool leader, double s) {
+    if (leader) {
       double ri = b[row] - s;
       r[row] = ri;
       a0 = fma(ri, ri, a0);
     }
-  }
+  });
   double v[1] = {a0};
   if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) *out_rr = v[0];
 }

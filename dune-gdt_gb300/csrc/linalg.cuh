@@ -13,6 +13,8 @@ __device__ __forceinline__ T ld_stream(const T* p) {
 
 // y_row = sum_k val[k] x[col[k]] over one CSR row, computed by G cooperating lanes; the result is
 // valid in every lane of the group. Accumulation in T (FP64 path: double, inner mixed path: float).
+// Every lane of the warp must call this (the group reduction shuffles over the full warp): lanes
+// without a row pass beg == end.
 template <int G, class T>
 __device__ __forceinline__ T csr_row(int beg, int end, int lane, const int* __restrict__ col,
                                      const T* __restrict__ val, const T* __restrict__ x) {
@@ -21,6 +23,23 @@ __device__ __forceinline__ T csr_row(int beg, int end, int lane, const int* __re
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
   return s;
+}
+
+// Warp-uniform loop over the rows of a CSR matrix, G lanes per row: the loop bound depends only on
+// the block, so whole warps iterate together and every lane reaches the shuffles of csr_row.
+// body(row, active, s) runs in every lane; `active` is false for lanes past the last row.
+template <int G, class T, class Body>
+__device__ __forceinline__ void for_rows(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                         const T* __restrict__ val, const T* __restrict__ x, Body body) {
+  const int lane = threadIdx.x & (G - 1);
+  const int rpb = blockDim.x / G;
+  for (int row0 = blockIdx.x * rpb; row0 < n; row0 += gridDim.x * rpb) {
+    const int row = row0 + threadIdx.x / G;
+    const bool active = row < n;
+    const int beg = active ? rp[row] : 0, end = active ? rp[row + 1] : 0;
+    const T s = csr_row<G, T>(beg, end, lane, col, val, x);
+    body(row, active && lane == 0, s);
+  }
 }
 
 // Two-level deterministic reduction of NV partial sums over the whole grid: every block writes its

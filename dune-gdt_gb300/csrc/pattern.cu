@@ -39,12 +39,14 @@ __global__ void cg_pattern_kernel(GridDesc g, int* __restrict__ row_nnz, const i
 
 // DG order 1: all local rows of element e share the sorted neighbour blocks
 template <bool FILL>
-__global__ void dg_pattern_kernel(GridDesc g, int lsize, bool with_self, int* __restrict__ row_nnz,
+__global__ void dg_pattern_kernel(GridDesc g, int lsize, int stencil, int* __restrict__ row_nnz,
                                   const int* __restrict__ rp, int* __restrict__ col) {
   long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= g.nelem) return;
   long long nb[8];
-  int k = dg_neighbours(g, e, with_self, nb);
+  int k = 1;
+  if (stencil == GDT_STENCIL_ELEMENT) nb[0] = e;  // the element block only
+  else k = dg_neighbours(g, e, stencil != GDT_STENCIL_INTERSECTION, nb);
   for (int i = 0; i < lsize; ++i) {
     long long row = e * lsize + i;
     if (!FILL) {
@@ -113,9 +115,8 @@ gdt_status build_pattern(gdt_context ctx, gdt_matrix m) {
   GDT_TRY_CUDA(ctx, cudaMalloc(&m->rp, sizeof(int) * (rows + 1)));
   GDT_TRY_CUDA(ctx, cudaMalloc(&row_nnz, sizeof(int) * (rows + 1)));
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(row_nnz + rows, 0, sizeof(int), s));
-  bool with_self = m->stencil != GDT_STENCIL_INTERSECTION;
   if (dg)
-    dg_pattern_kernel<false><<<grid_blocks(g.nelem, 256), 256, 0, s>>>(g, m->test.lsize, with_self, row_nnz, nullptr,
+    dg_pattern_kernel<false><<<grid_blocks(g.nelem, 256), 256, 0, s>>>(g, m->test.lsize, m->stencil, row_nnz, nullptr,
                                                                        nullptr);
   else
     dispatch_cg_pattern(g, false, row_nnz, nullptr, nullptr, s);
@@ -136,7 +137,7 @@ gdt_status build_pattern(gdt_context ctx, gdt_matrix m) {
   GDT_TRY_CUDA(ctx, cudaMalloc(&m->val, sizeof(double) * std::max<long long>(nnz, 1)));
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * nnz, s));
   if (dg)
-    dg_pattern_kernel<true><<<grid_blocks(g.nelem, 256), 256, 0, s>>>(g, m->test.lsize, with_self, nullptr, m->rp,
+    dg_pattern_kernel<true><<<grid_blocks(g.nelem, 256), 256, 0, s>>>(g, m->test.lsize, m->stencil, nullptr, m->rp,
                                                                       m->col);
   else
     dispatch_cg_pattern(g, true, nullptr, m->rp, m->col, s);

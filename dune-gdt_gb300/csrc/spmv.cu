@@ -8,12 +8,9 @@ namespace gdt {
 template <int G, class T>
 __global__ void __launch_bounds__(256) spmv_kernel(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                                    const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y) {
-  const int lane = threadIdx.x & (G - 1);
-  const int rows_per_block = blockDim.x / G;
-  for (int row = blockIdx.x * rows_per_block + threadIdx.x / G; row < n; row += gridDim.x * rows_per_block) {
-    T s = csr_row<G, T>(rp[row], rp[row + 1], lane, col, val, x);
-    if (lane == 0) y[row] = s;
-  }
+  for_rows<G, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
+    if (leader) y[row] = s;
+  });
 }
 
 template <class T>

@@ -192,6 +192,37 @@ gdt_status gdt_fv_estimate_dt(gdt_context ctx, gdt_space fv, const gdt_fv_desc* 
 gdt_status gdt_fv_timestep(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, int timestepper, double dt,
                            int64_t steps, int64_t nbatch, double* u, double* work);
 
+/* ------------------------------------------------------------------ batched --- */
+/* Many parametric stationary problems in one persistent launch (the pyMOR-style parameter sweeps of
+ * python/dune/gdt/gamm-2019-talk-on-conservative-rb.cc:74-95 run as one GPU job): problem i is
+ * -div(kappa grad u) = force on the unit square with cells[i] x cells[i] squares split into two
+ * triangles each, continuous P1, kappa = mu[4 i + q] on quadrant q = qx + 2 qy of the 2 x 2 split,
+ * homogeneous Dirichlet boundary. cells[i] even. Sizes may differ between problems. */
+typedef struct gdt_batch_s* gdt_batch;
+
+typedef struct gdt_batch_info {
+  int64_t problems;
+  int64_t total_dofs;
+  int max_iterations;
+  int min_iterations;
+  double max_rel_residual;  /* ||b - A x|| / ||b|| of the returned iterates, FP64 */
+  int all_converged;
+} gdt_batch_info;
+
+gdt_status gdt_batch_create(gdt_context ctx, int64_t nproblems, const int64_t* cells, gdt_batch* out);
+gdt_status gdt_batch_destroy(gdt_batch b);
+int64_t gdt_batch_total_dofs(gdt_batch b);
+/* host array of nproblems + 1 DoF offsets into the concatenated solution vector */
+gdt_status gdt_batch_dof_offsets(gdt_batch b, int64_t* offsets);
+/* assemble (FP64) and solve every problem to ||b - A x|| <= tol ||b|| in one persistent launch (CUDA
+ * graph, re-captured when the arguments change). mu: device [4 * nproblems]; x: device [total_dofs];
+ * stencil_out: optional device [total_dofs][7] receiving the assembled rows in CSR column order (NULL to
+ * skip); precision: GDT_PRECISION_FP64 or GDT_PRECISION_MIXED. info (optional) makes the call wait. */
+gdt_status gdt_batch_solve(gdt_context ctx, gdt_batch b, const double* mu, double force, int precision, double tol,
+                           int max_iter, double* x, double* stencil_out, gdt_batch_info* info);
+/* per-problem iteration counts (negative: -(count + 1) when not converged) and relative residuals (host) */
+gdt_status gdt_batch_iterations(gdt_context ctx, gdt_batch b, int* iterations, double* rel_residuals);
+
 /* ------------------------------------------------------------------ adjoint --- */
 /* out[e] = -d/dlog(kappa_e) [lam^T A(kappa) u]: the gradient of J(u(kappa)) w.r.t. log kappa when
  * lam solves A^T lam = dJ/du. CG: Laplace stiffness (Dirichlet rows excluded); DG: SWIPDG. */
