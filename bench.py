@@ -151,6 +151,11 @@ def run_gdt(args):
     u = torch.zeros(ndof, dtype=torch.float64, device="cuda")
     # FP64 reference solution at a tight tolerance (untimed) for the error statement
     op.assemble(rhs=rhs, force=1.0, dirichlet=True)
+    import ctypes as C
+
+    sched = C.c_int()
+    sched_ms = (C.c_double * 7)()
+    ctx.call("gdt_matrix_tune", op.handle, C.byref(sched), sched_ms)
     u_ref = op.apply_inverse(rhs, opts={"tol": 1e-14, "max_iter": 200000}).clone()
 
     def step(precision):
@@ -227,7 +232,9 @@ def run_gdt(args):
     value = world * ndof / (ms_mixed / 1e3)
     t64, n64, t32, n32 = tm
     spmv32_ms = t32 / max(n32, 1)
-    bytes32 = 8 * nnz + 4 * (ndof + 1) + 8 * ndof  # FP32 values + int32 cols, row_ptr, x, y
+    # FP32 symmetric-stencil SpMV of the inner CG: 14 slot arrays (diagonal + 13 upper neighbours of the
+    # 27-point Q1 stencil) streamed once, the iterated vector read once and the product written once
+    bytes32 = (1 + 13) * 4 * ndof + 4 * ndof + 4 * ndof
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -263,10 +270,14 @@ def run_gdt(args):
                        "spmv_gbs": bytes64 / (spmv64_ms / 1e3) / 1e9 if n64b else None,
                        "spmv_frac_of_hbm": (bytes64 / (spmv64_ms / 1e3) / 1e9) / hbm if n64b else None},
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "spmv_autotuner": {"chosen_schedule": sched.value,
+                           "ms_per_launch": {name: round(sched_ms[k], 4) for k, name in enumerate(
+                               ["csr_vector_g4", "csr_vector_g8", "csr_vector_g16", "csr_vector_g32",
+                                "warp_staged_pl8", "warp_staged_pl16", "warp_staged_pl32"]) if sched_ms[k] > 0}},
         "e2e": {"value": world * ndof / (ms_e2e / 1e3), "unit": "DoF/s", "h2d_bytes_per_step": 8 * grid.num_elements,
                 "d2h_bytes_per_step": 8 * ndof},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "FP32 CSR SpMV of the inner CG (k_spmv<float>)",
+        "roofline": {"bound": "hbm", "kernel": "FP32 symmetric-stencil SpMV of the inner CG (k_mx_spmv)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "bytes_per_launch": bytes32, "avg_launch_ms": spmv32_ms, "launches": n32,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)", "traffic": None},

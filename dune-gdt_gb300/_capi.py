@@ -86,6 +86,7 @@ _SIGNATURES = {
     "gdt_matrix_nnz": (C.c_int64, [P]),
     "gdt_matrix_device_arrays": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "gdt_matrix_set_zero": (C.c_int, [P, P]),
+    "gdt_matrix_tune": (C.c_int, [P, P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gdt_assemble_cg_diffusion": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_assemble_cg_rhs": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_dirichlet_apply": (C.c_int, [P, P, P]),

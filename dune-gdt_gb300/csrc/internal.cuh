@@ -70,7 +70,9 @@ struct gdt_matrix_s {
   int* rp = nullptr;
   int* col = nullptr;
   double* val = nullptr;
-  int spmv_group = 8;  // lanes per row chosen by the tuner
+  int max_row = 0;     // longest row
+  int spmv_sched = 1;  // SpMV schedule (see linalg.cuh), picked by tune_spmv on first use
+  int tuned = 0;
 };
 
 namespace gdt {
@@ -115,9 +117,14 @@ gdt_status swipdg_dlogkappa(gdt_context ctx, const gdt_space_s& s, const gdt_ipd
                             const double* lam, double* out);
 // spmv.cu
 gdt_status spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y);
+gdt_status tune_spmv(gdt_context ctx, gdt_matrix m, double* times_ms = nullptr);
 // krylov.cu
 gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
                  gdt_solve_info* info);
+// mixed.cu: FP32 symmetric-stencil CG with FP64 reliable updates (structured continuous spaces)
+bool mixed_stencil_supported(gdt_matrix m);
+gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
+                               gdt_solve_info* info, cudaStream_t s);
 // fv.cu
 gdt_status fv_apply(gdt_context ctx, const gdt_space_s& s, const gdt_fv_desc* d, const double* u, double* out);
 gdt_status fv_estimate_dt(gdt_context ctx, const gdt_space_s& s, const gdt_fv_desc* d, const double* u0,

@@ -17,10 +17,6 @@
 
 namespace gdt {
 
-template <class T>
-void launch_spmv(int G, int n, const int* rp, const int* col, const T* val, const T* x, T* y, int num_sms,
-                 cudaStream_t s);
-
 namespace {
 
 constexpr int TH = 256;
@@ -35,14 +31,14 @@ __device__ __forceinline__ bool stopped(const KState* st) { return *((volatile c
 // ---------------------------------------------------------------- generic pieces ---
 // y = A x; optional dot(w, y) -> st->hden / alpha (mode 1: CG alpha = rho / (p.Ap); mode 2: BiCGStab
 // alpha = rho / (rt.v); mode 3: two dots (t.s, t.t) -> omega)
-template <int G, class T, int MODE>
+template <int G, int PL, class T, int MODE>
 __global__ void __launch_bounds__(TH) k_spmv(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                             const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y,
                                             const T* __restrict__ w, KState* st, double* partials,
                                             unsigned int* ticket) {
   if (stopped(st)) return;
   T a0 = T(0), a1 = T(0);
-  for_rows<G, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
+  for_rows_csr<G, PL, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
     if (leader) {
       y[row] = s;
       if (MODE == 1) a0 = fma(x[row], s, a0);
@@ -79,14 +75,14 @@ __global__ void __launch_bounds__(TH) k_spmv(int n, const int* __restrict__ rp, 
 }
 
 // r = b - A x, z = M^{-1} r (Jacobi if dinv, else z = r), p = z (CG start); rho = r.z, rr0 = r.r
-template <int G, class T>
+template <int G, int PL, class T>
 __global__ void __launch_bounds__(TH) k_residual_init(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                                      const T* __restrict__ val, const T* __restrict__ x,
                                                      const T* __restrict__ b, T* __restrict__ r,
                                                      const T* __restrict__ dinv, T* __restrict__ p,
                                                      KState* st, double* partials, unsigned int* ticket) {
   T a0 = T(0), a1 = T(0);
-  for_rows<G, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
+  for_rows_csr<G, PL, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
     if (leader) {
       T ri = b[row] - s;
       r[row] = ri;
@@ -375,13 +371,13 @@ __global__ void k_to_float(long long n, const double* __restrict__ a, float* __r
 }
 
 // r64 = b - A x (FP64) ; rr = r.r ; r32 = r64 * inv_scale where inv_scale = 1/||r|| is applied on the host side
-template <int G>
+template <int G, int PL>
 __global__ void __launch_bounds__(TH) k_residual64(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                                   const double* __restrict__ val, const double* __restrict__ x,
                                                   const double* __restrict__ b, double* __restrict__ r,
                                                   double* out_rr, double* partials, unsigned int* ticket) {
   double a0 = 0.0;
-  for_rows<G, double>(n, rp, col, val, x, [&](int row, bool leader, double s) {
+  for_rows_csr<G, PL, double>(n, rp, col, val, x, [&](int row, bool leader, double s) {
     if (leader) {
       double ri = b[row] - s;
       r[row] = ri;
@@ -408,53 +404,49 @@ __global__ void k_correct(int n, double* __restrict__ x, const float* __restrict
 struct Launch {
   gdt_context ctx;
   int n;
-  int G;
+  int sched;
   int vec_blocks;
-  int spmv_blocks;
   cudaStream_t s;
   double* partials;
   unsigned int* ticket;
+  template <class T>
+  LaunchShape shape() const {
+    return schedule_shape<T>(sched, n, ctx->num_sms);
+  }
 };
 
 template <class T, int MODE>
 void spmv_mode(const Launch& L, const int* rp, const int* col, const T* val, const T* x, T* y, const T* w,
                KState* st) {
+  const LaunchShape sh = L.shape<T>();
   timing_begin(L.ctx, L.s, sizeof(T) == 8 ? 0 : 1);
-  struct End {
-    const Launch& L;
-    ~End() { timing_end(L.ctx, L.s); }
-  } end{L};
-  switch (L.G) {
-    case 2: k_spmv<2, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
-    case 4: k_spmv<4, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
-    case 8: k_spmv<8, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
-    case 16: k_spmv<16, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
-    default: k_spmv<32, T, MODE><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket); break;
-  }
+#define GDT_K_SPMV(GG, PP) \
+  k_spmv<GG, PP, T, MODE><<<sh.blocks, sh.threads, sh.smem, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket)
+  GDT_SCHEDULE_SWITCH(L.sched, GDT_K_SPMV)
+#undef GDT_K_SPMV
+  timing_end(L.ctx, L.s);
   L.ctx->launches++;
 }
 
 template <class T>
 void residual_init(const Launch& L, const int* rp, const int* col, const T* val, const T* x, const T* b, T* r,
                    const T* dinv, T* p, KState* st) {
-  switch (L.G) {
-    case 2: k_residual_init<2, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
-    case 4: k_residual_init<4, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
-    case 8: k_residual_init<8, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
-    case 16: k_residual_init<16, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
-    default: k_residual_init<32, T><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, L.partials, L.ticket); break;
-  }
+  const LaunchShape sh = L.shape<T>();
+#define GDT_K_RESINIT(GG, PP)                                                                                    \
+  k_residual_init<GG, PP, T><<<sh.blocks, sh.threads, sh.smem, L.s>>>(L.n, rp, col, val, x, b, r, dinv, p, st, \
+                                                                      L.partials, L.ticket)
+  GDT_SCHEDULE_SWITCH(L.sched, GDT_K_RESINIT)
+#undef GDT_K_RESINIT
   L.ctx->launches++;
 }
 
 void residual64(const Launch& L, gdt_matrix m, const double* x, const double* b, double* r, double* rr) {
-  switch (L.G) {
-    case 2: k_residual64<2><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
-    case 4: k_residual64<4><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
-    case 8: k_residual64<8><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
-    case 16: k_residual64<16><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
-    default: k_residual64<32><<<L.spmv_blocks, TH, 0, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, L.ticket); break;
-  }
+  const LaunchShape sh = L.shape<double>();
+#define GDT_K_RES64(GG, PP)                                                                                      \
+  k_residual64<GG, PP><<<sh.blocks, sh.threads, sh.smem, L.s>>>(L.n, m->rp, m->col, m->val, x, b, r, rr, L.partials, \
+                                                                L.ticket)
+  GDT_SCHEDULE_SWITCH(L.sched, GDT_K_RES64)
+#undef GDT_K_RES64
   L.ctx->launches++;
 }
 
@@ -538,44 +530,6 @@ void ilu_apply(gdt_context ctx, gdt_matrix m, const Ilu& f, const double* r, dou
   }
 }
 
-// Runs `body` (one iteration's launches) in graph-captured chunks until the device flag says stop.
-template <class Body>
-gdt_status iterate(gdt_context ctx, cudaStream_t s, KState* st, int chunk, int max_chunks, Body body) {
-  cudaGraphExec_t exec = nullptr;
-  cudaGraph_t graph = nullptr;
-  bool use_graph = true;
-  // launches recorded while capturing run once per graph launch: count them there
-  const long long before = ctx->launches;
-  if (ctx->timing) {
-    use_graph = false;  // per-launch events need plain launches
-  } else if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-    for (int k = 0; k < chunk; ++k) body();
-    if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
-        cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
-      use_graph = false;
-  } else {
-    use_graph = false;
-  }
-  const long long per_chunk = ctx->launches - before;
-  ctx->launches = before;
-  cudaGetLastError();
-  int* flag = reinterpret_cast<int*>(ctx->host_pinned);
-  for (int c = 0; c < max_chunks; ++c) {
-    if (use_graph) {
-      GDT_TRY_CUDA(ctx, cudaGraphLaunch(exec, s));
-      ctx->launches += per_chunk;
-    } else {
-      for (int k = 0; k < chunk; ++k) body();
-    }
-    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(flag, &st->converged, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
-    if (ctx->timing) timing_harvest(ctx);
-    if (*flag) break;
-  }
-  if (exec) cudaGraphExecDestroy(exec);
-  if (graph) cudaGraphDestroy(graph);
-  return GDT_OK;
-}
 
 }  // namespace
 
@@ -600,16 +554,17 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
   Launch L;
   L.ctx = ctx;
   L.n = n;
-  L.G = m->spmv_group;
+  GDT_CHECK(ctx, tune_spmv(ctx, m));
+  L.sched = m->spmv_sched;
   L.s = s;
   L.vec_blocks = std::max(1, std::min(grid_blocks(n, TH), ctx->num_sms * 8));
-  L.spmv_blocks = std::max(1, std::min(grid_blocks((long long)n * L.G, TH), ctx->num_sms * 8));
   L.partials = ctx->scratch;
   L.ticket = ctx->counters;
   const int chunk = o->check_every > 0 ? o->check_every : 32;
   const bool mixed = o->precision == GDT_PRECISION_MIXED;
   if (mixed && (o->solver != GDT_SOLVER_CG || o->precond == GDT_PREC_ILU0))
     return fail(ctx, GDT_EUNSUPPORTED, "mixed precision is provided for CG with Jacobi or no preconditioner");
+  if (mixed && mixed_stencil_supported(m)) return solve_mixed_stencil(ctx, m, b, x, o, info, s);
   KState* st = nullptr;
   GDT_TRY_CUDA(ctx, cudaMallocAsync(&st, sizeof(KState), s));
   KState init{};
@@ -667,7 +622,7 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
           GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
         }
         residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
-        GDT_CHECK(ctx, iterate(ctx, s, st, chunk_used, max_chunks, [&] {
+        GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
           spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
           k_cg_update_jacobi<double, double><<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);
           k_cg_p_jacobi<double><<<L.vec_blocks, TH, 0, s>>>(n, p, r, one, st);
@@ -682,7 +637,7 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
         k_cg_beta<<<L.vec_blocks, TH, 0, s>>>(n, r, z, st, L.partials, L.ticket);
         GDT_TRY_CUDA(ctx, cudaMemcpyAsync(p, z, vb, cudaMemcpyDeviceToDevice, s));
         ctx->launches++;
-        GDT_CHECK(ctx, iterate(ctx, s, st, chunk_used, max_chunks, [&] {
+        GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
           spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
           k_cg_update<<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, st, L.partials, L.ticket);
           ilu_apply(ctx, m, ilu, r, z, st, s);
@@ -709,7 +664,7 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
           ctx->launches++;
         }
       };
-      GDT_CHECK(ctx, iterate(ctx, s, st, chunk_used, max_chunks, [&] {
+      GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
         k_bicg_rho<<<L.vec_blocks, TH, 0, s>>>(n, rt, r, st, L.partials, L.ticket);
         k_bicg_p<<<L.vec_blocks, TH, 0, s>>>(n, p, r, v, st);
         prec(p, y);
@@ -742,7 +697,7 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
     // ---------------------------------------------------- FP64 iterative refinement, FP32 inner CG
     const size_t vb = sizeof(double) * std::max(n, 1), fb = sizeof(float) * std::max(n, 1);
     double* r = (double*)alloc(vb);
-    float* val32 = (float*)alloc(sizeof(float) * std::max<long long>(m->nnz, 1));
+    float* val32 = (float*)alloc(sizeof(float) * (m->nnz + 8));
     float* r32 = (float*)alloc(fb);
     float* d32 = (float*)alloc(fb);
     float* p32 = (float*)alloc(fb);
@@ -785,7 +740,7 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
       GDT_TRY_CUDA(ctx, cudaMemcpyAsync(st, &in, sizeof(KState), cudaMemcpyHostToDevice, s));
       k_init_from_rhs<float><<<L.vec_blocks, TH, 0, s>>>(n, r32, dinv32, p32, st, L.partials, L.ticket);
       ctx->launches += 2;
-      GDT_CHECK(ctx, iterate(ctx, s, st, chunk, in.max_iter / chunk + 2, [&] {
+      GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk, in.max_iter / chunk + 2, [&] {
         spmv_mode<float, 1>(L, m->rp, m->col, val32, p32, q32, nullptr, st);
         k_cg_update_jacobi<float, float><<<L.vec_blocks, TH, 0, s>>>(n, d32, p32, r32, q32, dinv32, st, L.partials,
                                                                      L.ticket);

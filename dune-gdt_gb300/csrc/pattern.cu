@@ -1,6 +1,7 @@
 // Sparsity patterns built on the device, equal entry for entry to the reference's
 // make_element_sparsity_pattern / make_element_and_intersection_sparsity_pattern + sort()
 // (tools/sparsity-pattern.hh:33-50, 117-144) for the structured grids of this library.
+#include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include "structured.cuh"
@@ -129,24 +130,36 @@ gdt_status build_pattern(gdt_context ctx, gdt_matrix m) {
   GDT_CHECK(ctx, check_launch(ctx, "pattern scan"));
   int nnz = 0;
   GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&nnz, m->rp + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
+  int* dmax = nullptr;
+  size_t max_bytes = 0;
+  GDT_TRY_CUDA(ctx, cudaMalloc(&dmax, sizeof(int)));
+  cub::DeviceReduce::Max(nullptr, max_bytes, row_nnz, dmax, int(rows), s);
+  void* tmax = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMalloc(&tmax, max_bytes));
+  cub::DeviceReduce::Max(tmax, max_bytes, row_nnz, dmax, int(rows), s);
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&m->max_row, dmax, sizeof(int), cudaMemcpyDeviceToHost, s));
   GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+  cudaFree(tmax);
+  cudaFree(dmax);
   cudaFree(tmp);
   cudaFree(row_nnz);
   m->nnz = nnz;
-  GDT_TRY_CUDA(ctx, cudaMalloc(&m->col, sizeof(int) * std::max<long long>(nnz, 1)));
-  GDT_TRY_CUDA(ctx, cudaMalloc(&m->val, sizeof(double) * std::max<long long>(nnz, 1)));
-  GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * nnz, s));
+  // a few elements of padding so that vectorised/staged loads of a row slice never leave the arrays
+  GDT_TRY_CUDA(ctx, cudaMalloc(&m->col, sizeof(int) * (nnz + 8)));
+  GDT_TRY_CUDA(ctx, cudaMalloc(&m->val, sizeof(double) * (nnz + 8)));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * (nnz + 8), s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->col, 0, sizeof(int) * (nnz + 8), s));
   if (dg)
     dg_pattern_kernel<true><<<grid_blocks(g.nelem, 256), 256, 0, s>>>(g, m->test.lsize, m->stencil, nullptr, m->rp,
                                                                       m->col);
   else
     dispatch_cg_pattern(g, true, nullptr, m->rp, m->col, s);
   GDT_CHECK(ctx, check_launch(ctx, "pattern fill"));
-  // lanes per row for the vector-CSR SpMV: the smallest power of two >= mean row length / 4
-  double mean = rows ? double(nnz) / double(rows) : 1.0;
-  int gsz = 2;
-  while (gsz < 32 && gsz * 4 < mean) gsz *= 2;
-  m->spmv_group = gsz;
+  // untuned default schedule: vector-CSR with about four entries per lane (the first SpMV-type call
+  // replaces it with the autotuner's choice)
+  const double mean = rows ? double(nnz) / double(rows) : 1.0;
+  m->spmv_sched = mean <= 16 ? 0 : mean <= 32 ? 1 : mean <= 64 ? 2 : 3;
+  m->tuned = 0;
   return GDT_OK;
 }
 

@@ -115,6 +115,12 @@ int64_t gdt_matrix_cols(gdt_matrix m);
 int64_t gdt_matrix_nnz(gdt_matrix m);
 gdt_status gdt_matrix_device_arrays(gdt_matrix m, const int32_t** row_ptr, const int32_t** col, double** val);
 gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m);
+/* SpMV schedule autotuner (no reference counterpart; the reference's ISTL BCRS has one schedule):
+ * times every valid SpMV schedule on this matrix with CUDA events and keeps the fastest for all
+ * SpMV-type kernels of the matrix. Runs automatically on the first SpMV-type call; schedule (may be
+ * NULL) receives the chosen index, times_ms (may be NULL, 7 entries) the measured ms per launch of
+ * each schedule (-1 where a schedule does not apply). */
+gdt_status gdt_matrix_tune(gdt_context ctx, gdt_matrix m, int* schedule, double* times_ms);
 
 /* ----------------------------------------------------------------- assembly --- */
 typedef struct gdt_diffusion_desc {
