@@ -43,6 +43,13 @@ def parse():
     p.add_argument("--tol", type=float, default=1e-11, help="relative residual stop of both solvers")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-iters", type=int, default=60, help="CG iterations timed in the CPU sample")
+    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv"],
+                   help="heat3d: the headline 128^3 workload; batched: 512 parametric P1 problems of uneven "
+                        "size in one persistent launch; fv: 2D Burgers FV, SSP-RK2")
+    p.add_argument("--problems", type=int, default=512, help="batched: number of problems")
+    p.add_argument("--fv-n", type=int, default=4096, help="fv: cells per axis")
+    p.add_argument("--fv-steps", type=int, default=500, help="fv: SSP-RK2 steps per bench step")
+    p.add_argument("--fv-batch", type=int, default=1, help="fv: independent initial conditions")
     return p.parse_args()
 
 
@@ -195,11 +202,9 @@ def run_gdt(args):
     ms_mixed, launches, info_mixed, err_mixed, tm = timed("mixed", args.steps, args.warmup, timing=True)
     clk = clocks.stop()
     ms_fp64, _, info_fp64, err_fp64, tm64 = timed("fp64", max(1, args.steps // 2), 1, timing=True)
-    # max over ranks
-    if world > 1:
-        t = torch.tensor([ms_mixed, ms_fp64], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_mixed, ms_fp64 = t.tolist()
+    # replicas: units of all ranks over the slowest rank's time (no collective on the data path)
+    ms_mixed = gdt.replicas.max_over_ranks(ms_mixed, device="cuda")
+    ms_fp64 = gdt.replicas.max_over_ranks(ms_fp64, device="cuda")
 
     # end to end through the public API: host kappa (pinned) -> device, assemble + solve, solution -> host
     kappa_pinned = torch.tensor(kappa_host).pin_memory()
@@ -223,11 +228,7 @@ def run_gdt(args):
         e2e_step()
     e1.record()
     barrier()
-    ms_e2e = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = t.item()
+    ms_e2e = gdt.replicas.max_over_ranks(e0.elapsed_time(e1) / args.steps, device="cuda")
 
     value = world * ndof / (ms_mixed / 1e3)
     t64, n64, t32, n32 = tm
@@ -298,6 +299,181 @@ def run_gdt(args):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------------- batched (config 3) ---
+def quadrant_kappa(n, mu):
+    cells = np.arange(n * n)
+    cx, cy = cells % n, cells // n
+    q = (cx >= n // 2).astype(int) + 2 * (cy >= n // 2).astype(int)
+    return np.repeat(mu[q], 2)
+
+
+def run_batched(args):
+    """512 parametric diffusion problems on P1 triangle meshes of side n in {64,128,256,512}
+    (uneven, seeded), kappa = mu_q per quadrant, mu ~ U[0.1, 10]: assemble + solve all in one
+    persistent launch (FP64 and mixed), against the plain FP64 GPU path problem by problem."""
+    import torch
+
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    rng = np.random.default_rng(SEED + 3)
+    sides = rng.choice([64, 128, 256, 512], size=args.problems)
+    mu = rng.uniform(0.1, 10.0, (args.problems, 4))
+    mu_t = torch.tensor(mu, device="cuda")
+    b = gdt.BatchedDiffusion(sides.tolist())
+    ndof = b.total_dofs
+    x_ref = b.solve(mu_t, precision="fp64", tol=1e-13, max_iter=200000).clone()
+    x = torch.empty_like(x_ref)
+
+    def err(xx):
+        e = 0.0
+        for i in range(args.problems):
+            r = b.unpack(x_ref, i)
+            e = max(e, ((b.unpack(xx, i) - r).abs().max() / r.abs().max()).item())
+        return e
+
+    def timed(precision):
+        for _ in range(args.warmup):
+            b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000, wait=False)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000)  # waits, fills last_info
+        return ms, dict(b.last_info), err(x)
+
+    clocks = Clocks(0)
+    clocks.start()
+    ms_mixed, info_mixed, err_mixed = timed("mixed")
+    clk = clocks.stop()
+    ms_fp64, info_fp64, err_fp64 = timed("fp64")
+    # plain FP64 GPU path, one problem after another (operators built beforehand, as a user would):
+    # a stratified sample of `per_class` problems of every size, scaled by the class counts
+    per_class = 4
+    t_plain = 0.0
+    sample = []
+    for side in (64, 128, 256, 512):
+        idx = np.nonzero(sides == side)[0]
+        pick = idx[:per_class]
+        probs = []
+        for i in pick:
+            g = gdt.make_cube_grid([0, 0], [1, 1], [side, side], simplex=True)
+            pr = gdt.DiffusionProblem(g, solver_opts={"tol": args.tol, "max_iter": 200000})
+            k = torch.tensor(quadrant_kappa(side, mu[i]), device="cuda")
+            pr.solve(k)  # warm-up (pattern tuning, first use)
+            probs.append((pr, k))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for pr, k in probs:
+            pr.solve(k)
+        e1.record()
+        torch.cuda.synchronize()
+        t_class = e0.elapsed_time(e1) / len(probs) * len(idx)
+        t_plain += t_class
+        sample.append(f"{len(probs)} of {len(idx)} problems of side {side}")
+    line = {
+        "metric": "batched DoF/s assembled+solved (512 uneven P1 problems, one persistent launch)",
+        "value": ndof / (ms_mixed / 1e3), "unit": "DoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 assembly + FP32 inner CG / FP64 refinement", "data": "synthetic (seeded sizes and mu)",
+        "config": {"workload": f"{args.problems} problems, side n uniform in {{64,128,256,512}}, P1 Kuhn triangles, "
+                               "kappa = mu_q per quadrant, mu ~ U[0.1,10], f=1, Dirichlet 0",
+                   "dofs": ndof, "tol_rel_residual": args.tol},
+        "batched_mixed": {"ms": ms_mixed, "error_vs_fp64_reference": err_mixed, **info_mixed},
+        "batched_fp64": {"ms": ms_fp64, "value": ndof / (ms_fp64 / 1e3), "error_vs_fp64_reference": err_fp64,
+                         **info_fp64},
+        "plain_fp64_sequential": {"ms": t_plain, "value": ndof / (t_plain / 1e3),
+                                  "sample": "; ".join(sample) + " (assemble + solve per problem, timed with CUDA "
+                                                                "events, scaled by the class counts)"},
+        "speedup_batched_mixed_vs_plain_fp64": t_plain / ms_mixed,
+        "speedup_batched_fp64_vs_plain_fp64": t_plain / ms_fp64,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------- FV (config 5) ---
+def bumps(n, seed, count=32):
+    rng = np.random.default_rng(seed)
+    xc = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(xc, xc, indexing="xy")  # X varies along axis 1 (x fastest in the flat index)
+    u = np.zeros((n, n))
+    for _ in range(count):
+        a = rng.uniform(-1, 1)
+        w = rng.uniform(0.01, 0.1)
+        cx, cy = rng.uniform(0, 1, 2)
+        dx = np.minimum(np.abs(X - cx), 1 - np.abs(X - cx))
+        dy = np.minimum(np.abs(Y - cy), 1 - np.abs(Y - cy))
+        u += a * np.exp(-(dx * dx + dy * dy) / (2 * w * w))
+    return u.reshape(-1)
+
+
+def run_fv(args):
+    """2D inviscid Burgers on periodic n^2 cubes, FV P0, local LF flux, SSP-RK2 at CFL 0.5."""
+    import torch
+
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    n, nb = args.fv_n, args.fv_batch
+    g = gdt.make_cube_grid([0, 0], [1, 1], [n, n], periodic=True)
+    space = gdt.FiniteVolumeSpace(g)
+    op = gdt.AdvectionFvOperator(g, gdt.NumericalLaxFriedrichsFlux(gdt.BurgersFlux()), space)
+    u0 = np.concatenate([bumps(n, SEED + 5 + b) for b in range(nb)])
+    u0_t = torch.tensor(u0, device="cuda")
+    dt = 0.5 * min(gdt.estimate_dt_for_hyperbolic_system(g, u0_t[b * n * n:(b + 1) * n * n].contiguous(), op)
+                   for b in range(nb))
+    u = u0_t.clone()
+    stepper = gdt.ExplicitRungeKuttaTimeStepper(op, u, method="ssp2")
+    for _ in range(args.warmup):
+        u.copy_(u0_t)
+        stepper.step(dt, args.fv_steps)
+    torch.cuda.synchronize()
+    ms = []
+    clocks = Clocks(0)
+    clocks.start()
+    for _ in range(args.steps):
+        u.copy_(u0_t)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        stepper.step(dt, args.fv_steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    t = sum(ms) / len(ms)
+    cells = n * n * nb
+    mass0 = u0_t.view(nb, -1).sum(1)
+    mass_err = ((u.view(nb, -1).sum(1) - mass0).abs() / mass0.abs()).max().item()
+    per_step_s = t / 1e3 / args.fv_steps
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bytes_step = 40 * cells  # fused SSP-RK2: read u twice and k0, write k0 and the next state
+    line = {
+        "metric": "FV cell-updates/s (2D Burgers, LF flux, SSP-RK2)", "value": cells * args.fv_steps / (t / 1e3),
+        "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (32 seeded Gaussian bumps per state)",
+        "config": {"workload": f"{nb} x {n}^2 periodic cells, {args.fv_steps} SSP-RK2 steps per bench step, "
+                               "dt = 0.5 estimate_dt_for_hyperbolic_system", "dt": dt},
+        "rel_mass_conservation_error": mass_err,
+        "roofline": {"bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s); HBM fraction shown",
+                     "achieved": bytes_step / per_step_s / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": bytes_step / per_step_s / 1e9 / hbm, "bytes_per_step": bytes_step},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------------------------- reference arm ---
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
@@ -354,5 +530,9 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config == "batched":
+        run_batched(a)
+    elif a.config == "fv":
+        run_fv(a)
     else:
         run_gdt(a)

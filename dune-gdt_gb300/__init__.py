@@ -13,6 +13,7 @@ import ctypes as C
 import torch
 
 from . import _capi as capi
+from . import replicas
 from ._capi import GdtError
 
 __all__ = [
