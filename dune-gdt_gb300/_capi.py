@@ -93,6 +93,8 @@ _SIGNATURES = {
     "gdt_assemble_swipdg": (C.c_int, [P, P, C.POINTER(IpdgDesc), P]),
     "gdt_spmv": (C.c_int, [P, P, P, P]),
     "gdt_solve": (C.c_int, [P, P, P, P, C.POINTER(SolverOpts), C.POINTER(SolveInfo)]),
+    "gdt_solve_cg_jacobi_noalloc": (C.c_int, [P, P, P, C.c_int64, P, P, C.c_double, C.c_int, P,
+                                              C.POINTER(SolveInfo)]),
     "gdt_fv_apply": (C.c_int, [P, P, C.POINTER(FvDesc), P, P]),
     "gdt_fv_estimate_dt": (C.c_int, [P, P, C.POINTER(FvDesc), P, C.POINTER(C.c_double)]),
     "gdt_fv_timestep": (C.c_int, [P, P, C.POINTER(FvDesc), C.c_int, C.c_double, C.c_int64, C.c_int64, P, P]),

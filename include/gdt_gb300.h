@@ -181,6 +181,21 @@ typedef struct gdt_solve_info {
 gdt_status gdt_solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* opts,
                      gdt_solve_info* info);
 
+/* CG + Jacobi solve (FP64) of a caller-owned CSR system on `stream` that allocates no memory: no
+ * context, no cudaMalloc/cudaFree, no allocating library call. No counterpart in the reference. For
+ * callers that may not allocate device memory themselves or let a library do it: code inside a host
+ * framework that owns all device memory through its own pool, or a time-critical loop that cannot
+ * take cudaMalloc's implicit device synchronisation. Its work vectors live in a fixed file-scope
+ * device array (about 8 MB, held by every GPU that loads the library until exit), so
+ * n <= GDT_NOALLOC_MAX_ROWS; larger n returns GDT_EINVAL (use gdt_solve). The first call on a device
+ * looks the array's address up (make it before any stream capture). All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. x holds the initial guess;
+ * stop when ||b - A x|| <= tol ||b - A x0|| (recursive residual), GDT_ENOCONV after max_iter. */
+#define GDT_NOALLOC_MAX_ROWS 262144
+gdt_status gdt_solve_cg_jacobi_noalloc(const int32_t* row_ptr, const int32_t* col, const double* val, int64_t n,
+                                       const double* b, double* x, double tol, int max_iter, void* stream,
+                                       gdt_solve_info* info);
+
 /* --------------------------------------------------------------- finite volume --- */
 typedef struct gdt_fv_desc {
   int flux;              /* GDT_FLUX_BURGERS: f(u) = u^2/2 (1,..,1); GDT_FLUX_TRANSPORT: f(u) = v u */
