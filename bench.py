@@ -30,6 +30,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "DoF/s assembled+solved at 1e-8 rel err: mixed/batched vs FP64 GPU; SpMV GB/s"
+# kernel classes timed by gdt_context_kernel_timing, in GDT_TIMING_* order
+KERNEL_CLASSES = ["spmv_fp64", "spmv_fp32", "cg_update", "cg_direction", "reliable_update"]
 SEED = 20261205
 
 
@@ -161,7 +163,7 @@ def run_gdt(args):
     import ctypes as C
 
     sched = C.c_int()
-    sched_ms = (C.c_double * 7)()
+    sched_ms = (C.c_double * 8)()
     ctx.call("gdt_matrix_tune", op.handle, C.byref(sched), sched_ms)
     u_ref = op.apply_inverse(rhs, opts={"tol": 1e-14, "max_iter": 200000}).clone()
 
@@ -189,19 +191,28 @@ def run_gdt(args):
         launches = ctx.kernel_launches - launches0
         import ctypes as C
 
-        t64, n64, t32, n32 = C.c_double(), C.c_int64(), C.c_double(), C.c_int64()
-        lib.gdt_context_spmv_timing(ctx.handle, C.byref(t64), C.byref(n64), C.byref(t32), C.byref(n32), 1)
+        kinds = {}
+        for k, name in enumerate(KERNEL_CLASSES):
+            t, c = C.c_double(), C.c_int64()
+            lib.gdt_context_kernel_timing(ctx.handle, k, C.byref(t), C.byref(c), 1)
+            if c.value:
+                kinds[name] = (t.value, c.value)
         lib.gdt_context_set_timing(ctx.handle, 0)
         info = dict(op.last_solve_info)
         err = ((u - u_ref).abs().max() / u_ref.abs().max()).item()
-        return ms, launches, info, err, (t64.value, n64.value, t32.value, n32.value)
+        return ms, launches, info, err, kinds
 
-    # inputs are larger than L2 (FP64 CSR 728 MB per SpMV), so no L2 flush is needed between steps
+    # inputs are larger than L2 (FP64 CSR 728 MB per SpMV), so no L2 flush is needed between steps.
+    # The timed steps run the solvers as launched in production (iterations captured in CUDA graphs);
+    # one further step per precision, outside the timed region, brackets every kernel class with
+    # CUDA events (no graph capture) for the roofline and the per-kernel breakdown.
     clocks = Clocks(local)
     clocks.start()
-    ms_mixed, launches, info_mixed, err_mixed, tm = timed("mixed", args.steps, args.warmup, timing=True)
+    ms_mixed, launches, info_mixed, err_mixed, _ = timed("mixed", args.steps, args.warmup)
     clk = clocks.stop()
-    ms_fp64, _, info_fp64, err_fp64, tm64 = timed("fp64", max(1, args.steps // 2), 1, timing=True)
+    ms_fp64, _, info_fp64, err_fp64, _ = timed("fp64", max(1, args.steps // 2), 1)
+    _, _, _, _, kinds32 = timed("mixed", 1, 0, timing=True)
+    _, _, _, _, kinds64 = timed("fp64", 1, 0, timing=True)
     # replicas: units of all ranks over the slowest rank's time (no collective on the data path)
     ms_mixed = gdt.replicas.max_over_ranks(ms_mixed, device="cuda")
     ms_fp64 = gdt.replicas.max_over_ranks(ms_fp64, device="cuda")
@@ -231,7 +242,7 @@ def run_gdt(args):
     ms_e2e = gdt.replicas.max_over_ranks(e0.elapsed_time(e1) / args.steps, device="cuda")
 
     value = world * ndof / (ms_mixed / 1e3)
-    t64, n64, t32, n32 = tm
+    t32, n32 = kinds32["spmv_fp32"]
     spmv32_ms = t32 / max(n32, 1)
     # FP32 symmetric-stencil SpMV of the inner CG: 14 slot arrays (diagonal + 13 upper neighbours of the
     # 27-point Q1 stencil) streamed once, the iterated vector read once and the product written once
@@ -244,7 +255,7 @@ def run_gdt(args):
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
     achieved = bytes32 / (spmv32_ms / 1e3) / 1e9
-    t64b, n64b = tm64[0], tm64[1]
+    t64b, n64b = kinds64.get("spmv_fp64", (0.0, 0))
     spmv64_ms = t64b / max(n64b, 1)
     bytes64 = 12 * nnz + 4 * (ndof + 1) + 16 * ndof
     line = {
@@ -274,10 +285,14 @@ def run_gdt(args):
         "spmv_autotuner": {"chosen_schedule": sched.value,
                            "ms_per_launch": {name: round(sched_ms[k], 4) for k, name in enumerate(
                                ["csr_vector_g4", "csr_vector_g8", "csr_vector_g16", "csr_vector_g32",
-                                "warp_staged_pl8", "warp_staged_pl16", "warp_staged_pl32"]) if sched_ms[k] > 0}},
+                                "warp_staged_pl8", "warp_staged_pl16", "warp_staged_pl32", "async_staged_28"]) if sched_ms[k] > 0}},
         "e2e": {"value": world * ndof / (ms_e2e / 1e3), "unit": "DoF/s", "h2d_bytes_per_step": 8 * grid.num_elements,
                 "d2h_bytes_per_step": 8 * ndof},
         "gpu_launches": launches,
+        "kernel_ms_per_launch": {
+            "mixed": {k: round(t / c, 5) for k, (t, c) in kinds32.items()},
+            "fp64": {k: round(t / c, 5) for k, (t, c) in kinds64.items()},
+            "note": "CUDA events around each kernel class in one extra solve without graph capture"},
         "roofline": {"bound": "hbm", "kernel": "FP32 symmetric-stencil SpMV of the inner CG (k_mx_spmv)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "bytes_per_launch": bytes32, "avg_launch_ms": spmv32_ms, "launches": n32,

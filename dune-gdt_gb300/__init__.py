@@ -344,6 +344,12 @@ class MatrixOperator:
     def matrix(self):
         return self.csr()
 
+    def set_spmv_schedule(self, schedule):
+        """Pin the SpMV schedule (0 .. capi.SPMV_SCHEDULES-1) of every SpMV-type kernel of this matrix
+        instead of autotuning it; raises GdtError(EINVAL) when it cannot hold the longest row."""
+        capi.check(capi.load().gdt_matrix_set_schedule(self.handle, int(schedule)), what="gdt_matrix_set_schedule")
+        return self
+
     def _diffusion_desc(self, rhs_force=None, dirichlet=False):
         kappa = 1.0
         for f in self.forms:
@@ -609,12 +615,23 @@ class ExplicitRungeKuttaTimeStepper:
         self.op = op
         self.u = initial_values
         self.method = {"ssp2": capi.TIMESTEPPER_SSPRK2, "euler": capi.TIMESTEPPER_EXPLICIT_EULER}[method]
-        self.work = torch.empty_like(initial_values)
+        self.work = torch.empty(0, dtype=torch.float64, device=initial_values.device)
         self.t = 0.0
+
+    def work_doubles(self, nbatch):
+        """Size of the work buffer gdt_fv_timestep needs: the SSP2 stage vector and the next state
+        (2 N per state), or the next state alone for explicit Euler."""
+        n = self.op.space.num_DoFs
+        return (2 if self.method == capi.TIMESTEPPER_SSPRK2 else 1) * nbatch * n
 
     def step(self, dt, steps=1):
         n = self.op.space.num_DoFs
+        if self.u.numel() == 0 or self.u.numel() % n:
+            raise GdtError(capi.ESHAPE, f"state of {self.u.numel()} values is not a batch of {n}-cell states")
+        _f64(self.u, self.u.numel(), "state")
         nbatch = self.u.numel() // n
+        if self.work.numel() < self.work_doubles(nbatch):
+            self.work = torch.empty(self.work_doubles(nbatch), dtype=torch.float64, device=self.u.device)
         self.op.ctx.call("gdt_fv_timestep", self.op.space.handle, C.byref(self.op.desc), self.method,
                          C.c_double(dt), C.c_int64(steps), C.c_int64(nbatch), _ptr(self.u), _ptr(self.work))
         self.t += dt * steps

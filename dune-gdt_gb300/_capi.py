@@ -9,6 +9,9 @@ import os
 
 from . import _build
 
+SPMV_SCHEDULES = 8
+TIMING_SPMV_FP64, TIMING_SPMV_FP32, TIMING_CG_UPDATE, TIMING_CG_DIRECTION, TIMING_RELIABLE_UPDATE = range(5)
+TIMING_KINDS = 8
 OK, EINVAL, ESHAPE, ENOCONV, ETIMEOUT, ENAN, EUNSUPPORTED, ECUDA, ENOMEM = range(9)
 SPACE_CG, SPACE_DG, SPACE_FV = 0, 1, 2
 STENCIL_ELEMENT, STENCIL_INTERSECTION, STENCIL_ELEMENT_AND_INTERSECTION = 0, 1, 2
@@ -69,6 +72,7 @@ _SIGNATURES = {
     "gdt_context_set_timing": (C.c_int, [P, C.c_int]),
     "gdt_context_spmv_timing": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                           C.POINTER(C.c_int64), C.c_int]),
+    "gdt_context_kernel_timing": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int]),
     "gdt_grid_create_cube": (C.c_int, [C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(P)]),
     "gdt_grid_destroy": (C.c_int, [P]),
@@ -87,6 +91,7 @@ _SIGNATURES = {
     "gdt_matrix_device_arrays": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "gdt_matrix_set_zero": (C.c_int, [P, P]),
     "gdt_matrix_tune": (C.c_int, [P, P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "gdt_matrix_set_schedule": (C.c_int, [P, C.c_int]),
     "gdt_assemble_cg_diffusion": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_assemble_cg_rhs": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_dirichlet_apply": (C.c_int, [P, P, P]),

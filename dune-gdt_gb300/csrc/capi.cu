@@ -45,8 +45,8 @@ void timing_harvest(gdt_context ctx) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx->events[k], ctx->events[k + 1]) == cudaSuccess) {
       const int kind = ctx->event_kind[k / 2];
-      ctx->spmv_ms[kind] += ms;
-      ctx->spmv_launches[kind] += 1;
+      ctx->kind_ms[kind] += ms;
+      ctx->kind_launches[kind] += 1;
     }
   }
   ctx->events_used = 0;
@@ -105,14 +105,22 @@ gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp
   if (!ctx) return GDT_EINVAL;
   GDT_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   timing_harvest(ctx);
-  if (fp64_ms) *fp64_ms = ctx->spmv_ms[0];
-  if (fp64_launches) *fp64_launches = ctx->spmv_launches[0];
-  if (fp32_ms) *fp32_ms = ctx->spmv_ms[1];
-  if (fp32_launches) *fp32_launches = ctx->spmv_launches[1];
-  if (reset) {
-    ctx->spmv_ms[0] = ctx->spmv_ms[1] = 0.0;
-    ctx->spmv_launches[0] = ctx->spmv_launches[1] = 0;
-  }
+  if (fp64_ms) *fp64_ms = ctx->kind_ms[GDT_TIMING_SPMV_FP64];
+  if (fp64_launches) *fp64_launches = ctx->kind_launches[GDT_TIMING_SPMV_FP64];
+  if (fp32_ms) *fp32_ms = ctx->kind_ms[GDT_TIMING_SPMV_FP32];
+  if (fp32_launches) *fp32_launches = ctx->kind_launches[GDT_TIMING_SPMV_FP32];
+  if (reset)
+    for (int k = 0; k < GDT_TIMING_KINDS; ++k) ctx->kind_ms[k] = 0.0, ctx->kind_launches[k] = 0;
+  return GDT_OK;
+}
+
+gdt_status gdt_context_kernel_timing(gdt_context ctx, int kind, double* ms, int64_t* launches, int reset) {
+  if (!ctx || kind < 0 || kind >= GDT_TIMING_KINDS) return GDT_EINVAL;
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  timing_harvest(ctx);
+  if (ms) *ms = ctx->kind_ms[kind];
+  if (launches) *launches = ctx->kind_launches[kind];
+  if (reset) ctx->kind_ms[kind] = 0.0, ctx->kind_launches[kind] = 0;
   return GDT_OK;
 }
 

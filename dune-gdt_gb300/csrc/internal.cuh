@@ -40,14 +40,15 @@ struct gdt_context_s {
   unsigned int* counters = nullptr; // kCounters uints (last-block tickets)
   double* host_pinned = nullptr;   // pinned host mirror for convergence checks
   int num_sms = 152;
-  // kernel timing: when on, solver iterations run without graph capture and every SpMV launch is
-  // bracketed by CUDA events on the context stream; durations accumulate per precision
+  // kernel timing: when on, solver iterations run without graph capture and the launches of each
+  // kernel class (GDT_TIMING_*) are bracketed by CUDA events on the launching stream; durations
+  // accumulate per class
   int timing = 0;
   std::vector<cudaEvent_t> events;  // pairs (start, stop)
-  std::vector<int> event_kind;      // 0: FP64 SpMV, 1: FP32 SpMV
+  std::vector<int> event_kind;      // GDT_TIMING_* class of each pair
   size_t events_used = 0;
-  double spmv_ms[2] = {0, 0};
-  long long spmv_launches[2] = {0, 0};
+  double kind_ms[GDT_TIMING_KINDS] = {};
+  long long kind_launches[GDT_TIMING_KINDS] = {};
 };
 
 struct gdt_grid_s {

@@ -419,7 +419,7 @@ template <class T, int MODE>
 void spmv_mode(const Launch& L, const int* rp, const int* col, const T* val, const T* x, T* y, const T* w,
                KState* st) {
   const LaunchShape sh = L.shape<T>();
-  timing_begin(L.ctx, L.s, sizeof(T) == 8 ? 0 : 1);
+  timing_begin(L.ctx, L.s, sizeof(T) == 8 ? GDT_TIMING_SPMV_FP64 : GDT_TIMING_SPMV_FP32);
 #define GDT_K_SPMV(GG, PP) \
   k_spmv<GG, PP, T, MODE><<<sh.blocks, sh.threads, sh.smem, L.s>>>(L.n, rp, col, val, x, y, w, st, L.partials, L.ticket)
   GDT_SCHEDULE_SWITCH(L.sched, GDT_K_SPMV)
@@ -624,8 +624,12 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
         residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
         GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
           spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
+          timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);
           k_cg_update_jacobi<double, double><<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);
+          timing_end(ctx, s);
+          timing_begin(ctx, s, GDT_TIMING_CG_DIRECTION);
           k_cg_p_jacobi<double><<<L.vec_blocks, TH, 0, s>>>(n, p, r, one, st);
+          timing_end(ctx, s);
           ctx->launches += 2;
         }));
       } else {

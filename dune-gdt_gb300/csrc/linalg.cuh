@@ -98,19 +98,107 @@ __device__ __forceinline__ void for_rows_pipelined(int n, const int* __restrict_
   }
 }
 
+// 16-byte asynchronous global -> shared copies (LDGSTS, L2 only) and their group waits
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Asynchronous double-buffered warp staging: each warp owns 32 consecutive rows per step. While it
+// reduces the current slice from one shared-memory buffer, the next slice (values and indices,
+// rounded out to 16-byte boundaries; the CSR arrays carry padding) is already being copied into the
+// other buffer with cp.async. Lane i reduces row r0 + i: one lane per row, so the FP64 instructions
+// per row are the row's FMAs only (no shuffle reductions). Rows of at most CAP entries.
+template <class T, int CAP>
+struct AsyncWindow {
+  static constexpr int VE = 16 / sizeof(T);            // values per 16-byte chunk
+  static constexpr int VCAP = 32 * CAP + 2 * VE;       // values per buffer (slack for alignment)
+  static constexpr int CCAP = 32 * CAP + 8;            // indices per buffer
+  static constexpr size_t bytes_per_warp = 2 * (VCAP * sizeof(T) + CCAP * sizeof(int));
+};
+
+template <class T, int CAP, class Body>
+__device__ __forceinline__ void for_rows_async(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                               const T* __restrict__ val, const T* __restrict__ x, Body body) {
+  using W = AsyncWindow<T, CAP>;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  unsigned char* const base = gdt_dyn_smem + warp * W::bytes_per_warp;
+  auto vbuf = [&](int b) { return reinterpret_cast<T*>(base + b * (W::VCAP * sizeof(T))); };
+  auto cbuf = [&](int b) {
+    return reinterpret_cast<int*>(base + 2 * W::VCAP * sizeof(T) + b * (W::CCAP * sizeof(int)));
+  };
+  const int step = gridDim.x * wpb * 32;
+  // stage the slice of rows [r, r+32) into buffer b; returns this lane's row bounds and the slice's
+  // aligned (value, index) start offsets. Warp-uniform: every lane calls it.
+  auto stage = [&](int r, int b, int& rbeg, int& rend, int& vb, int& cb) {
+    const int row = r + lane;
+    rbeg = row < n ? rp[row] : 0;
+    rend = row < n ? rp[row + 1] : 0;
+    const int last = (n - 1 - r) < 31 ? (n - 1 - r) : 31;
+    const int beg = __shfl_sync(0xffffffffu, rbeg, 0);
+    const int end = __shfl_sync(0xffffffffu, rend, last);
+    vb = beg & ~(W::VE - 1);
+    cb = beg & ~3;
+    const int nv = (end - vb + W::VE - 1) / W::VE, nc = (end - cb + 3) / 4;
+    T* dv = vbuf(b);
+    int* dc = cbuf(b);
+    for (int k = lane; k < nv; k += 32) cp_async16(dv + k * W::VE, val + vb + k * W::VE);
+    for (int k = lane; k < nc; k += 32) cp_async16(dc + k * 4, col + cb + k * 4);
+    cp_async_commit();
+  };
+  int r0 = (blockIdx.x * wpb + warp) * 32;
+  int rb = 0, re = 0, vb = 0, cb = 0, cur = 0;
+  if (r0 < n) stage(r0, 0, rb, re, vb, cb);
+  for (; r0 < n; r0 += step, cur ^= 1) {
+    const bool more = r0 + step < n;
+    int rb2 = 0, re2 = 0, vb2 = 0, cb2 = 0;
+    if (more) {
+      stage(r0 + step, cur ^ 1, rb2, re2, vb2, cb2);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncwarp();
+    const int row = r0 + lane;
+    const bool active = row < n;
+    const T* wv = vbuf(cur) + (rb - vb);
+    const int* wc = cbuf(cur) + (rb - cb);
+    const int len = re - rb;
+    T s0 = T(0), s1 = T(0);
+#pragma unroll
+    for (int j = 0; j < CAP; j += 2) {
+      if (j < len) s0 = fma(wv[j], __ldg(x + wc[j]), s0);
+      if (j + 1 < len) s1 = fma(wv[j + 1], __ldg(x + wc[j + 1]), s1);
+    }
+    body(row, active, s0 + s1);
+    __syncwarp();  // the buffer just read is refilled by the next stage
+    rb = rb2, re = re2, vb = vb2, cb = cb2;
+  }
+}
+
 // SpMV schedules: PL == 0 -> vector-CSR with G lanes per row; PL > 0 -> pipelined warp staging with
-// PL entries per lane (rows of at most PL entries). Chosen per matrix by the autotuner.
+// PL entries per lane; PL < 0 -> asynchronous double-buffered staging for rows of at most -PL
+// entries. Chosen per matrix by the autotuner.
 template <int G, int PL, class T, class Body>
 __device__ __forceinline__ void for_rows_csr(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                              const T* __restrict__ val, const T* __restrict__ x, Body body) {
   if constexpr (PL > 0) for_rows_pipelined<T, PL>(n, rp, col, val, x, body);
+  else if constexpr (PL < 0) for_rows_async<T, -PL>(n, rp, col, val, x, body);
   else for_rows<G, T>(n, rp, col, val, x, body);
 }
 
 // the schedule table: index -> (G, PL)
-constexpr int kSchedules = 7;
+constexpr int kSchedules = 8;
 __host__ __device__ constexpr int sched_G(int s) { return s == 0 ? 4 : s == 1 ? 8 : s == 2 ? 16 : s == 3 ? 32 : 0; }
-__host__ __device__ constexpr int sched_PL(int s) { return s == 4 ? 8 : s == 5 ? 16 : s == 6 ? 32 : 0; }
+__host__ __device__ constexpr int sched_PL(int s) {
+  return s == 4 ? 8 : s == 5 ? 16 : s == 6 ? 32 : s == 7 ? -28 : 0;
+}
 
 // expands F<G, PL> for a runtime schedule index
 #define GDT_SCHEDULE_SWITCH(sched, F)  \
@@ -121,7 +209,8 @@ __host__ __device__ constexpr int sched_PL(int s) { return s == 4 ? 8 : s == 5 ?
     case 3: F(32, 0); break;           \
     case 4: F(0, 8); break;            \
     case 5: F(0, 16); break;           \
-    default: F(0, 32); break;          \
+    case 6: F(0, 32); break;           \
+    default: F(0, -28); break;         \
   }
 
 struct LaunchShape {
@@ -133,14 +222,20 @@ template <class T>
 inline LaunchShape schedule_shape(int sched, long long n, int num_sms) {
   LaunchShape s;
   const int PL = sched_PL(sched);
-  if (PL > 0) {
-    const size_t per_warp = size_t(32) * PL * (sizeof(T) + sizeof(int));
-    int warps = int((48 * 1024) / per_warp);  // within the default 48 KB of dynamic shared memory
+  if (PL != 0) {
+    const size_t per_warp = PL > 0 ? size_t(32) * PL * (sizeof(T) + sizeof(int))
+                                   : AsyncWindow<T, -sched_PL(7)>::bytes_per_warp;
+    // the default limit is 48 KB of shared memory per block, static included: the solver kernels
+    // that fuse a grid reduction into the SpMV hold up to 1 KB of static reduction buffers
+    int warps = int((47 * 1024) / per_warp);
     warps = warps > 4 ? 4 : (warps < 1 ? 1 : warps);
     s.threads = 32 * warps;
     s.smem = size_t(warps) * per_warp;
     const long long b = (n + s.threads - 1) / s.threads;
-    s.blocks = int(b < num_sms * 16 ? b : num_sms * 16);
+    // the asynchronous schedule streams its rows per warp, so no more blocks than fit at once
+    const int resident = PL > 0 ? 16 : int((220 * 1024) / (s.smem + 1024));
+    const long long cap = (long long)num_sms * (resident > 16 ? 16 : (resident < 1 ? 1 : resident));
+    s.blocks = int(b < cap ? b : cap);
   } else {
     const int G = sched_G(sched);
     s.threads = 256;
@@ -156,6 +251,7 @@ inline LaunchShape schedule_shape(int sched, long long n, int num_sms) {
 // schedules usable for a matrix whose longest row has max_row entries
 inline bool schedule_valid(int sched, int max_row) {
   const int PL = sched_PL(sched);
+  if (PL < 0) return max_row > 0 && max_row <= -PL;
   return PL == 0 || (max_row > 0 && max_row <= PL);
 }
 

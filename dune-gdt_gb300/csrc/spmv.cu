@@ -1,9 +1,10 @@
 // CSR SpMV y = A x (ConstMatrixOperator::apply, operators/matrix-based.hh:121-129) and the SpMV
 // schedule autotuner.
 //
-// Schedules (linalg.cuh): vector-CSR with G in {4, 8, 16, 32} lanes per row, or register-pipelined
-// warp staging with PL in {8, 16, 32} entries per lane. The first SpMV-type call on a matrix times
-// every schedule valid for its longest row with CUDA events (FP64, three launches each, after one
+// Schedules (linalg.cuh): vector-CSR with G in {4, 8, 16, 32} lanes per row, register-pipelined
+// warp staging with PL in {8, 16, 32} entries per lane, or cp.async double-buffered warp staging for
+// rows of at most 28 entries. The first SpMV-type call on a matrix times every schedule valid for its
+// longest row with CUDA events (FP64, on a non-trivial probe vector, three launches each, after one
 // warm-up) and keeps the fastest; all SpMV-type kernels of that matrix (plain, fused dot, residual,
 // mixed-precision residual) then use it.
 #include <cfloat>
@@ -35,6 +36,12 @@ template void launch_spmv<double>(int, int, const int*, const int*, const double
 template void launch_spmv<float>(int, int, const int*, const int*, const float*, const float*, float*, int,
                                  cudaStream_t);
 
+// probe vector of the autotuner: non-trivial values (an all-zero x would time the FMAs on zero operands)
+__global__ void k_probe_vector(int n, double* __restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = 1.0 + 0.001 * double(i % 997);
+}
+
 gdt_status tune_spmv(gdt_context ctx, gdt_matrix m, double* times_ms) {
   if (m->tuned && !times_ms) return GDT_OK;
   if (times_ms)
@@ -44,7 +51,7 @@ gdt_status tune_spmv(gdt_context ctx, gdt_matrix m, double* times_ms) {
   double *x = nullptr, *y = nullptr;
   GDT_TRY_CUDA(ctx, cudaMallocAsync(&x, sizeof(double) * std::max(n, 1), s));
   GDT_TRY_CUDA(ctx, cudaMallocAsync(&y, sizeof(double) * std::max(n, 1), s));
-  GDT_TRY_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * std::max(n, 1), s));
+  k_probe_vector<<<std::max(1, std::min(grid_blocks(n, 256), ctx->num_sms * 8)), 256, 0, s>>>(n, x);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -77,7 +84,7 @@ gdt_status tune_spmv(gdt_context ctx, gdt_matrix m, double* times_ms) {
 
 gdt_status spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y) {
   GDT_CHECK(ctx, tune_spmv(ctx, m));
-  timing_begin(ctx, ctx->stream, 0);
+  timing_begin(ctx, ctx->stream, GDT_TIMING_SPMV_FP64);
   launch_spmv<double>(m->spmv_sched, int(m->rows), m->rp, m->col, m->val, x, y, ctx->num_sms, ctx->stream);
   timing_end(ctx, ctx->stream);
   return check_launch(ctx, "spmv");
@@ -90,5 +97,14 @@ extern "C" gdt_status gdt_matrix_tune(gdt_context ctx, gdt_matrix m, int* schedu
   m->tuned = 0;
   GDT_CHECK(ctx, gdt::tune_spmv(ctx, m, times_ms));
   if (schedule) *schedule = m->spmv_sched;
+  return GDT_OK;
+}
+
+extern "C" gdt_status gdt_matrix_set_schedule(gdt_matrix m, int schedule) {
+  static_assert(gdt::kSchedules == GDT_SPMV_SCHEDULES, "schedule table and header disagree");
+  if (!m || schedule < 0 || schedule >= gdt::kSchedules || !gdt::schedule_valid(schedule, m->max_row))
+    return GDT_EINVAL;
+  m->spmv_sched = schedule;
+  m->tuned = 1;
   return GDT_OK;
 }

@@ -79,11 +79,23 @@ const char* gdt_status_string(gdt_status s);
 int64_t gdt_context_kernel_launches(gdt_context ctx);
 /* kernel timing (tracing aid, no reference counterpart beyond Dune::Timer around solves,
  * test/stationary-eocstudies/base.hh:221-225): while enabled, solver iterations are launched without
- * graph capture and every SpMV launch is bracketed by CUDA events on the context stream. */
+ * graph capture and the launches of each kernel class (GDT_TIMING_*) are bracketed by CUDA events on
+ * the context stream. */
 gdt_status gdt_context_set_timing(gdt_context ctx, int enable);
 /* accumulated SpMV kernel time (ms) and launch counts since the last reset, FP64 and FP32 separately */
 gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp64_launches, double* fp32_ms,
                                    int64_t* fp32_launches, int reset);
+/* kernel classes timed while timing is on */
+#define GDT_TIMING_SPMV_FP64 0      /* CSR SpMV and the SpMV-fused solver kernels, FP64 */
+#define GDT_TIMING_SPMV_FP32 1      /* FP32 SpMV of the mixed-precision inner iterations */
+#define GDT_TIMING_CG_UPDATE 2      /* x += alpha p, r -= alpha q and their dot products */
+#define GDT_TIMING_CG_DIRECTION 3   /* p = M^-1 r + beta p */
+#define GDT_TIMING_RELIABLE_UPDATE 4 /* FP64 accumulation and true residual (launched every inner
+                                      * iteration, working only when a replacement is due) */
+#define GDT_TIMING_KINDS 8
+/* accumulated time (ms) and launch count of one kernel class since its last reset (all classes are
+ * reset by gdt_context_spmv_timing with reset = 1) */
+gdt_status gdt_context_kernel_timing(gdt_context ctx, int kind, double* ms, int64_t* launches, int reset);
 
 /* --------------------------------------------------------------------- grid --- */
 /* make_cube_grid(lower_left, upper_right, num_elements): equidistant YaspGrid-like cube grid
@@ -118,9 +130,14 @@ gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m);
 /* SpMV schedule autotuner (no reference counterpart; the reference's ISTL BCRS has one schedule):
  * times every valid SpMV schedule on this matrix with CUDA events and keeps the fastest for all
  * SpMV-type kernels of the matrix. Runs automatically on the first SpMV-type call; schedule (may be
- * NULL) receives the chosen index, times_ms (may be NULL, 7 entries) the measured ms per launch of
- * each schedule (-1 where a schedule does not apply). */
+ * NULL) receives the chosen index, times_ms (may be NULL, GDT_SPMV_SCHEDULES entries) the measured ms
+ * per launch of each schedule (-1 where a schedule does not apply). */
 gdt_status gdt_matrix_tune(gdt_context ctx, gdt_matrix m, int* schedule, double* times_ms);
+/* Pins the SpMV schedule of m (0 .. GDT_SPMV_SCHEDULES-1; no reference counterpart) instead of
+ * tuning it. GDT_EINVAL when the index is out of range or the schedule cannot hold the matrix's
+ * longest row (the staged schedules take rows of at most 8, 16, 32 and 28 entries). */
+#define GDT_SPMV_SCHEDULES 8
+gdt_status gdt_matrix_set_schedule(gdt_matrix m, int schedule);
 
 /* ----------------------------------------------------------------- assembly --- */
 typedef struct gdt_diffusion_desc {
@@ -209,7 +226,12 @@ gdt_status gdt_fv_apply(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, 
 /* dt of estimate_dt_for_hyperbolic_system for initial data u0 (host result) */
 gdt_status gdt_fv_estimate_dt(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, const double* u0, double* dt);
 /* `steps` explicit steps in place on a batch of `nbatch` states stored one after another
- * (u[b * N + cell]); work must hold nbatch * N doubles. */
+ * (u[b * N + cell]); work must hold nbatch * N doubles for GDT_TIMESTEPPER_EXPLICIT_EULER and
+ * 2 * nbatch * N doubles for GDT_TIMESTEPPER_SSPRK2 (the stage vector k0 and the next state: both
+ * stages read the neighbours' values, so neither can be updated in place).
+ * GDT_FV_WORK_DOUBLES gives the size. */
+#define GDT_FV_WORK_DOUBLES(timestepper, nbatch, N) \
+  ((timestepper) == GDT_TIMESTEPPER_SSPRK2 ? 2 * (nbatch) * (N) : (nbatch) * (N))
 gdt_status gdt_fv_timestep(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, int timestepper, double dt,
                            int64_t steps, int64_t nbatch, double* u, double* work);
 

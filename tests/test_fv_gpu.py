@@ -123,3 +123,33 @@ def test_burgers_1d_tables_on_gpu(gdt, oracle, golden, flux):
         assert float("%.2e" % (dt / fv_dt)) == pytest.approx(res["quantity.CFL"][lvl], rel=1e-12)
         m0 = u0.sum() / n
         assert max(abs(m - m0) / m0 for m in masses) < 1e-14
+
+
+@pytest.mark.parametrize("dim,n", [(1, [37]), (2, [40, 33]), (3, [9, 7, 6])])
+@pytest.mark.parametrize("method", ["euler", "ssp2"])
+def test_fv_timestep_stays_inside_its_work_buffer(gdt, oracle, dim, n, method):
+    # gdt_fv_timestep through the C ABI with a work buffer of exactly GDT_FV_WORK_DOUBLES doubles,
+    # followed by a guard band of sentinels inside the same allocation: the guard must come back intact
+    import ctypes as C
+
+    g = gdt.make_cube_grid([0] * dim, [1] * dim, n, periodic=True)
+    og = oracle.grid(dim, n, 0.0, 1.0, periodic=True)
+    op, space = _op(gdt, g, "burgers", "lf", dim)
+    N, nbatch = space.num_DoFs, 2
+    states = [_bumps(dim, n, s) for s in (11, 12)]
+    u = torch.tensor(np.concatenate(states), device="cuda")
+    stepper = gdt.ExplicitRungeKuttaTimeStepper(op, u, method=method)
+    need = stepper.work_doubles(nbatch)
+    assert need == (2 if method == "ssp2" else 1) * nbatch * N
+    guard = 4096
+    buf = torch.full((need + guard,), 1.2345e300, dtype=torch.float64, device="cuda")
+    dt = 0.4 * min(oracle.fv_estimate_dt(og, oracle.FLUX_BURGERS, s) for s in states)
+    tsm = gdt._capi.TIMESTEPPER_SSPRK2 if method == "ssp2" else gdt._capi.TIMESTEPPER_EXPLICIT_EULER
+    op.ctx.call("gdt_fv_timestep", space.handle, C.byref(op.desc), tsm, C.c_double(dt), C.c_int64(7),
+                C.c_int64(nbatch), C.c_void_p(u.data_ptr()), C.c_void_p(buf.data_ptr()))
+    torch.cuda.synchronize()
+    assert bool((buf[need:] == 1.2345e300).all()), "gdt_fv_timestep wrote past its documented work size"
+    step_ref = oracle.fv_ssprk2 if method == "ssp2" else oracle.fv_explicit_euler
+    out = u.cpu().numpy().reshape(nbatch, -1)
+    for b, s in enumerate(states):
+        assert rel_err(out[b], step_ref(og, oracle.FLUX_BURGERS, oracle.NUMFLUX_LAX_FRIEDRICHS, s, dt, 7)) < 1e-12
