@@ -406,14 +406,8 @@ class MatrixOperator:
         self.ctx.call("gdt_spmv", self.handle, _ptr(source), _ptr(_f64(range, n, "range")))
         return range
 
-    def apply_inverse(self, range, source=None, opts=None):
-        """Solve A source = range; opts: type ('cg'|'bicgstab'), precond ('jacobi'|'ilu0'|'none'),
-        precision ('fp64'|'mixed'), tol (relative residual), max_iter, check_every, inner_tol."""
-        opts = dict(opts or {})
-        n = self.shape[0]
-        _f64(range, n, "range")
-        if source is None:
-            source = torch.zeros(n, dtype=torch.float64, device=self.ctx.device)
+    @staticmethod
+    def _solver_opts(opts):
         o = capi.SolverOpts()
         o.solver = {"cg": capi.SOLVER_CG, "bicgstab": capi.SOLVER_BICGSTAB}[opts.get("type", "cg")]
         o.precond = {"none": capi.PREC_NONE, "jacobi": capi.PREC_JACOBI, "ilu0": capi.PREC_ILU0}[
@@ -423,6 +417,35 @@ class MatrixOperator:
         o.max_iter = int(opts.get("max_iter", 100000))
         o.check_every = int(opts.get("check_every", 0))
         o.inner_tol = float(opts.get("inner_tol", 0.0))
+        return o
+
+    def apply_inverse(self, range, source=None, opts=None):
+        """Solve A source = range; opts: type ('cg'|'bicgstab'), precond ('jacobi'|'ilu0'|'none'),
+        precision ('fp64'|'mixed'), tol (relative residual), max_iter, check_every, inner_tol.
+
+        type 'newton' runs the damped Newton of OperatorInterface::apply_inverse on x -> A x - range
+        (keys precision, max_iter, max_dampening_iter as in the reference, and 'jacobian': the linear
+        solver options of the defect systems); `source` is the initial guess."""
+        opts = dict(opts or {})
+        n = self.shape[0]
+        _f64(range, n, "range")
+        if source is None:
+            source = torch.zeros(n, dtype=torch.float64, device=self.ctx.device)
+        if opts.get("type") == "newton":
+            no = capi.load().gdt_newton_default_opts()
+            no.precision = float(opts.get("precision", no.precision))
+            no.max_iter = int(opts.get("max_iter", no.max_iter))
+            no.max_dampening_iter = int(opts.get("max_dampening_iter", no.max_dampening_iter))
+            if "jacobian" in opts:
+                no.jacobian_solver = self._solver_opts(dict(opts["jacobian"]))
+            ninfo = capi.NewtonInfo()
+            self.ctx.call("gdt_newton_solve", self.handle, _ptr(range), _ptr(_f64(source, n, "source")), C.byref(no),
+                          C.byref(ninfo))
+            self.last_solve_info = {"iterations": ninfo.iterations, "dampening_steps": ninfo.dampening_steps,
+                                    "linear_iterations": ninfo.linear_iterations, "residual": ninfo.residual,
+                                    "converged": True}
+            return source
+        o = self._solver_opts(opts)
         info = capi.SolveInfo()
         self.ctx.call("gdt_solve", self.handle, _ptr(range), _ptr(_f64(source, n, "source")), C.byref(o),
                       C.byref(info))

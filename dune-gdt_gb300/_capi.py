@@ -44,6 +44,16 @@ class SolveInfo(C.Structure):
                 ("converged", C.c_int)]
 
 
+class NewtonOpts(C.Structure):
+    _fields_ = [("precision", C.c_double), ("max_iter", C.c_int), ("max_dampening_iter", C.c_int),
+                ("jacobian_solver", SolverOpts)]
+
+
+class NewtonInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("dampening_steps", C.c_int), ("linear_iterations", C.c_int),
+                ("residual", C.c_double)]
+
+
 class FvDesc(C.Structure):
     _fields_ = [("flux", C.c_int), ("velocity", C.c_double * 3), ("numflux", C.c_int), ("lf_lambda", C.c_double)]
 
@@ -98,6 +108,8 @@ _SIGNATURES = {
     "gdt_assemble_swipdg": (C.c_int, [P, P, C.POINTER(IpdgDesc), P]),
     "gdt_spmv": (C.c_int, [P, P, P, P]),
     "gdt_solve": (C.c_int, [P, P, P, P, C.POINTER(SolverOpts), C.POINTER(SolveInfo)]),
+    "gdt_newton_default_opts": (NewtonOpts, []),
+    "gdt_newton_solve": (C.c_int, [P, P, P, P, C.POINTER(NewtonOpts), C.POINTER(NewtonInfo)]),
     "gdt_solve_cg_jacobi_noalloc": (C.c_int, [P, P, P, C.c_int64, P, P, C.c_double, C.c_int, P,
                                               C.POINTER(SolveInfo)]),
     "gdt_fv_apply": (C.c_int, [P, P, C.POINTER(FvDesc), P, P]),

@@ -249,6 +249,15 @@ class MatrixOperator {
   void apply(const DeviceVector& source, DeviceVector& range) const {
     check(gdt_spmv(default_context(), handle(), source.data(), range.data()), default_context(), "apply");
   }
+  // OperatorInterface::apply_inverse(range, source, {{"type", "newton"}, ...}): damped Newton on
+  // x -> A x - range, source is the initial guess (operators/interfaces.hh:490-599)
+  gdt_newton_info apply_inverse(const DeviceVector& range, DeviceVector& source,
+                                gdt_newton_opts opts = gdt_newton_default_opts()) const {
+    gdt_newton_info info{};
+    check(gdt_newton_solve(default_context(), handle(), range.data(), source.data(), &opts, &info), default_context(),
+          "apply_inverse");
+    return info;
+  }
 
  private:
   Space<d> space_;

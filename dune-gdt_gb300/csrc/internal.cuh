@@ -74,6 +74,7 @@ struct gdt_matrix_s {
   int max_row = 0;     // longest row
   int spmv_sched = 1;  // SpMV schedule (see linalg.cuh), picked by tune_spmv on first use
   int tuned = 0;
+  int mx_tiled = -1;   // mixed solver, 3D grids: plane-tiled (1) or linear (0) FP32 stencil SpMV, timed on first use
 };
 
 namespace gdt {
@@ -122,6 +123,9 @@ gdt_status tune_spmv(gdt_context ctx, gdt_matrix m, double* times_ms = nullptr);
 // krylov.cu
 gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
                  gdt_solve_info* info);
+// newton.cu
+gdt_status newton_solve(gdt_context ctx, gdt_matrix m, const double* range, double* x, const gdt_newton_opts* o,
+                        gdt_newton_info* info);
 // mixed.cu: FP32 symmetric-stencil CG with FP64 reliable updates (structured continuous spaces)
 bool mixed_stencil_supported(gdt_matrix m);
 gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,

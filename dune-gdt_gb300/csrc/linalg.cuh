@@ -103,6 +103,12 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+// 4-byte asynchronous copy; when `valid` is false nothing is read and the word is zero-filled
+__device__ __forceinline__ void cp_async4_zfill(void* smem, const void* gmem, bool valid) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  const int bytes = valid ? 4 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -323,6 +329,108 @@ inline gdt_status iterate_chunks(gdt_context ctx, cudaStream_t s, const int* con
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   return GDT_OK;
+}
+
+// Conditional section of a captured iteration. Kernels launched between begin() and end() become the
+// body of a graph IF node: they run only when a kernel earlier in the same iteration (given the
+// handle from next_handle()) set the condition with cudaGraphSetConditional; otherwise the graph
+// skips them without a launch. Outside capture (timing mode, or when capture is unavailable) handles
+// are 0 and begin() returns the main stream: the kernels are launched every iteration and must
+// check the same device-side flag themselves.
+struct CondSection {
+  cudaStream_t main = nullptr, side = nullptr;
+  bool capturing = false;
+  cudaError_t err = cudaSuccess;
+  cudaGraphConditionalHandle next_handle() {
+    if (!capturing) return 0;
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle h = 0;
+    if (err == cudaSuccess) err = cudaStreamGetCaptureInfo(main, &st, nullptr, &g, nullptr, nullptr, nullptr);
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    return h;
+  }
+  cudaStream_t begin(cudaGraphConditionalHandle h) {
+    if (!capturing) return main;
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (err == cudaSuccess) err = cudaStreamGetCaptureInfo(main, &st, nullptr, &g, &deps, nullptr, &nd);
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, g, deps, nullptr, nd, &p);
+    if (err == cudaSuccess)
+      err = cudaStreamUpdateCaptureDependencies(main, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (err == cudaSuccess)
+      err = cudaStreamBeginCaptureToGraph(side, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    side_active = err == cudaSuccess;
+    // after a failure the kernels go into the main capture, which is then discarded
+    return side_active ? side : main;
+  }
+  void end() {
+    if (!side_active) return;
+    side_active = false;
+    cudaGraph_t body = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(side, &body);
+    if (err == cudaSuccess) err = e;
+  }
+  bool side_active = false;
+};
+
+// iterate_chunks for a body(CondSection&) with a conditional section; *graphed tells whether the
+// iterations ran as graphs (conditional kernels then launched only when their condition was set)
+template <class Body>
+inline gdt_status iterate_chunks_cond(gdt_context ctx, cudaStream_t s, const int* converged, int chunk,
+                                      int max_chunks, bool* graphed, Body body) {
+  CondSection cs;
+  cs.main = s;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  bool use_graph = !ctx->timing && cudaStreamCreateWithFlags(&cs.side, cudaStreamNonBlocking) == cudaSuccess;
+  const long long before = ctx->launches;
+  if (use_graph && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    cs.capturing = true;
+    for (int k = 0; k < chunk; ++k) body(cs);
+    const cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess || cs.err != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+      use_graph = false;
+  } else {
+    use_graph = false;
+  }
+  cs.capturing = false;
+  const long long per_chunk = ctx->launches - before;
+  ctx->launches = before;
+  cudaGetLastError();
+  if (graphed) *graphed = use_graph;
+  int* flag = reinterpret_cast<int*>(ctx->host_pinned);
+  gdt_status status = GDT_OK;
+  for (int c = 0; c < max_chunks; ++c) {
+    cudaError_t e = cudaSuccess;
+    if (use_graph) {
+      e = cudaGraphLaunch(exec, s);
+      ctx->launches += per_chunk;
+    } else {
+      for (int k = 0; k < chunk; ++k) body(cs);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(flag, converged, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      status = fail(ctx, GDT_ECUDA, std::string("solver iterations: ") + cudaGetErrorString(e));
+      break;
+    }
+    if (ctx->timing) timing_harvest(ctx);
+    if (*flag) break;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (cs.side) cudaStreamDestroy(cs.side);
+  return status;
 }
 
 }  // namespace gdt

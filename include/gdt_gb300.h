@@ -198,6 +198,29 @@ typedef struct gdt_solve_info {
 gdt_status gdt_solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* opts,
                      gdt_solve_info* info);
 
+/* OperatorInterface::apply_inverse with type "newton" (operators/interfaces.hh:490-599) for the affine
+ * residual operator x -> A x - range, as the EOC studies invert `lhs - rhs`
+ * (test/stationary-eocstudies/base.hh:186-191). x is the initial guess and receives the solution.
+ * Damped Newton with the automatic damping of the reference; the Jacobian is A and the defect systems
+ * are solved by gdt_solve with `jacobian_solver` (its tol is replaced by 0.1 * precision, as the
+ * reference passes to its linear solvers). GDT_ENOCONV (the reference's operator_error) when max_iter
+ * steps or max_dampening_iter halvings do not suffice. */
+typedef struct gdt_newton_opts {
+  double precision;                /* stop when ||A x - range||_2 < precision (reference default 1e-7) */
+  int max_iter;                    /* Newton steps (reference default 100) */
+  int max_dampening_iter;          /* damping halvings per step (reference default: that of max_iter, 100) */
+  gdt_solver_opts jacobian_solver; /* default: CG + Jacobi, FP64 */
+} gdt_newton_opts;
+typedef struct gdt_newton_info {
+  int iterations;        /* Newton steps taken */
+  int dampening_steps;   /* halvings of the damping parameter, summed over the steps */
+  int linear_iterations; /* Krylov iterations, summed over the steps */
+  double residual;       /* final ||A x - range||_2 */
+} gdt_newton_info;
+gdt_newton_opts gdt_newton_default_opts(void);
+gdt_status gdt_newton_solve(gdt_context ctx, gdt_matrix m, const double* range, double* x, const gdt_newton_opts* opts,
+                            gdt_newton_info* info);
+
 /* CG + Jacobi solve (FP64) of a caller-owned CSR system on `stream` that allocates no memory: no
  * context, no cudaMalloc/cudaFree, no allocating library call. No counterpart in the reference. For
  * callers that may not allocate device memory themselves or let a library do it: code inside a host

@@ -156,6 +156,48 @@ def test_mixed_precision_refinement_reaches_fp64_accuracy(gdt, oracle):
     assert rel_err(x.cpu().numpy(), xd) < 1e-9
 
 
+@pytest.mark.parametrize("n,simplex", [([37, 11, 6], False), ([13, 9, 7], True), ([40, 2, 9], True),
+                                       ([1, 5, 6], False), ([33, 8, 3], False)])
+def test_mixed_precision_3d_grids_match_direct(gdt, oracle, n, simplex):
+    # 3D vertex grids run the plane-tiled FP32 stencil SpMV (ragged 32 x 8 tiles, z chunks); grids
+    # only one cell wide fall back to the linear stencil kernel
+    op, rhs, A, b = _heat_problem(gdt, oracle, 3, n, simplex)
+    xd = spl.spsolve(A.to_scipy().tocsc(), b)
+    x = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+    assert op.last_solve_info["converged"]
+    assert rel_err(x.cpu().numpy(), xd) < 1e-9
+
+
+@pytest.mark.parametrize("dim,n,simplex", [(2, [24, 20], True), (3, [9, 8, 7], False)])
+def test_newton_apply_inverse_matches_direct(gdt, oracle, dim, n, simplex):
+    # OperatorInterface::apply_inverse, type "newton" (operators/interfaces.hh:490-599) on the affine
+    # residual operator x -> A x - b: one undamped step with an exact-enough defect solve
+    op, rhs, A, b = _heat_problem(gdt, oracle, dim, n, simplex)
+    xd = spl.spsolve(A.to_scipy().tocsc(), b)
+    x = op.apply_inverse(rhs, opts={"type": "newton", "precision": 1e-10})
+    info = op.last_solve_info
+    assert info["iterations"] == 1 and info["dampening_steps"] == 0 and info["linear_iterations"] > 0
+    assert info["residual"] < 1e-10
+    assert np.linalg.norm(A.to_scipy() @ x.cpu().numpy() - b) < 1e-10
+    assert rel_err(x.cpu().numpy(), xd) < 1e-8
+    # the reference's defaults (precision 1e-7, max_iter 100) and an initial guess already at the solution
+    x2 = op.apply_inverse(rhs, x.clone(), opts={"type": "newton"})
+    assert op.last_solve_info["iterations"] == 0
+    assert torch.equal(x2, x)
+
+
+def test_newton_reports_operator_error(gdt, oracle):
+    op, rhs, A, b = _heat_problem(gdt, oracle, 2, [16, 16], False)
+    with pytest.raises(gdt.GdtError) as e:
+        op.apply_inverse(rhs, opts={"type": "newton", "max_iter": 0})
+    assert e.value.status == gdt._capi.ENOCONV
+    # the defect system cannot be solved (one Krylov iteration allowed)
+    with pytest.raises(gdt.GdtError) as e:
+        op.apply_inverse(rhs, opts={"type": "newton", "jacobian": {"max_iter": 1}})
+    assert e.value.status == gdt._capi.ENOCONV
+    assert "defect" in str(e.value)
+
+
 def test_solver_reports_non_convergence(gdt, oracle):
     op, rhs, A, b = _heat_problem(gdt, oracle, 2, [30, 30], False)
     with pytest.raises(gdt.GdtError) as e:

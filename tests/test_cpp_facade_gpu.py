@@ -18,6 +18,9 @@ def test_stationary_heat_equation_example(gdt):
         out = subprocess.run([exe, str(cells)], capture_output=True, text=True, timeout=300, check=True).stdout
         fields = out.split()
         assert int(fields[1]) == (cells + 1) ** 2
+        # Newton on x -> A x - b (OperatorInterface::apply_inverse) reaches the CG solution in one step
+        assert fields[6] == "newton_steps" and int(fields[7]) == 1
+        assert float(fields[9]) < 1e-8
         errs.append(float(fields[-1]))
     # second-order convergence of the vertex error (element-barycentre source lowering)
     assert errs[1] < errs[0] / 3.0
