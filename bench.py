@@ -45,13 +45,16 @@ def parse():
     p.add_argument("--tol", type=float, default=1e-11, help="relative residual stop of both solvers")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-iters", type=int, default=60, help="CG iterations timed in the CPU sample")
-    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv"],
+    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg"],
                    help="heat3d: the headline 128^3 workload; batched: 512 parametric P1 problems of uneven "
-                        "size in one persistent launch; fv: 2D Burgers FV, SSP-RK2")
+                        "size in one persistent launch; fv: 2D Burgers FV, SSP-RK2; swipdg: SWIPDG P1 "
+                        "forward solve + adjoint log-kappa gradient on 256^2 squares")
     p.add_argument("--problems", type=int, default=512, help="batched: number of problems")
     p.add_argument("--fv-n", type=int, default=4096, help="fv: cells per axis")
     p.add_argument("--fv-steps", type=int, default=500, help="fv: SSP-RK2 steps per bench step")
     p.add_argument("--fv-batch", type=int, default=1, help="fv: independent initial conditions")
+    p.add_argument("--dg-n", type=int, default=256, help="swipdg: squares per axis (2 triangles each)")
+    p.add_argument("--dg-fd", type=int, default=16, help="swipdg: elements of the finite-difference check")
     return p.parse_args()
 
 
@@ -411,6 +414,108 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------ SWIPDG (config 4) ---
+def run_swipdg(args):
+    """SWIPDG P1 on n^2 squares split into triangles (theta = 1, omega = kappa, sigma 8 / 14), log kappa
+    ~ N(0,1) plus horizontal stripes 8 cells wide with kappa x 1e4, f = 1; one step = forward assemble +
+    solve, J = 0.5 ||u - u_d||^2 and its log-kappa gradient (adjoint solve + element kernel)."""
+    import torch
+
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    n = args.dg_n
+    g = gdt.make_cube_grid([0, 0], [1, 1], [n, n], simplex=True)
+    ne = g.num_elements
+    rng = np.random.default_rng(SEED + 4)
+    stripe = (((np.arange(ne) // 2) // n) // 8) % 2
+    logk_host = rng.standard_normal(ne) + stripe * np.log(1e4)
+    tol = 1e-12
+    prob = gdt.DiffusionProblem(g, dg=True, solver_opts={"tol": tol, "max_iter": 400000})
+    ndof = prob.space.num_DoFs
+    u_d = prob.solve(torch.exp(torch.tensor(rng.standard_normal(ne), device="cuda"))).clone()
+    logk = torch.tensor(logk_host, device="cuda")
+
+    def J(lk):
+        u = gdt.DiffusionSolve.apply(lk, prob)
+        return 0.5 * torch.sum((u - u_d) ** 2)
+
+    def step():
+        lk = logk.clone().requires_grad_(True)
+        j = J(lk)
+        j.backward()
+        return j, lk.grad
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        j, grad = step()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    iters = prob.op.last_solve_info["iterations"]
+    # FP64 SpMV of the CG iterations, timed per launch (one extra forward solve in timing mode)
+    lib = gdt._capi.load()
+    ctx = prob.op.ctx
+    lib.gdt_context_set_timing(ctx.handle, 1)
+    lib.gdt_context_spmv_timing(ctx.handle, None, None, None, None, 1)
+    prob.solve(torch.exp(logk))
+    import ctypes as C
+
+    t64, n64 = C.c_double(), C.c_int64()
+    lib.gdt_context_spmv_timing(ctx.handle, C.byref(t64), C.byref(n64), None, None, 1)
+    lib.gdt_context_set_timing(ctx.handle, 0)
+    spmv_ms = t64.value / max(n64.value, 1)
+    nnz = prob.op.nnz
+    bytes64 = 12 * nnz + 4 * (ndof + 1) + 16 * ndof
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    # central differences on seeded elements, untimed: h = 1e-6 (the stated check) and h = 1e-4 (less
+    # sensitive to the 1e-12 solver tolerance at this contrast); errors relative to max |gradient|
+    grad_h = grad.detach().cpu().numpy()
+    picks = rng.choice(ne, args.dg_fd, replace=False)
+    fd_err = {1e-6: 0.0, 1e-4: 0.0}
+    scale = max(np.abs(grad_h).max(), 1e-300)
+    with torch.no_grad():
+        for e in picks:
+            for h in fd_err:
+                lp = logk.clone()
+                lp[e] += h
+                lm = logk.clone()
+                lm[e] -= h
+                fd = (J(lp).item() - J(lm).item()) / (2 * h)
+                fd_err[h] = max(fd_err[h], abs(fd - grad_h[e]) / scale)
+    line = {
+        "metric": "SWIPDG adjoint gradients: DoF/s (forward solve + adjoint solve + log-kappa gradient)",
+        "value": ndof / (ms / 1e3), "unit": "DoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded log kappa: N(0,1) + stripes x1e4, seeded target field)",
+        "config": {"workload": f"{n}^2 squares -> {ne} triangles, SWIPDG P1 ({ndof} DoF, {nnz} nnz), theta=1, "
+                               "sigma 8/14, f=1; J = 0.5||u - u_d||^2, CG-Jacobi to 1e-12 rel. residual",
+                   "dofs": ndof, "nnz": nnz},
+        "cg_iterations_per_solve": iters,
+        "gradient_vs_central_differences": {"max_rel_error_h1e-6": fd_err[1e-6], "max_rel_error_h1e-4": fd_err[1e-4],
+                                            "elements": int(args.dg_fd), "relative_to": "max |gradient|"},
+        "roofline": {"bound": "hbm", "kernel": "FP64 CSR SpMV of the CG iterations (k_spmv)",
+                     "achieved": bytes64 / (spmv_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": bytes64 / (spmv_ms / 1e3) / 1e9 / hbm, "bytes_per_launch": bytes64,
+                     "avg_launch_ms": spmv_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                     "traffic": None},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------------- FV (config 5) ---
 def bumps(n, seed, count=32):
     rng = np.random.default_rng(seed)
@@ -549,5 +654,7 @@ if __name__ == "__main__":
         run_batched(a)
     elif a.config == "fv":
         run_fv(a)
+    elif a.config == "swipdg":
+        run_swipdg(a)
     else:
         run_gdt(a)
