@@ -114,29 +114,34 @@ __global__ void __launch_bounds__(TH) k_mx_spmv(int n, Stencil S, const float* _
 
 // 3D form of the same product, tiled for GB300's shared memory and fed by TMA (vertex grids with
 // nx, ny >= 3, where every stencil slot has its own linear offset). A CTA owns a 32 x 8 tile of an
-// x-y plane and walks a chunk of z planes. Per plane, one thread issues bulk-tensor loads of
-// 40 x 10-element boxes (the tile with a one-vertex halo, x rounded out to 16-byte boundaries; the
-// hardware zero-fills outside the grid): the in-plane upper slots (dz = 0) and out-of-plane upper
-// slots (dz = +1) of the next plane and p of the plane after it, completing on an mbarrier while the
-// current plane is computed. Every lower term D_o[i - o] p[i - o] is read from shared memory (the
-// plane's in-plane slots, or the previous plane's out-of-plane slots), so per row the kernel streams
-// (1 + upper slots) * 4 bytes from HBM and issues no per-element staging instructions. Rings:
-// p of planes z-1 .. z+2 (4), out-of-plane slots of planes z-1 .. z+1 (3), in-plane slots of
-// planes z, z+1 (2). A wait that runs out sets MState::fault and the kernel stops computing.
+// x-y plane and walks a chunk of z planes. One thread issues bulk-tensor loads of 40 x 10-element
+// boxes (the tile with a one-vertex halo, x rounded out to 16-byte boundaries; the hardware
+// zero-fills outside the grid) LA planes ahead, each plane's boxes completing on its own mbarrier:
+// the in-plane upper slots (dz = 0) and out-of-plane upper slots (dz = +1) of the plane and p of the
+// plane after it. Row (x, y, z) is
+//   D_0 p + sum_in [D_o(i) p(i + o) + D_o(i - o) p(i - o)] + sum_up D_o(i) p(i + o) + L(x, y, z),
+// where the in-plane lower terms and the out-of-plane upper terms use plane z's boxes, and
+// L(x, y, z) = sum_up D_o(i - o) p(i - o) only needs plane z - 1: each thread computes it for its
+// own column while plane z - 1 is resident and carries it in a register to the next plane. So per
+// plane the CTA holds the slot boxes of one plane (plus those in flight) and p of two. Per row the
+// kernel streams (1 + upper slots) * 4 bytes from HBM and issues no per-element staging
+// instructions. A wait that runs out sets MState::fault and the kernel stops computing.
 constexpr int S3X = 32, S3Y = 8;
-constexpr int TW = 40, TR = 10;       // box: x0 - 4 .. x0 + 35, y0 - 1 .. y0 + 8
-constexpr int TS = 416;               // tile stride in floats: 1600-byte box rounded up to 128 bytes
+constexpr int TW = 40, TR = 10;  // box: x0 - 4 .. x0 + 35, y0 - 1 .. y0 + 8
+constexpr int TS = 416;          // box stride in shared memory, floats (1600 bytes rounded up to 128)
 constexpr uint32_t kBoxBytes = TW * TR * 4;
+constexpr int LA = 2;            // planes in flight ahead of the one computed
 
 struct Stencil3 {
   int nin, nup;
   int in_slot[4], up_slot[9];  // indices into the upper slots of Stencil
-  int in_o[4], up_o[9];        // in-tile offsets dy * TW + dx
+  int in_o[4], up_o[9];        // in-box offsets dy * TW + dx
 };
 
+// rings: p of LA + 2 planes, slot boxes of LA + 1 planes, LA + 1 barriers
 template <int NIN, int NUP>
 constexpr size_t spmv3d_smem_bytes() {
-  return 128 + sizeof(float) * TS * (4 + 3 * NUP + 2 * NIN) + 2 * sizeof(uint64_t);
+  return 128 + sizeof(float) * TS * ((LA + 2) + (LA + 1) * (NUP + NIN)) + (LA + 1) * sizeof(uint64_t);
 }
 
 // 1D grid (the grid reduction counts blocks along x): block b = (bz * tiles_y + by) * tiles_x + bx.
@@ -149,95 +154,107 @@ __global__ void __launch_bounds__(S3X* S3Y) k_mx_spmv3d(int nx, int ny, int nz, 
                                                         MState* st, double* partials, unsigned int* ticket) {
   if (mstopped(st)) return;
   float* const P = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(gdt_dyn_smem) + 127) & ~uintptr_t(127));
-  float* const U = P + 4 * TS;
-  float* const I = U + 3 * NUP * TS;
-  uint64_t* const bar = reinterpret_cast<uint64_t*>(I + 2 * NIN * TS);
+  float* const U = P + (LA + 2) * TS;
+  float* const I = U + (LA + 1) * NUP * TS;
+  uint64_t* const bar = reinterpret_cast<uint64_t*>(I + (LA + 1) * NIN * TS);
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int tiles_x = (nx + S3X - 1) / S3X, tiles_y = (ny + S3Y - 1) / S3Y;
   const int bx = blockIdx.x % tiles_x, by = (blockIdx.x / tiles_x) % tiles_y, bz = blockIdx.x / (tiles_x * tiles_y);
   const int x0 = bx * S3X, y0 = by * S3Y, xs = x0 - 4, ys = y0 - 1;
   const int zb = bz * zlen, ze = min(nz, zb + zlen);
-  auto Pz = [&](int z) { return P + ((z + 4) & 3) * TS; };
-  auto Uz = [&](int z) { return U + ((z + 3) % 3) * (NUP * TS); };
-  auto Iz = [&](int z) { return I + ((z + 2) & 1) * (NIN * TS); };
-  auto issue_slots = [&](int z, uint64_t* b) {
+  // ring slots by plane (planes >= zb - 1)
+  auto Pz = [&](int z) { return P + ((z - zb + 1) % (LA + 2)) * TS; };
+  auto Uz = [&](int z) { return U + ((z - zb + 1) % (LA + 1)) * (NUP * TS); };
+  auto Iz = [&](int z) { return I + ((z - zb + 1) % (LA + 1)) * (NIN * TS); };
+  // stage k: 0 = out-of-plane slots and p of plane zb - 1, p of plane zb; k >= 1 = slots of plane
+  // zb + k - 1 and p of plane zb + k; barrier k % (LA + 1), phase parity (k / (LA + 1)) & 1
+  auto issue = [&](int k) {
+    uint64_t* b = &bar[k % (LA + 1)];
+    if (k == 0) {
+      mbar_arrive_expect_tx(b, kBoxBytes * (NUP + 2));
+      tma_load_3d(Pz(zb - 1), &tmP, xs, ys, zb - 1, b);
+      tma_load_3d(Pz(zb), &tmP, xs, ys, zb, b);
 #pragma unroll
-    for (int k = 0; k < NIN; ++k) tma_load_4d(Iz(z) + k * TS, &tmD, xs, ys, z, T3.in_slot[k] + 1, b);
+      for (int u = 0; u < NUP; ++u) tma_load_4d(Uz(zb - 1) + u * TS, &tmD, xs, ys, zb - 1, T3.up_slot[u] + 1, b);
+    } else {
+      const int z = zb + k - 1;
+      mbar_arrive_expect_tx(b, kBoxBytes * (NIN + NUP + 1));
 #pragma unroll
-    for (int k = 0; k < NUP; ++k) tma_load_4d(Uz(z) + k * TS, &tmD, xs, ys, z, T3.up_slot[k] + 1, b);
+      for (int u = 0; u < NIN; ++u) tma_load_4d(Iz(z) + u * TS, &tmD, xs, ys, z, T3.in_slot[u] + 1, b);
+#pragma unroll
+      for (int u = 0; u < NUP; ++u) tma_load_4d(Uz(z) + u * TS, &tmD, xs, ys, z, T3.up_slot[u] + 1, b);
+      tma_load_3d(Pz(z + 1), &tmP, xs, ys, z + 1, b);
+    }
   };
+  auto wait = [&](int k) { return mbar_wait(&bar[k % (LA + 1)], (k / (LA + 1)) & 1); };
+  const int kmax = ze - zb;  // stages 0 .. kmax
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+#pragma unroll
+    for (int b = 0; b <= LA; ++b) mbar_init(&bar[b], 1);
     mbar_init_fence();
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    // prologue on bar[0]: p of planes zb-1, zb, zb+1, out-of-plane slots of zb-1, all slots of zb
-    mbar_arrive_expect_tx(&bar[0], kBoxBytes * (3 + NUP + NIN + NUP));
-    tma_load_3d(Pz(zb - 1), &tmP, xs, ys, zb - 1, &bar[0]);
-    tma_load_3d(Pz(zb), &tmP, xs, ys, zb, &bar[0]);
-    tma_load_3d(Pz(zb + 1), &tmP, xs, ys, zb + 1, &bar[0]);
-#pragma unroll
-    for (int k = 0; k < NUP; ++k) tma_load_4d(Uz(zb - 1) + k * TS, &tmD, xs, ys, zb - 1, T3.up_slot[k] + 1, &bar[0]);
-    issue_slots(zb, &bar[0]);
-  }
+  __syncthreads();  // every thread sees initialised barriers before its first wait
+  if (threadIdx.x == 0)
+    for (int k = 0; k <= LA && k <= kmax; ++k) issue(k);
   const int gx = x0 + tx, gy = y0 + ty;
   const bool own = gx < nx && gy < ny;
   const int c = (ty + 1) * TW + tx + 4;
-  float acc = 0.f;
+  float acc = 0.f, lower = 0.f;
   int failed_at = -1;
-  for (int z = zb, j = 0; z < ze; ++z, ++j) {
-    // plane z + 1 (its slots, p of plane z + 2) on the other barrier while plane z is computed
-    if (threadIdx.x == 0 && z + 1 < ze) {
-      uint64_t* b = &bar[(j + 1) & 1];
+  // L(x, y, zb) from plane zb - 1
+  if (!__syncthreads_and(wait(0))) {
+    failed_at = 0;
+  } else {
+    const float* Pm = Pz(zb - 1);
+    const float* Um = Uz(zb - 1);
+#pragma unroll
+    for (int u = 0; u < NUP; ++u) lower = fmaf(Um[u * TS + c - T3.up_o[u]], Pm[c - T3.up_o[u]], lower);
+    __syncthreads();  // stage LA + 1 reuses the slots of plane zb - 1
+  }
+  for (int z = zb, k = 1; failed_at < 0 && z < ze; ++z, ++k) {
+    if (threadIdx.x == 0 && k + LA <= kmax) {
       fence_proxy_async_smem();
-      mbar_arrive_expect_tx(b, kBoxBytes * (NIN + NUP + 1));
-      issue_slots(z + 1, b);
-      tma_load_3d(Pz(z + 2), &tmP, xs, ys, z + 2, b);
+      issue(k + LA);
     }
     const long long ip = gx + pitch * (gy + (long long)ny * z);
     const float d0 = own ? __ldcs(D0 + ip) : 0.f;
-    const bool ok = mbar_wait(&bar[j & 1], (j >> 1) & 1);
-    if (!__syncthreads_and(ok)) {
-      failed_at = j;
+    if (!__syncthreads_and(wait(k))) {
+      failed_at = k;
       break;
     }
+    const float* Pc = Pz(z);
+    const float* Pn = Pz(z + 1);
+    const float* Ic = Iz(z);
+    const float* Uc = Uz(z);
+    float s = fmaf(d0, Pc[c], lower);
+    float next = 0.f;
+#pragma unroll
+    for (int u = 0; u < NIN; ++u) {
+      const int o = T3.in_o[u];
+      s = fmaf(Ic[u * TS + c], Pc[c + o], s);
+      s = fmaf(Ic[u * TS + c - o], Pc[c - o], s);
+    }
+#pragma unroll
+    for (int u = 0; u < NUP; ++u) {
+      const int o = T3.up_o[u];
+      s = fmaf(Uc[u * TS + c], Pn[c + o], s);
+      next = fmaf(Uc[u * TS + c - o], Pc[c - o], next);
+    }
     if (own) {
-      const float* Pc = Pz(z);
-      const float* Pn = Pz(z + 1);
-      const float* Pm = Pz(z - 1);
-      const float* Ic = Iz(z);
-      const float* Uc = Uz(z);
-      const float* Um = Uz(z - 1);
-      float s = d0 * Pc[c];
-#pragma unroll
-      for (int k = 0; k < NIN; ++k) {
-        const int o = T3.in_o[k];
-        s = fmaf(Ic[k * TS + c], Pc[c + o], s);
-        s = fmaf(Ic[k * TS + c - o], Pc[c - o], s);
-      }
-#pragma unroll
-      for (int k = 0; k < NUP; ++k) {
-        const int o = T3.up_o[k];
-        s = fmaf(Uc[k * TS + c], Pn[c + o], s);
-        s = fmaf(Um[k * TS + c - o], Pm[c - o], s);
-      }
       q[ip] = s;
       acc = fmaf(Pc[c], s, acc);
     }
-    __syncthreads();  // the next loads overwrite Iz(z), Uz(z - 1) and Pz(z - 1)
+    lower = next;
+    __syncthreads();  // stage k + LA + 1 reuses the slots of plane z and the box of p(z)
   }
   if (failed_at >= 0) {
-    // report, then give the copies in flight (this plane and the next) a bounded chance to land
-    // before the CTA's shared memory is released
+    // report, then give the copies in flight a bounded chance to land before the CTA's shared
+    // memory is released
     if (threadIdx.x == 0) {
       st->fault = 1;
       st->breakdown = 1;
       st->converged = 1;
-      const int j = failed_at;
-      mbar_wait(&bar[j & 1], (j >> 1) & 1);
-      if (zb + j + 1 < ze) mbar_wait(&bar[(j + 1) & 1], ((j + 1) >> 1) & 1);
+      for (int k = failed_at; k <= kmax && k <= failed_at + LA; ++k) wait(k);
     }
     acc = 0.f;
   }
@@ -617,12 +634,13 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
     }
   };
   auto launch_tiled = [&](cudaStream_t st_) {
+    const int ny = int(g.vn[1]), nz = int(g.vn[2]);
     if (T3.nup == 9)
-      k_mx_spmv3d<4, 9><<<grid3, S3X * S3Y, smem3, st_>>>(nx, int(g.vn[1]), int(g.vn[2]), zlen, pitch, T3, tmD, tmP,
-                                                          D + S.pad, q32, st, partials, ticket);
+      k_mx_spmv3d<4, 9><<<grid3, S3X * S3Y, smem3, st_>>>(nx, ny, nz, zlen, pitch, T3, tmD, tmP, D + S.pad, q32, st,
+                                                          partials, ticket);
     else
-      k_mx_spmv3d<3, 4><<<grid3, S3X * S3Y, smem3, st_>>>(nx, int(g.vn[1]), int(g.vn[2]), zlen, pitch, T3, tmD, tmP,
-                                                          D + S.pad, q32, st, partials, ticket);
+      k_mx_spmv3d<3, 4><<<grid3, S3X * S3Y, smem3, st_>>>(nx, ny, nz, zlen, pitch, T3, tmD, tmP, D + S.pad, q32, st,
+                                                          partials, ticket);
   };
   if (tiled3 && m->mx_tiled < 0) {
     cudaEvent_t e0, e1, e2;
