@@ -171,6 +171,19 @@ class _Space:
     def max_local_size(self):
         return int(self.lib.gdt_space_max_local_size(self.handle))
 
+    def quadrature(self):
+        """(x_ref [nq, 3], w_ref [nq]) of the element-batched assembly path: coefficients given per
+        quadrature point are [element, q] at these reference points."""
+        import numpy as np
+
+        nq = int(self.lib.gdt_space_quadrature(self.handle, None, None))
+        if nq < 0:
+            raise GdtError(capi.EUNSUPPORTED, "quadrature of a continuous space only")
+        x = np.zeros((nq, 3))
+        w = np.zeros(nq)
+        self.lib.gdt_space_quadrature(self.handle, x.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p))
+        return x, w
+
     def global_indices(self, ctx: Context | None = None):
         """mapper.global_indices of every element: int64 CUDA tensor [num_elements, local_size]."""
         ctx = ctx or default_context()
@@ -214,6 +227,15 @@ def _coef(c):
     return None, float(c)
 
 
+def _coef_qp(c):
+    """(per-element tensor, constant, per-quadrature-point tensor): a number, a 1D tensor with one value
+    per element, or a 2D tensor [element, quadrature point] (points of _Space.quadrature())."""
+    if isinstance(c, torch.Tensor) and c.dim() == 2:
+        return None, 0.0, _f64(c.contiguous() if c.is_contiguous() else c, name="coefficient")
+    t, k = _coef(c)
+    return t, k, None
+
+
 class LocalLaplaceIntegrand:
     def __init__(self, diffusion=1.0):
         self.diffusion = diffusion
@@ -226,12 +248,16 @@ class _ProductWithAnsatz:
 
 
 class LocalElementProductIntegrand:
+    """weight * phi_i * phi_j (local/integrands/product.hh:89-130): as a bilinear form the weighted
+    product (mass) matrix, weight a number, a per-element tensor or a [element, quadrature point]
+    tensor; with_ansatz(f) lowers the load-vector integrand (unit weight)."""
+
     def __init__(self, weight=1.0):
-        if weight != 1.0:
-            raise GdtError(capi.EUNSUPPORTED, "only the unit weight is lowered to the GPU library")
         self.weight = weight
 
     def with_ansatz(self, function):
+        if isinstance(self.weight, torch.Tensor) or self.weight != 1.0:
+            raise GdtError(capi.EUNSUPPORTED, "only the unit weight is lowered for load vectors")
         return _ProductWithAnsatz(self.weight, function)
 
 
@@ -350,15 +376,26 @@ class MatrixOperator:
         capi.check(capi.load().gdt_matrix_set_schedule(self.handle, int(schedule)), what="gdt_matrix_set_schedule")
         return self
 
+    def _check_qp(self, t):
+        if t is None:
+            return
+        nq = self.source_space.quadrature()[0].shape[0]
+        if tuple(t.shape) != (self.grid.num_elements, nq):
+            raise ValueError(f"per-quadrature-point coefficient has shape {tuple(t.shape)}, expected "
+                             f"({self.grid.num_elements}, {nq})")
+
     def _diffusion_desc(self, rhs_force=None, dirichlet=False):
         kappa = 1.0
         for f in self.forms:
             if isinstance(f, LocalElementIntegralBilinearForm) and isinstance(f.integrand, LocalLaplaceIntegrand):
                 kappa = f.integrand.diffusion
-        kt, kc = _coef(kappa)
+        kt, kc, kq = _coef_qp(kappa)
+        self._check_qp(kq)
         d = capi.DiffusionDesc()
         d.kappa = kt.data_ptr() if kt is not None else None
         d.kappa_const = kc
+        d.kappa_qp = kq.data_ptr() if kq is not None else None
+        self._keep = [kt, kq]
         ft, fc = _coef(1.0 if rhs_force is None else rhs_force)
         d.force = ft.data_ptr() if ft is not None else None
         d.force_const = fc
@@ -394,6 +431,21 @@ class MatrixOperator:
             d = self._ipdg_desc(0.0 if force is None else force)
             self.ctx.call("gdt_assemble_swipdg", self.handle, C.byref(d), _ptr(rhs))
         else:
+            products = [f for f in self.forms if isinstance(f, LocalElementIntegralBilinearForm)
+                        and isinstance(f.integrand, LocalElementProductIntegrand)]
+            if products:
+                if len(products) != len(self.forms) or len(products) > 1 or rhs is not None or dirichlet:
+                    raise GdtError(capi.EUNSUPPORTED, "a product (mass) form is assembled on its own")
+                wt, wc, wq = _coef_qp(products[0].integrand.weight)
+                self._check_qp(wq)
+                if wt is not None and wt.numel() != self.grid.num_elements:
+                    raise ValueError(f"weight has {wt.numel()} entries, expected {self.grid.num_elements}")
+                pd = capi.ProductDesc()
+                pd.weight = wt.data_ptr() if wt is not None else None
+                pd.weight_const = wc
+                pd.weight_qp = wq.data_ptr() if wq is not None else None
+                self.ctx.call("gdt_assemble_cg_product", self.handle, C.byref(pd))
+                return self
             d = self._diffusion_desc(force, dirichlet)
             self.ctx.call("gdt_assemble_cg_diffusion", self.handle, C.byref(d), _ptr(rhs))
         return self

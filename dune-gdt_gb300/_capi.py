@@ -25,7 +25,11 @@ TIMESTEPPER_EXPLICIT_EULER, TIMESTEPPER_SSPRK2 = 0, 1
 
 class DiffusionDesc(C.Structure):
     _fields_ = [("kappa", C.c_void_p), ("kappa_const", C.c_double), ("force", C.c_void_p),
-                ("force_const", C.c_double), ("dirichlet", C.c_int)]
+                ("force_const", C.c_double), ("dirichlet", C.c_int), ("kappa_qp", C.c_void_p)]
+
+
+class ProductDesc(C.Structure):
+    _fields_ = [("weight", C.c_void_p), ("weight_const", C.c_double), ("weight_qp", C.c_void_p)]
 
 
 class IpdgDesc(C.Structure):
@@ -105,6 +109,8 @@ _SIGNATURES = {
     "gdt_assemble_cg_diffusion": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_assemble_cg_rhs": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_dirichlet_apply": (C.c_int, [P, P, P]),
+    "gdt_assemble_cg_product": (C.c_int, [P, P, C.POINTER(ProductDesc)]),
+    "gdt_space_quadrature": (C.c_int, [P, P, P]),
     "gdt_assemble_swipdg": (C.c_int, [P, P, C.POINTER(IpdgDesc), P]),
     "gdt_spmv": (C.c_int, [P, P, P, P]),
     "gdt_solve": (C.c_int, [P, P, P, P, C.POINTER(SolverOpts), C.POINTER(SolveInfo)]),

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <new>
 
+#include "highorder.cuh"
 #include "internal.cuh"
 
 namespace gdt {
@@ -215,10 +216,16 @@ gdt_status gdt_space_create(gdt_grid g, int kind, int order, gdt_space* out) {
   s.kind = kind;
   s.order = order;
   if (kind == GDT_SPACE_CG) {
-    if (order != 1) return GDT_EUNSUPPORTED;
+    if (order != 1 && order != 2) return GDT_EUNSUPPORTED;
     if (d.periodic) return GDT_EUNSUPPORTED;
-    s.lsize = d.simplex ? d.dim + 1 : (1 << d.dim);
-    s.size = d.nvert;
+    if (order == 1) {
+      s.lsize = d.simplex ? d.dim + 1 : (1 << d.dim);
+      s.size = d.nvert;
+    } else {
+      const ho::HoSpaceInfo info = ho::space_info(d, order);
+      s.lsize = info.lsize;
+      s.size = info.size;
+    }
   } else if (kind == GDT_SPACE_DG) {
     if (order != 1 || d.periodic) return GDT_EUNSUPPORTED;
     s.lsize = d.simplex ? d.dim + 1 : (1 << d.dim);
@@ -278,6 +285,7 @@ gdt_status gdt_matrix_create(gdt_context ctx, gdt_space test, gdt_space ansatz, 
 
 gdt_status gdt_matrix_destroy(gdt_matrix m) {
   if (!m) return GDT_EINVAL;
+  ho_matrix_free(static_cast<HoMatrix*>(m->ho));
   if (m->rp) cudaFree(m->rp);
   if (m->col) cudaFree(m->col);
   if (m->val) cudaFree(m->val);
@@ -307,19 +315,37 @@ gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m) {
 gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs) {
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  if (m->test.order == 2 || d->kappa_qp) {
+    GDT_CHECK(ctx, ho_prepare(ctx, m));
+    return ho_assemble(ctx, m, 0, d->kappa, d->kappa_const, d->kappa_qp, d->force, d->force_const, rhs, d->dirichlet);
+  }
   return assemble_cg(ctx, m, d, rhs);
 }
 
 gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space s, const gdt_diffusion_desc* d, double* rhs) {
   if (!ctx || !s || !d || !rhs) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
+  if (s->order == 2) return ho_assemble_rhs(ctx, *s, d->force, d->force_const, d->dirichlet, rhs);
   return assemble_cg_rhs(ctx, *s, d, rhs);
 }
 
 gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
   if (!ctx || !m) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  if (m->test.order == 2) return ho_dirichlet(ctx, m, rhs);
   return dirichlet_apply(ctx, m, rhs);
+}
+
+gdt_status gdt_assemble_cg_product(gdt_context ctx, gdt_matrix m, const gdt_product_desc* d) {
+  if (!ctx || !m || !d) return GDT_EINVAL;
+  if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  GDT_CHECK(ctx, ho_prepare(ctx, m));
+  return ho_assemble(ctx, m, 1, d->weight, d->weight_const, d->weight_qp, nullptr, 0.0, nullptr, 0);
+}
+
+int gdt_space_quadrature(gdt_space s, double* x_ref, double* w_ref) {
+  if (!s || s->kind != GDT_SPACE_CG) return -1;
+  return ho_quadrature(*s, x_ref, w_ref);
 }
 
 gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs) {
@@ -384,6 +410,7 @@ gdt_status gdt_cg_dlogkappa(gdt_context ctx, gdt_space s, const double* kappa, c
                             double* out) {
   if (!ctx || !s || !kappa || !u || !lam || !out) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
+  if (s->order != 1) return fail(ctx, GDT_EUNSUPPORTED, "log-kappa gradient of order-2 spaces");
   return cg_dlogkappa(ctx, *s, kappa, u, lam, out);
 }
 

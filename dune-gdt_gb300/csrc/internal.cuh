@@ -75,6 +75,7 @@ struct gdt_matrix_s {
   int spmv_sched = 1;  // SpMV schedule (see linalg.cuh), picked by tune_spmv on first use
   int tuned = 0;
   int mx_tiled = -1;   // mixed solver, 3D grids: plane-tiled (1) or linear (0) FP32 stencil SpMV, timed on first use
+  void* ho = nullptr;  // element-batched assembly data (order-2 spaces), owned (highorder.cu)
 };
 
 namespace gdt {

@@ -4,6 +4,7 @@
 #include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include "highorder.cuh"
 #include "structured.cuh"
 
 namespace gdt {
@@ -107,6 +108,7 @@ __global__ void global_indices_kernel(GridDesc g, int kind, int lsize, long long
 }  // namespace
 
 gdt_status build_pattern(gdt_context ctx, gdt_matrix m) {
+  if (m->test.kind == GDT_SPACE_CG && m->test.order == 2) return ho_build_pattern(ctx, m);
   const GridDesc& g = m->test.g;
   cudaStream_t s = ctx->stream;
   const bool dg = m->test.kind == GDT_SPACE_DG;
@@ -167,6 +169,7 @@ gdt_status build_pattern(gdt_context ctx, gdt_matrix m) {
 
 extern "C" gdt_status gdt_space_global_indices(gdt_context ctx, gdt_space s, int64_t* out) {
   if (!ctx || !s || !out) return GDT_EINVAL;
+  if (s->kind == GDT_SPACE_CG && s->order == 2) return gdt::ho_global_indices(ctx, *s, out, nullptr);
   gdt::global_indices_kernel<<<gdt::grid_blocks(s->g.nelem, 256), 256, 0, ctx->stream>>>(
       s->g, s->kind, s->lsize, reinterpret_cast<long long*>(out));
   return gdt::check_launch(ctx, "global indices");

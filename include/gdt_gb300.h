@@ -108,7 +108,10 @@ int64_t gdt_grid_num_elements(gdt_grid grid);
 int64_t gdt_grid_num_vertices(gdt_grid grid);
 
 /* -------------------------------------------------------------------- space --- */
-/* kind: GDT_SPACE_CG (order 1), GDT_SPACE_DG (order 1), GDT_SPACE_FV (order 0, m = 1). */
+/* kind: GDT_SPACE_CG (order 1 or 2; make_continuous_lagrange_space, spaces/h1/continuous-lagrange.hh:189-203),
+ * GDT_SPACE_DG (order 1), GDT_SPACE_FV (order 0, m = 1). Order-2 DoFs: MCMG layout by codim
+ * (cells, faces, edges, vertices), edges and faces numbered in order of first appearance in the
+ * element walk (ContinuousMapper, spaces/mapper/continuous.hh:117-182). */
 gdt_status gdt_space_create(gdt_grid grid, int kind, int order, gdt_space* out);
 gdt_status gdt_space_destroy(gdt_space space);
 int64_t gdt_space_size(gdt_space space);
@@ -142,14 +145,20 @@ gdt_status gdt_matrix_set_schedule(gdt_matrix m, int schedule);
 /* ----------------------------------------------------------------- assembly --- */
 typedef struct gdt_diffusion_desc {
   const double* kappa;   /* device, one scalar diffusion value per element, or NULL */
-  double kappa_const;    /* used when kappa == NULL */
+  double kappa_const;    /* used when kappa == NULL (and kappa_qp == NULL) */
   const double* force;   /* device, one source value per element, or NULL */
   double force_const;    /* used when force == NULL */
   int dirichlet;         /* 1: all-Dirichlet boundary, homogeneous (unit row + col, rhs = 0) */
+  const double* kappa_qp; /* device, diffusion at the quadrature points of every element
+                           * ([element][gdt_space_quadrature point]), or NULL; order-2 spaces (or
+                           * any order through the element-batched path) */
 } gdt_diffusion_desc;
 
 /* continuous Lagrange: stiffness of LocalLaplaceIntegrand(kappa) into m, and (if rhs != NULL) the
- * load vector of LocalElementProductIntegrand().with_ansatz(force); Dirichlet constraints fused. */
+ * load vector of LocalElementProductIntegrand().with_ansatz(force); Dirichlet constraints fused.
+ * Order 1 (P1/Q1): vertex-row kernel, kappa per element. Order 2 (P2/Q2), or kappa_qp given:
+ * element-batched local matrices on the FP64 tensor cores (sum over quadrature points as a small
+ * GEMM per batch of elements) and coloured scatter into the CSR pattern. */
 gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* desc, double* rhs);
 
 /* load vector only (VectorBasedFunctional::assemble, functionals/vector-based.hh:276-279); with
@@ -158,6 +167,21 @@ gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space cg, const gdt_diffusio
 /* DirichletConstraints::apply(M, V) (tools/dirichlet-constraints.hh:153-184) on an assembled
  * matrix of a continuous space, all-Dirichlet boundary: unit_col + unit_row, rhs[D] = 0 (rhs may be NULL). */
 gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs);
+
+/* LocalElementIntegralBilinearForm(LocalElementProductIntegrand(weight))
+ * (local/bilinear-forms/integrals.hh:97-134, local/integrands/product.hh:89-130): the weighted
+ * product (mass) matrix M_ij = int weight phi_i phi_j of a continuous space of order 1 or 2 into m,
+ * by the element-batched tensor-core path. */
+typedef struct gdt_product_desc {
+  const double* weight;     /* device, one value per element, or NULL */
+  double weight_const;      /* used when weight == NULL and weight_qp == NULL */
+  const double* weight_qp;  /* device, [element][gdt_space_quadrature point], or NULL */
+} gdt_product_desc;
+gdt_status gdt_assemble_cg_product(gdt_context ctx, gdt_matrix m, const gdt_product_desc* desc);
+/* quadrature rule of the element-batched path of a continuous space: returns the number of points
+ * nq; x_ref (nq x 3 reference-element coordinates) and w_ref (nq weights on the reference element)
+ * may be NULL. The physical point of element e is its first vertex plus J_e x_ref. */
+int gdt_space_quadrature(gdt_space s, double* x_ref, double* w_ref);
 
 typedef struct gdt_ipdg_desc {
   const double* kappa;   /* device, per element, or NULL */
