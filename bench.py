@@ -45,15 +45,17 @@ def parse():
     p.add_argument("--tol", type=float, default=1e-11, help="relative residual stop of both solvers")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-iters", type=int, default=60, help="CG iterations timed in the CPU sample")
-    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg"],
+    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg", "q2"],
                    help="heat3d: the headline 128^3 workload; batched: 512 parametric P1 problems of uneven "
                         "size in one persistent launch; fv: 2D Burgers FV, SSP-RK2; swipdg: SWIPDG P1 "
-                        "forward solve + adjoint log-kappa gradient on 256^2 squares")
+                        "forward solve + adjoint log-kappa gradient on 256^2 squares; q2: 3D Q2 assembly "
+                        "(tensor-core local matrices, diffusion at quadrature points) + solve")
     p.add_argument("--problems", type=int, default=512, help="batched: number of problems")
     p.add_argument("--fv-n", type=int, default=4096, help="fv: cells per axis")
     p.add_argument("--fv-steps", type=int, default=500, help="fv: SSP-RK2 steps per bench step")
     p.add_argument("--fv-batch", type=int, default=1, help="fv: independent initial conditions")
     p.add_argument("--dg-n", type=int, default=256, help="swipdg: squares per axis (2 triangles each)")
+    p.add_argument("--q2-n", type=int, default=64, help="q2: hexahedra per axis")
     p.add_argument("--dg-fd", type=int, default=16, help="swipdg: elements of the finite-difference check")
     return p.parse_args()
 
@@ -414,6 +416,85 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------- Q2 (next-1 row) ---
+def run_q2(args):
+    """-div(kappa grad u) = 1 on the unit cube, n^3 hexahedra, continuous Q2, Dirichlet 0; kappa at the
+    quadrature points = exp(N(0,1)) per element x (1 + 0.5 sin(2 pi x) sin(2 pi y) sin(2 pi z)); one step =
+    element-batched assembly (FP64 tensor cores) + load vector + Dirichlet + CG-Jacobi solve (FP64)."""
+    import ctypes as C
+
+    import torch
+
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    n = args.q2_n
+    g = gdt.make_cube_grid([0, 0, 0], [1, 1, 1], [n, n, n])
+    space = gdt.ContinuousLagrangeSpace(g, 2)
+    ne, ndof = g.num_elements, space.num_DoFs
+    xq, _ = space.quadrature()
+    nq = xq.shape[0]
+    rng = np.random.default_rng(SEED + 6)
+    ke = torch.tensor(np.exp(rng.standard_normal(ne)), device="cuda")
+    e = torch.arange(ne, device="cuda", dtype=torch.float64)
+    ci = torch.stack([e % n, (e // n) % n, e // (n * n)], 1)  # [ne, 3]
+    X = (ci[:, None, :] + torch.tensor(xq, device="cuda")[None, :, :]) / n  # physical points [ne, nq, 3]
+    s2 = torch.sin(2 * np.pi * X)
+    kappa_qp = (ke[:, None] * (1 + 0.5 * s2[..., 0] * s2[..., 1] * s2[..., 2])).contiguous()
+    op = gdt.MatrixOperator(g, space)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kappa_qp))
+    rhs = torch.zeros(ndof, dtype=torch.float64, device="cuda")
+    u = torch.zeros(ndof, dtype=torch.float64, device="cuda")
+    tol = 1e-10
+
+    def assemble():
+        op.assemble(rhs=rhs, force=1.0, dirichlet=True)
+
+    def step():
+        assemble()
+        u.zero_()
+        op.apply_inverse(rhs, u, opts={"tol": tol, "max_iter": 200000})
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    clocks = Clocks(0)
+    clocks.start()
+    ev[0].record()
+    for _ in range(args.steps):
+        step()
+    ev[1].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    info = dict(op.last_solve_info)
+    ev[2].record()
+    for _ in range(args.steps):
+        assemble()
+    ev[3].record()
+    torch.cuda.synchronize()
+    ms_asm = ev[2].elapsed_time(ev[3]) / args.steps
+    # the contraction's arithmetic: 2 flops per (pair, quadrature point, element), pairs i <= j
+    L = space.max_local_size
+    flops = 2.0 * (L * (L + 1) // 2) * nq * ne
+    r = (op.apply(u) - rhs).norm().item() / rhs.norm().item()
+    line = {
+        "metric": "Q2 DoF/s assembled+solved (3D, diffusion at quadrature points)",
+        "value": ndof / (ms / 1e3), "unit": "DoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded lognormal kappa per element x smooth factor at quadrature points)",
+        "config": {"workload": f"{n}^3 hexahedra, continuous Q2 ({ndof} DoF, {op.nnz} nnz), {nq} quadrature "
+                               "points per element, f=1, Dirichlet 0, CG-Jacobi FP64 to 1e-10 rel. residual",
+                   "dofs": ndof, "nnz": op.nnz},
+        "assembly_ms": ms_asm,
+        "assembly_contraction_flops": flops,
+        "assembly_tflops_upper_bound": flops / (ms_asm / 1e3) / 1e12,
+        "solve": info, "final_rel_residual": r,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------------ SWIPDG (config 4) ---
 def run_swipdg(args):
     """SWIPDG P1 on n^2 squares split into triangles (theta = 1, omega = kappa, sigma 8 / 14), log kappa
@@ -656,5 +737,7 @@ if __name__ == "__main__":
         run_fv(a)
     elif a.config == "swipdg":
         run_swipdg(a)
+    elif a.config == "q2":
+        run_q2(a)
     else:
         run_gdt(a)

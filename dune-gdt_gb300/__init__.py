@@ -24,8 +24,8 @@ __all__ = [
     "LocalIPDGBoundaryPenalty", "LocalCouplingIntersectionIntegralBilinearForm",
     "LocalIntersectionIntegralBilinearForm", "MatrixOperator", "VectorFunctional", "DirichletConstraints",
     "Walker", "DiscreteFunction", "BurgersFlux", "LinearTransportFlux", "NumericalLaxFriedrichsFlux",
-    "NumericalUpwindFlux", "AdvectionFvOperator", "ExplicitRungeKuttaTimeStepper",
-    "estimate_dt_for_hyperbolic_system", "GdtError",
+    "NumericalUpwindFlux", "NumericalEngquistOsherFlux", "AdvectionFvOperator", "ExplicitRungeKuttaTimeStepper",
+    "estimate_dt_for_hyperbolic_system", "GdtError", "element_error",
 ]
 
 
@@ -171,18 +171,56 @@ class _Space:
     def max_local_size(self):
         return int(self.lib.gdt_space_max_local_size(self.handle))
 
-    def quadrature(self):
-        """(x_ref [nq, 3], w_ref [nq]) of the element-batched assembly path: coefficients given per
-        quadrature point are [element, q] at these reference points."""
+    def quadrature(self, order=None):
+        """(x_ref [nq, 3], w_ref [nq]) on the reference element: with order=None the rule of the
+        element-batched assembly path (coefficients given per quadrature point are [element, q] at
+        these points), else a rule exact to that polynomial order (element_error)."""
         import numpy as np
 
-        nq = int(self.lib.gdt_space_quadrature(self.handle, None, None))
+        if order is None:
+            fn, args = self.lib.gdt_space_quadrature, ()
+        else:
+            fn, args = self.lib.gdt_space_quadrature_order, (int(order),)
+        nq = int(fn(self.handle, *args, None, None))
         if nq < 0:
-            raise GdtError(capi.EUNSUPPORTED, "quadrature of a continuous space only")
+            raise GdtError(capi.EUNSUPPORTED, "no quadrature rule for this space")
         x = np.zeros((nq, 3))
         w = np.zeros(nq)
-        self.lib.gdt_space_quadrature(self.handle, x.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p))
+        fn(self.handle, *args, x.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p))
         return x, w
+
+    def quadrature_points(self, order=None, device=None):
+        """Physical quadrature points of every element, a float64 tensor [element, q, dim]."""
+        import itertools
+        import math
+
+        x, _ = self.quadrature(order)
+        g = self.grid
+        d = g.dimension
+        device = device or torch.device("cuda", torch.cuda.current_device())
+        lo = torch.tensor(g.lower_left, dtype=torch.float64, device=device)
+        h = torch.tensor([(g.upper_right[a] - g.lower_left[a]) / g.num_cells[a] for a in range(d)],
+                         dtype=torch.float64, device=device)
+        xr = torch.tensor(x[:, :d], device=device)
+        simplex = g.simplex and d >= 2
+        nsub = math.factorial(d) if simplex else 1
+        e = torch.arange(g.num_elements, device=device)
+        cube, t = e // nsub, e % nsub
+        idx, rest = [], cube
+        for a in range(d):
+            idx.append(rest % g.num_cells[a])
+            rest = rest // g.num_cells[a]
+        ci = torch.stack(idx, 1).to(torch.float64)  # [ne, d]
+        if simplex:  # type t maps the reference simplex onto corners 0, e_pi0, e_pi0 + e_pi1, ...
+            J = torch.zeros((nsub, d, d), dtype=torch.float64, device=device)
+            for k, perm in enumerate(itertools.permutations(range(d))):
+                for m in range(d):
+                    for a in perm[:m + 1]:
+                        J[k, a, m] = 1.0
+            local = torch.einsum("tam,qm->tqa", J, xr)[t]  # [ne, nq, d]
+        else:
+            local = xr[None].expand(g.num_elements, -1, -1)
+        return lo + h * (ci[:, None, :] + local)
 
     def global_indices(self, ctx: Context | None = None):
         """mapper.global_indices of every element: int64 CUDA tensor [num_elements, local_size]."""
@@ -644,6 +682,13 @@ class NumericalUpwindFlux:
         self.flux, self.lf_lambda = flux, 0.0
 
 
+class NumericalEngquistOsherFlux:
+    numflux = capi.NUMFLUX_ENGQUIST_OSHER
+
+    def __init__(self, flux):
+        self.flux, self.lf_lambda = flux, 0.0
+
+
 def _fv_desc(numerical_flux):
     d = capi.FvDesc()
     d.flux = numerical_flux.flux.kind
@@ -788,6 +833,30 @@ class DiffusionSolve(torch.autograd.Function):
         problem.assemble(kappa)  # the operator may have been reassembled since forward
         lam = problem.op.apply_inverse(grad_u.contiguous().to(torch.float64), opts=problem.solver_opts)
         return dlogkappa(problem.op, u, lam, kappa), None
+
+
+# ------------------------------------------------------------------------------ error norms ---
+def element_error(space, u, reference, norm="h1_semi", quad_order=None, ctx: Context | None = None):
+    """Element indicators of u - u_ref as the EOC studies' norms (test/stationary-eocstudies/base.hh:259-269):
+    eta_e^2 = int_e |grad u - g|^2 ("h1_semi", reference = g at space.quadrature_points(quad_order),
+    [element, q, dim]) or int_e (u - v)^2 ("l2", reference [element, q]). Returns (eta2 tensor, total),
+    total = sqrt(sum eta2)."""
+    ctx = ctx or default_context()
+    if quad_order is None:
+        quad_order = 2 * space.order + 2
+    nq = space.quadrature(quad_order)[0].shape[0]
+    ne = space.grid.num_elements
+    kind = {"h1_semi": capi.NORM_H1_SEMI, "l2": capi.NORM_L2}[norm]
+    shape = (ne, nq, space.grid.dimension) if kind == capi.NORM_H1_SEMI else (ne, nq)
+    ref = _f64(reference.contiguous(), name="reference")
+    if tuple(ref.shape) != shape:
+        raise ValueError(f"reference has shape {tuple(ref.shape)}, expected {shape}")
+    _f64(u, space.num_DoFs, "u")
+    eta2 = torch.empty(ne, dtype=torch.float64, device=ctx.device)
+    total = C.c_double()
+    ctx.call("gdt_element_error", space.handle, kind, int(quad_order), _ptr(u), _ptr(ref), _ptr(eta2),
+             C.byref(total))
+    return eta2, total.value
 
 
 # ---------------------------------------------------------------------------------- batched ---

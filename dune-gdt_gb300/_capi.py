@@ -10,6 +10,7 @@ import os
 from . import _build
 
 SPMV_SCHEDULES = 8
+NORM_H1_SEMI, NORM_L2 = 0, 1
 TIMING_SPMV_FP64, TIMING_SPMV_FP32, TIMING_CG_UPDATE, TIMING_CG_DIRECTION, TIMING_RELIABLE_UPDATE = range(5)
 TIMING_KINDS = 8
 OK, EINVAL, ESHAPE, ENOCONV, ETIMEOUT, ENAN, EUNSUPPORTED, ECUDA, ENOMEM = range(9)
@@ -19,7 +20,7 @@ SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 PREC_NONE, PREC_JACOBI, PREC_ILU0 = 0, 1, 2
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 FLUX_BURGERS, FLUX_TRANSPORT = 0, 1
-NUMFLUX_LAX_FRIEDRICHS, NUMFLUX_UPWIND = 0, 1
+NUMFLUX_LAX_FRIEDRICHS, NUMFLUX_UPWIND, NUMFLUX_ENGQUIST_OSHER = 0, 1, 2
 TIMESTEPPER_EXPLICIT_EULER, TIMESTEPPER_SSPRK2 = 0, 1
 
 
@@ -111,6 +112,8 @@ _SIGNATURES = {
     "gdt_dirichlet_apply": (C.c_int, [P, P, P]),
     "gdt_assemble_cg_product": (C.c_int, [P, P, C.POINTER(ProductDesc)]),
     "gdt_space_quadrature": (C.c_int, [P, P, P]),
+    "gdt_space_quadrature_order": (C.c_int, [P, C.c_int, P, P]),
+    "gdt_element_error": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P, C.POINTER(C.c_double)]),
     "gdt_assemble_swipdg": (C.c_int, [P, P, C.POINTER(IpdgDesc), P]),
     "gdt_spmv": (C.c_int, [P, P, P, P]),
     "gdt_solve": (C.c_int, [P, P, P, P, C.POINTER(SolverOpts), C.POINTER(SolveInfo)]),

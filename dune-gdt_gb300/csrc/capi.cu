@@ -348,6 +348,21 @@ int gdt_space_quadrature(gdt_space s, double* x_ref, double* w_ref) {
   return ho_quadrature(*s, x_ref, w_ref);
 }
 
+int gdt_space_quadrature_order(gdt_space s, int quad_order, double* x_ref, double* w_ref) {
+  if (!s || quad_order < 0 || quad_order > 40) return -1;
+  return quadrature_order(*s, quad_order, x_ref, w_ref);
+}
+
+gdt_status gdt_element_error(gdt_context ctx, gdt_space s, int norm, int quad_order, const double* u,
+                             const double* ref_qp, double* eta2, double* total) {
+  if (!ctx || !s || !u || !ref_qp || !eta2) return GDT_EINVAL;
+  if (norm != GDT_NORM_H1_SEMI && norm != GDT_NORM_L2) return fail(ctx, GDT_EINVAL, "unknown norm");
+  if (quad_order < 0 || quad_order > 40) return fail(ctx, GDT_EINVAL, "quadrature order out of range");
+  if (s->kind == GDT_SPACE_FV || (s->kind == GDT_SPACE_DG && s->order != 1))
+    return fail(ctx, GDT_EUNSUPPORTED, "element error of continuous (order 1, 2) and DG (order 1) spaces");
+  return element_error(ctx, *s, norm, quad_order, u, ref_qp, eta2, total);
+}
+
 gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs) {
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_DG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a DG space");
@@ -379,7 +394,8 @@ static gdt_status fv_check(gdt_context ctx, gdt_space s, const gdt_fv_desc* d) {
   if (s->kind != GDT_SPACE_FV) return fail(ctx, GDT_ESHAPE, "not a finite-volume space");
   if (!s->g.periodic) return fail(ctx, GDT_EUNSUPPORTED, "finite volumes need a periodic grid");
   if (d->flux != GDT_FLUX_BURGERS && d->flux != GDT_FLUX_TRANSPORT) return fail(ctx, GDT_EINVAL, "unknown flux");
-  if (d->numflux != GDT_NUMFLUX_LAX_FRIEDRICHS && d->numflux != GDT_NUMFLUX_UPWIND)
+  if (d->numflux != GDT_NUMFLUX_LAX_FRIEDRICHS && d->numflux != GDT_NUMFLUX_UPWIND &&
+      d->numflux != GDT_NUMFLUX_ENGQUIST_OSHER)
     return fail(ctx, GDT_EINVAL, "unknown numerical flux");
   return GDT_OK;
 }

@@ -1,8 +1,9 @@
 // Finite volumes on periodic structured cube grids (m = 1):
 //   AdvectionFvOperator::apply (operators/advection-fv.hh:66-115) = LocalAdvectionFvCouplingOperator on
 //   every inner/periodic intersection once (local/operators/advection-fv.hh:127-153) with
-//   NumericalLaxFriedrichsFlux (local/numerical-fluxes/lax-friedrichs.hh:61-87) or NumericalUpwindFlux
-//   (upwind.hh:61-73); estimate_dt_for_hyperbolic_system (tools/hyperbolic.hh:38-86); explicit Euler
+//   NumericalLaxFriedrichsFlux (local/numerical-fluxes/lax-friedrichs.hh:61-87), NumericalUpwindFlux
+//   (upwind.hh:61-73) or NumericalEngquistOsherFlux (engquist-osher.hh:72-103);
+//   estimate_dt_for_hyperbolic_system (tools/hyperbolic.hh:38-86); explicit Euler
 //   (test/instationary-eocstudies/base.hh:428-447) and ExplicitRungeKuttaTimeStepper with the SSP2
 //   tableau (tools/timestepper/explicit-rungekutta.hh:82-97, 237-270), r = -1.
 //
@@ -50,6 +51,14 @@ __device__ __forceinline__ double face_flux(const FvParams& p, int dim, int k, d
     }
     const double fsum = f_of(p, u, k) + f_of(p, v, k);
     return 0.5 * fma(u - v, lam, fsum);
+  }
+  if (p.numflux == GDT_NUMFLUX_ENGQUIST_OSHER) {
+    // f(0).n + int_0^u max(f'(s), 0) ds + int_0^v min(f'(s), 0) ds, each integral only for a positive
+    // state (the reference integrates over [0, state] only then); in closed form for both fluxes,
+    // f(0) = 0: Burgers f'(s) = s, transport f'(s) = v_k
+    if (p.flux == GDT_FLUX_BURGERS) return u > 0.0 ? 0.5 * u * u : 0.0;
+    const double a = p.vel[k];
+    return (u > 0.0 ? u * fmax(a, 0.0) : 0.0) + (v > 0.0 ? v * fmin(a, 0.0) : 0.0);
   }
   const double w = (u + v) * 0.5;
   return df_of(p, w, k) > 0.0 ? f_of(p, u, k) : f_of(p, v, k);

@@ -302,6 +302,85 @@ QuadratureInfo quadrature_info(const GridDesc& g, int order) {
   return r;
 }
 
+// affine map of element type t: J[:, m] = X_{m+1} - X_0 (cube: diag(h)); returns |det J|, Ji = J^-1
+static double type_jacobian(const GridDesc& g, bool simplex, int t, double (&Ji)[3][3]) {
+  double J[3][3] = {{0}};
+  if (!simplex) {
+    for (int a = 0; a < g.dim; ++a) J[a][a] = g.h[a];
+  } else {
+    for (int m = 0; m < g.dim; ++m) {
+      const int c = local_corner(g.dim, true, t, m + 1);
+      for (int a = 0; a < g.dim; ++a) J[a][m] = ((c >> a) & 1) ? g.h[a] : 0.0;
+    }
+  }
+  for (auto& r : Ji)
+    for (double& v : r) v = 0.0;
+  double det = 1.0;
+  if (g.dim == 1) {
+    det = J[0][0];
+    Ji[0][0] = 1.0 / det;
+  } else if (g.dim == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    Ji[0][0] = J[1][1] / det;
+    Ji[0][1] = -J[0][1] / det;
+    Ji[1][0] = -J[1][0] / det;
+    Ji[1][1] = J[0][0] / det;
+  } else {
+    det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+          J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        const int r1 = (c + 1) % 3, r2 = (c + 2) % 3, c1 = (r + 1) % 3, c2 = (r + 2) % 3;
+        Ji[r][c] = (J[r1][c1] * J[r2][c2] - J[r1][c2] * J[r2][c1]) / det;
+      }
+  }
+  return std::fabs(det);
+}
+
+BasisTables basis_tables(const GridDesc& g, int order, int quad_order) {
+  BasisTables B;
+  const bool simplex = g.simplex != 0 && g.dim >= 2;
+  const Nodal fe(g.dim, simplex, order);
+  const QRule q = quadrature(g.dim, simplex, quad_order);
+  B.lsize = fe.size;
+  B.nq = int(q.w.size());
+  B.ntypes = simplex ? num_sub(g.dim, true) : 1;
+  B.phi.assign(size_t(B.ntypes) * B.nq * B.lsize, 0.0);
+  B.grad.assign(size_t(B.ntypes) * B.nq * B.lsize * 3, 0.0);
+  B.wdet.assign(size_t(B.ntypes) * B.nq, 0.0);
+  std::vector<double> phi(fe.size), grbuf(3 * fe.size);
+  double(*gr)[3] = reinterpret_cast<double(*)[3]>(grbuf.data());
+  for (int t = 0; t < B.ntypes; ++t) {
+    double Ji[3][3];
+    const double adet = type_jacobian(g, simplex, t, Ji);
+    for (int k = 0; k < B.nq; ++k) {
+      fe.values(q.x[k], phi.data());
+      fe.gradients(q.x[k], gr);
+      B.wdet[size_t(t) * B.nq + k] = q.w[k] * adet;
+      for (int i = 0; i < fe.size; ++i) {
+        B.phi[(size_t(t) * B.nq + k) * B.lsize + i] = phi[i];
+        for (int a = 0; a < g.dim; ++a) {
+          double v = 0.0;
+          for (int r = 0; r < g.dim; ++r) v += Ji[r][a] * gr[i][r];
+          B.grad[((size_t(t) * B.nq + k) * B.lsize + i) * 3 + a] = v;
+        }
+      }
+    }
+  }
+  return B;
+}
+
+QuadratureInfo quadrature_info_order(const GridDesc& g, int quad_order) {
+  const QRule q = quadrature(g.dim, g.simplex != 0 && g.dim >= 2, quad_order);
+  QuadratureInfo r;
+  r.nq = int(q.w.size());
+  for (int k = 0; k < r.nq; ++k) {
+    for (int a = 0; a < 3; ++a) r.x.push_back(q.x[k].x[a]);
+    r.w.push_back(q.w[k]);
+  }
+  return r;
+}
+
 ContractionTables contraction_tables(const GridDesc& g, int order) {
   ContractionTables T;
   const bool simplex = g.simplex != 0 && g.dim >= 2;
@@ -325,37 +404,8 @@ ContractionTables contraction_tables(const GridDesc& g, int order) {
   std::vector<double> phi(fe.size), grbuf(3 * fe.size);
   double(*gr)[3] = reinterpret_cast<double(*)[3]>(grbuf.data());
   for (int t = 0; t < T.ntypes; ++t) {
-    // affine map of element type t: J[:, m] = X_{m+1} - X_0, X_j the corners of the type
-    double J[3][3] = {{0}};
-    if (!simplex) {
-      for (int a = 0; a < g.dim; ++a) J[a][a] = g.h[a];
-    } else {
-      for (int m = 0; m < g.dim; ++m) {
-        const int c = local_corner(g.dim, true, t, m + 1);
-        for (int a = 0; a < g.dim; ++a) J[a][m] = ((c >> a) & 1) ? g.h[a] : 0.0;
-      }
-    }
-    // inverse and determinant (dim <= 3)
-    double Ji[3][3] = {{0}}, det = 1.0;
-    if (g.dim == 1) {
-      det = J[0][0];
-      Ji[0][0] = 1.0 / det;
-    } else if (g.dim == 2) {
-      det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-      Ji[0][0] = J[1][1] / det;
-      Ji[0][1] = -J[0][1] / det;
-      Ji[1][0] = -J[1][0] / det;
-      Ji[1][1] = J[0][0] / det;
-    } else {
-      det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-            J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-      for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) {
-          const int r1 = (c + 1) % 3, r2 = (c + 2) % 3, c1 = (r + 1) % 3, c2 = (r + 2) % 3;
-          Ji[r][c] = (J[r1][c1] * J[r2][c2] - J[r1][c2] * J[r2][c1]) / det;
-        }
-    }
-    const double adet = std::fabs(det);
+    double Ji[3][3];
+    const double adet = type_jacobian(g, simplex, t, Ji);
     for (int k = 0; k < T.nq; ++k) {
       fe.values(q.x[k], phi.data());
       fe.gradients(q.x[k], gr);
@@ -646,7 +696,11 @@ __device__ __forceinline__ void dmma_8x8x4(double& d0, double& d1, double a, dou
                : "d"(a), "d"(b));
 }
 
-// one warp: 8 elements of colour c; K(pairs x 8) = M(pairs x q) C(q x 8), scattered into val
+// warp task: 8 elements of colour c and a group of kTileGroup row tiles (8 pairs each) of
+// K(pairs x 8) = M(pairs x q) C(q x 8), four tiles at a time (independent accumulator chains), each
+// tile scattered into val once complete
+constexpr int kTileGroup = 8;
+
 __global__ void __launch_bounds__(256) k_ho_contract(GridDesc g, Colour c, const double* __restrict__ M, int npair,
                                                      int npair_pad, int nq, int nq_pad, const int* __restrict__ pi,
                                                      const int* __restrict__ pj, const double* __restrict__ coef,
@@ -655,7 +709,11 @@ __global__ void __launch_bounds__(256) k_ho_contract(GridDesc g, Colour c, const
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long base = warp * 8; base < c.total; base += nwarps * 8) {
+  const int ntile = npair_pad / 8, ngroup = (ntile + kTileGroup - 1) / kTileGroup;
+  const long long ntask = (c.total + 7) / 8 * ngroup;
+  for (long long task = warp; task < ntask; task += nwarps) {
+    const long long base = task / ngroup * 8;
+    const int t0 = int(task % ngroup) * kTileGroup, t1 = min(ntile, t0 + kTileGroup);
     const long long lb = base + (lane >> 2);
     const bool vb = lb < c.total;
     const long long eb = vb ? colour_element(g, c, lb) : 0;
@@ -668,29 +726,36 @@ __global__ void __launch_bounds__(256) k_ho_contract(GridDesc g, Colour c, const
       vc[h] = lc < c.total;
       ec[h] = vc[h] ? colour_element(g, c, lc) : 0;
     }
-    for (int rt = 0; rt < npair_pad / 8; ++rt) {
-      double d0 = 0.0, d1 = 0.0;
-      const double* Mr = M + size_t(rt * 8 + (lane >> 2)) * nq_pad + (lane & 3);
+    auto scatter = [&](int rt, double d0, double d1) {
+      const int p = rt * 8 + (lane >> 2);
+      if (p >= npair) return;
+      const int i = pi[p], j = pj[p];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (!vc[h]) continue;
+        const double v = h ? d1 : d0;
+        const int* sm = smap + ec[h] * L * L;
+        val[sm[i * L + j]] += v;
+        if (i != j) val[sm[j * L + i]] += v;
+      }
+    };
+    for (int rt = t0; rt < t1; rt += 4) {
+      const int nt = min(4, t1 - rt);  // warp-uniform: up to four independent accumulator chains
+      double d[4][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+      const double* Ma = M + size_t(rt * 8 + (lane >> 2)) * nq_pad + (lane & 3);
       for (int kt = 0; kt < nq_pad / 4; ++kt) {
         double b = cb;
         if (coef_qp) {
           const int q = kt * 4 + (lane & 3);
           b = (vb && q < nq) ? coef_qp[eb * nq + q] : 0.0;
         }
-        dmma_8x8x4(d0, d1, __ldg(Mr + kt * 4), b);
-      }
-      const int p = rt * 8 + (lane >> 2);
-      if (p < npair) {
-        const int i = pi[p], j = pj[p];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          if (!vc[h]) continue;
-          const double v = h ? d1 : d0;
-          const int* sm = smap + ec[h] * L * L;
-          val[sm[i * L + j]] += v;
-          if (i != j) val[sm[j * L + i]] += v;
-        }
+        for (int k = 0; k < 4; ++k)
+          if (k < nt) dmma_8x8x4(d[k][0], d[k][1], __ldg(Ma + size_t(k) * 8 * nq_pad + kt * 4), b);
       }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < nt) scatter(rt + k, d[k][0], d[k][1]);
     }
   }
 }
@@ -899,7 +964,8 @@ gdt_status ho_assemble(gdt_context ctx, gdt_matrix m, int form, const double* co
     const Colour c = colour_of(g, k);
     if (c.total == 0) continue;
     const double* M = (form == 0 ? h->stiff : h->mass) + msize * c.t;
-    const int blocks = int(std::max(1LL, std::min<long long>((c.total + 63) / 64, ctx->num_sms * 8LL)));
+    const long long tasks = (c.total + 7) / 8 * ((T.npair_pad / 8 + kTileGroup - 1) / kTileGroup);
+    const int blocks = int(std::max(1LL, std::min<long long>((tasks + 7) / 8, ctx->num_sms * 8LL)));
     k_ho_contract<<<blocks, 256, 0, st>>>(g, c, M, T.npair, T.npair_pad, T.nq, T.nq_pad, h->pi, h->pj, coef,
                                           coef_const, coef_qp, h->smap, T.lsize, m->val);
     if (rhs)
@@ -958,6 +1024,103 @@ gdt_status ho_assemble_rhs(gdt_context ctx, const gdt_space_s& sp, const double*
 
 int ho_quadrature(const gdt_space_s& sp, double* x_ref, double* w_ref) {
   const ho::QuadratureInfo q = ho::quadrature_info(sp.g, sp.order);
+  for (int k = 0; k < q.nq; ++k) {
+    if (x_ref)
+      for (int a = 0; a < 3; ++a) x_ref[3 * k + a] = q.x[3 * k + a];
+    if (w_ref) w_ref[k] = q.w[k];
+  }
+  return q.nq;
+}
+
+namespace {
+
+// eta_e^2 = sum_q w_q |J| |grad u_h(x_q) - g(x_q)|^2 (norm 0) or (u_h(x_q) - v(x_q))^2 (norm 1)
+__global__ void k_element_error(GridDesc g, int L, int nq, int norm, const double* __restrict__ phi,
+                                const double* __restrict__ grad, const double* __restrict__ wdet,
+                                const int* __restrict__ gi, const double* __restrict__ u,
+                                const double* __restrict__ ref, double* __restrict__ eta2) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < g.nelem; e += (long long)gridDim.x * blockDim.x) {
+    const int t = int(e % g.nsub);
+    double ue[ho::kMaxL];
+    for (int i = 0; i < L; ++i) ue[i] = u[gi ? gi[e * L + i] : e * L + i];
+    double acc = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      const size_t tq = size_t(t) * nq + q;
+      if (norm == 0) {
+        double d2 = 0.0;
+        for (int a = 0; a < g.dim; ++a) {
+          double v = 0.0;
+          for (int i = 0; i < L; ++i) v = fma(ue[i], grad[(tq * L + i) * 3 + a], v);
+          const double d = v - ref[(e * nq + q) * g.dim + a];
+          d2 = fma(d, d, d2);
+        }
+        acc = fma(wdet[tq], d2, acc);
+      } else {
+        double v = 0.0;
+        for (int i = 0; i < L; ++i) v = fma(ue[i], phi[tq * L + i], v);
+        const double d = v - ref[e * nq + q];
+        acc = fma(wdet[tq], d * d, acc);
+      }
+    }
+    eta2[e] = acc;
+  }
+}
+
+}  // namespace
+
+gdt_status element_error(gdt_context ctx, const gdt_space_s& sp, int norm, int quad_order, const double* u,
+                         const double* ref, double* eta2, double* total) {
+  const GridDesc& g = sp.g;
+  cudaStream_t st = ctx->stream;
+  const ho::BasisTables B = ho::basis_tables(g, sp.order, quad_order);
+  if (B.lsize != sp.lsize) return fail(ctx, GDT_EUNSUPPORTED, "element error: unsupported space");
+  double *phi = nullptr, *grad = nullptr, *wdet = nullptr, *sum = nullptr;
+  int* gi = nullptr;
+  void* tmp = nullptr;
+  struct Freer {
+    void* p[6];
+    cudaStream_t s;
+    ~Freer() {
+      for (void* q : p)
+        if (q) cudaFreeAsync(q, s);
+    }
+  } freer{{}, st};
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&phi, sizeof(double) * B.phi.size(), st));
+  freer.p[0] = phi;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&grad, sizeof(double) * B.grad.size(), st));
+  freer.p[1] = grad;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&wdet, sizeof(double) * B.wdet.size(), st));
+  freer.p[2] = wdet;
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(phi, B.phi.data(), sizeof(double) * B.phi.size(), cudaMemcpyHostToDevice, st));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(grad, B.grad.data(), sizeof(double) * B.grad.size(), cudaMemcpyHostToDevice, st));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(wdet, B.wdet.data(), sizeof(double) * B.wdet.size(), cudaMemcpyHostToDevice, st));
+  if (sp.kind == GDT_SPACE_CG) {
+    GDT_TRY_CUDA(ctx, cudaMallocAsync(&gi, sizeof(int) * g.nelem * B.lsize, st));
+    freer.p[3] = gi;
+    GDT_CHECK(ctx, ho_global_indices(ctx, sp, nullptr, gi));
+  }
+  k_element_error<<<vec_grid(g.nelem, ctx->num_sms), 256, 0, st>>>(g, B.lsize, B.nq, norm, phi, grad, wdet, gi, u, ref,
+                                                                   eta2);
+  ctx->launches++;
+  if (total) {
+    GDT_TRY_CUDA(ctx, cudaMallocAsync(&sum, sizeof(double), st));
+    freer.p[4] = sum;
+    size_t tb = 0;
+    cub::DeviceReduce::Sum(nullptr, tb, eta2, sum, int(g.nelem), st);
+    GDT_TRY_CUDA(ctx, cudaMallocAsync(&tmp, std::max<size_t>(tb, 16), st));
+    freer.p[5] = tmp;
+    cub::DeviceReduce::Sum(tmp, tb, eta2, sum, int(g.nelem), st);
+    double h = 0.0;
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&h, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    *total = std::sqrt(h);
+  }
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(st));  // the host tables outlive the copies
+  return check_launch(ctx, "element error");
+}
+
+int quadrature_order(const gdt_space_s& sp, int quad_order, double* x_ref, double* w_ref) {
+  const ho::QuadratureInfo q = ho::quadrature_info_order(sp.g, quad_order);
   for (int k = 0; k < q.nq; ++k) {
     if (x_ref)
       for (int a = 0; a < 3; ++a) x_ref[3 * k + a] = q.x[3 * k + a];

@@ -37,6 +37,16 @@ struct QuadratureInfo {
   std::vector<double> x, w;
 };
 QuadratureInfo quadrature_info(const GridDesc& g, int order);
+QuadratureInfo quadrature_info_order(const GridDesc& g, int quad_order);
+
+// nodal basis values and physical gradients at the points of a quadrature rule, per element type
+struct BasisTables {
+  int lsize = 0, nq = 0, ntypes = 1;
+  std::vector<double> phi;   // [type][q][i]
+  std::vector<double> grad;  // [type][q][i][3]
+  std::vector<double> wdet;  // [type][q]: w_q |det J|
+};
+BasisTables basis_tables(const GridDesc& g, int order, int quad_order);
 
 }  // namespace ho
 
@@ -50,6 +60,9 @@ gdt_status ho_prepare(gdt_context ctx, gdt_matrix m);
 gdt_status ho_assemble_rhs(gdt_context ctx, const gdt_space_s& sp, const double* force, double force_const,
                            int dirichlet, double* rhs);
 int ho_quadrature(const gdt_space_s& sp, double* x_ref, double* w_ref);
+gdt_status element_error(gdt_context ctx, const gdt_space_s& sp, int norm, int quad_order, const double* u,
+                         const double* ref, double* eta2, double* total);
+int quadrature_order(const gdt_space_s& sp, int quad_order, double* x_ref, double* w_ref);
 struct HoMatrix;
 void ho_matrix_free(HoMatrix* h);
 

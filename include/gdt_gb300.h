@@ -64,7 +64,7 @@ enum { GDT_SOLVER_CG = 0, GDT_SOLVER_BICGSTAB = 1 };
 enum { GDT_PREC_NONE = 0, GDT_PREC_JACOBI = 1, GDT_PREC_ILU0 = 2 };
 enum { GDT_PRECISION_FP64 = 0, GDT_PRECISION_MIXED = 1 };
 enum { GDT_FLUX_BURGERS = 0, GDT_FLUX_TRANSPORT = 1 };
-enum { GDT_NUMFLUX_LAX_FRIEDRICHS = 0, GDT_NUMFLUX_UPWIND = 1 };
+enum { GDT_NUMFLUX_LAX_FRIEDRICHS = 0, GDT_NUMFLUX_UPWIND = 1, GDT_NUMFLUX_ENGQUIST_OSHER = 2 };
 enum { GDT_TIMESTEPPER_EXPLICIT_EULER = 0, GDT_TIMESTEPPER_SSPRK2 = 1 };
 
 /* ------------------------------------------------------------------ context --- */
@@ -182,6 +182,18 @@ gdt_status gdt_assemble_cg_product(gdt_context ctx, gdt_matrix m, const gdt_prod
  * nq; x_ref (nq x 3 reference-element coordinates) and w_ref (nq weights on the reference element)
  * may be NULL. The physical point of element e is its first vertex plus J_e x_ref. */
 int gdt_space_quadrature(gdt_space s, double* x_ref, double* w_ref);
+/* the same for a Gauss rule (Duffy-collapsed on simplices) exact to polynomial order quad_order */
+int gdt_space_quadrature_order(gdt_space s, int quad_order, double* x_ref, double* w_ref);
+
+/* element indicators of u_h - u_ref, as the EOC studies compute their norms
+ * (test/stationary-eocstudies/base.hh:259-269): per element eta_e^2 = int_e |grad u_h - g|^2
+ * (GDT_NORM_H1_SEMI, ref_qp = [element][q][dim] values of the reference gradient g) or
+ * int_e (u_h - v)^2 (GDT_NORM_L2, ref_qp = [element][q] values of v), with the points of
+ * gdt_space_quadrature_order(s, quad_order). u: device DoF vector of s (continuous order 1 or 2,
+ * DG order 1); eta2: device, one value per element; total (host, may be NULL) = sqrt(sum eta2). */
+enum { GDT_NORM_H1_SEMI = 0, GDT_NORM_L2 = 1 };
+gdt_status gdt_element_error(gdt_context ctx, gdt_space s, int norm, int quad_order, const double* u,
+                             const double* ref_qp, double* eta2, double* total);
 
 typedef struct gdt_ipdg_desc {
   const double* kappa;   /* device, per element, or NULL */

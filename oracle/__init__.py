@@ -21,7 +21,7 @@ FORCE_DATA, FORCE_ESV2007 = 0, 1
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 PREC_NONE, PREC_JACOBI, PREC_ILU0 = 0, 1, 2
 FLUX_BURGERS, FLUX_TRANSPORT = 0, 1
-NUMFLUX_LAX_FRIEDRICHS, NUMFLUX_UPWIND = 0, 1
+NUMFLUX_LAX_FRIEDRICHS, NUMFLUX_UPWIND, NUMFLUX_ENGQUIST_OSHER = 0, 1, 2
 
 
 def build(verbose: bool = False) -> str:

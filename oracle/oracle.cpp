@@ -1057,8 +1057,9 @@ inline double flux_f(int flux, const double* vel, double u, int d) {
 }
 inline double flux_df(int flux, const double* vel, double u, int d) { return flux == ORC_FLUX_BURGERS ? u : vel[d]; }
 
-// NumericalLaxFriedrichsFlux::apply (local/numerical-fluxes/lax-friedrichs.hh:61-87) and
-// NumericalUpwindFlux::apply (local/numerical-fluxes/upwind.hh:61-73), m = 1
+// NumericalLaxFriedrichsFlux::apply (local/numerical-fluxes/lax-friedrichs.hh:61-87),
+// NumericalUpwindFlux::apply (local/numerical-fluxes/upwind.hh:61-73) and
+// NumericalEngquistOsherFlux::apply (local/numerical-fluxes/engquist-osher.hh:72-103), m = 1
 double numerical_flux(int flux, const double* vel, int numflux, double lf_lambda, int dim, double u, double v,
                       const double* n) {
   if (numflux == ORC_NUMFLUX_LAX_FRIEDRICHS) {
@@ -1074,6 +1075,29 @@ double numerical_flux(int flux, const double* vel, int numflux, double lf_lambda
     for (int dd = 0; dd < dim; ++dd) ret += (flux_f(flux, vel, u, dd) + flux_f(flux, vel, v, dd)) * (n[dd] * 0.5);
     ret += (u - v) * (0.5 / lambda);
     return ret;
+  }
+  if (numflux == ORC_NUMFLUX_ENGQUIST_OSHER) {
+    // NumericalEngquistOsherFlux::apply (local/numerical-fluxes/engquist-osher.hh:72-103): f(0).n plus
+    // int_0^u max(n.f'(s), 0) ds and int_0^v min(n.f'(s), 0) ds, each by a Gauss rule of the flux
+    // order on [0, state] and only for a positive state (the reference builds the interval [0, state]
+    // only then and returns 0 otherwise)
+    double ret = 0.0;
+    for (int dd = 0; dd < dim; ++dd) ret += flux_f(flux, vel, 0.0, dd) * n[dd];
+    const int order = flux == ORC_FLUX_BURGERS ? 2 : 1;
+    std::vector<double> xq, wq;
+    gauss_legendre01(order / 2 + 1, xq, wq);
+    auto integral = [&](double state, bool take_max) {
+      if (!(state > 0.)) return 0.0;
+      double acc = 0.0;
+      for (size_t q = 0; q < xq.size(); ++q) {
+        const double uu = state * xq[q];
+        double ndf = 0.0;
+        for (int dd = 0; dd < dim; ++dd) ndf += n[dd] * flux_df(flux, vel, uu, dd);
+        acc += state * wq[q] * (take_max ? std::max(ndf, 0.0) : std::min(ndf, 0.0));
+      }
+      return acc;
+    };
+    return ret + integral(u, true) + integral(v, false);
   }
   double w = (u + v) / 2.;
   double nd = 0;

@@ -33,7 +33,7 @@ enum { ORC_FORCE_DATA = 0, ORC_FORCE_ESV2007 = 1 };
 enum { ORC_SOLVER_CG = 0, ORC_SOLVER_BICGSTAB = 1 };
 enum { ORC_PREC_NONE = 0, ORC_PREC_JACOBI = 1, ORC_PREC_ILU0 = 2 };
 enum { ORC_FLUX_BURGERS = 0, ORC_FLUX_TRANSPORT = 1 };
-enum { ORC_NUMFLUX_LAX_FRIEDRICHS = 0, ORC_NUMFLUX_UPWIND = 1 };
+enum { ORC_NUMFLUX_LAX_FRIEDRICHS = 0, ORC_NUMFLUX_UPWIND = 1, ORC_NUMFLUX_ENGQUIST_OSHER = 2 };
 
 typedef struct orc_csr orc_csr;
 

@@ -55,7 +55,7 @@ def main(root):
     burg = "dune/gdt/test/burgers/burgers__1d__explicit__fv.mini"
     text = read(root, burg)
     res["burgers_1d"] = {"source": burg}
-    for flux in ("numerical_upwind_flux", "numerical_lax_friedrichs_flux"):
+    for flux in ("numerical_upwind_flux", "numerical_lax_friedrichs_flux", "numerical_engquist_osher_flux"):
         base = "Burgers1dExplicitFvTest.periodic_boundaries__" + flux
         res["burgers_1d"][flux] = {"setup": mini_section(text, base + ".setup"),
                                    "results": mini_section(text, base + ".results")}

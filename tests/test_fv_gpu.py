@@ -30,19 +30,22 @@ CASES = [
     (2, [64, 64]),
     (3, [9, 7, 6]),
 ]
-FLUXES = [("burgers", "lf"), ("burgers", "upwind"), ("transport", "lf"), ("transport", "upwind")]
+FLUXES = [("burgers", "lf"), ("burgers", "upwind"), ("burgers", "eo"), ("transport", "lf"), ("transport", "upwind"),
+          ("transport", "eo")]
 
 
 def _op(gdt, g, flux, numflux, dim):
     fl = gdt.BurgersFlux() if flux == "burgers" else gdt.LinearTransportFlux([0.7, -0.4, 0.25][:dim])
-    nf = gdt.NumericalLaxFriedrichsFlux(fl) if numflux == "lf" else gdt.NumericalUpwindFlux(fl)
+    nf = {"lf": gdt.NumericalLaxFriedrichsFlux, "upwind": gdt.NumericalUpwindFlux,
+          "eo": gdt.NumericalEngquistOsherFlux}[numflux](fl)
     space = gdt.FiniteVolumeSpace(g)
     return gdt.AdvectionFvOperator(g, nf, space), space
 
 
 def _orc_args(oracle, flux, numflux, dim):
     return dict(flux=oracle.FLUX_BURGERS if flux == "burgers" else oracle.FLUX_TRANSPORT,
-                numflux=oracle.NUMFLUX_LAX_FRIEDRICHS if numflux == "lf" else oracle.NUMFLUX_UPWIND,
+                numflux={"lf": oracle.NUMFLUX_LAX_FRIEDRICHS, "upwind": oracle.NUMFLUX_UPWIND,
+                         "eo": oracle.NUMFLUX_ENGQUIST_OSHER}[numflux],
                 velocity=[0.7, -0.4, 0.25][:dim])
 
 
@@ -98,7 +101,7 @@ def test_fv_batched_equals_single(gdt, oracle):
         assert rel_err(out[b], ref) < 1e-12
 
 
-@pytest.mark.parametrize("flux", ["numerical_upwind_flux", "numerical_lax_friedrichs_flux"])
+@pytest.mark.parametrize("flux", ["numerical_upwind_flux", "numerical_lax_friedrichs_flux", "numerical_engquist_osher_flux"])
 def test_burgers_1d_tables_on_gpu(gdt, oracle, golden, flux):
     # dune/gdt/test/burgers/burgers__1d__explicit__fv.mini through the GPU path
     case = golden["burgers_1d"][flux]
@@ -106,7 +109,8 @@ def test_burgers_1d_tables_on_gpu(gdt, oracle, golden, flux):
     for lvl, n in enumerate((16, 32)):
         g = gdt.make_cube_grid([0.0], [1.0], [n], periodic=True)
         fl = gdt.BurgersFlux()
-        nf = gdt.NumericalUpwindFlux(fl) if "upwind" in flux else gdt.NumericalLaxFriedrichsFlux(fl)
+        nf = {"numerical_upwind_flux": gdt.NumericalUpwindFlux, "numerical_lax_friedrichs_flux": gdt.NumericalLaxFriedrichsFlux,
+              "numerical_engquist_osher_flux": gdt.NumericalEngquistOsherFlux}[flux](fl)
         op = gdt.AdvectionFvOperator(g, nf, gdt.FiniteVolumeSpace(g))
         u0 = fv_cell_average_1d(n, lambda x: np.exp(-(x - 0.33) ** 2 / (2 * 0.075 ** 2)), 3)
         ut = torch.tensor(u0, device="cuda")

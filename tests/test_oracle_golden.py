@@ -47,13 +47,14 @@ def _burgers_run(O, ncell, numflux, fixed_dt):
     return sols, dt / fv_dt
 
 
-@pytest.mark.parametrize("flux", ["numerical_upwind_flux", "numerical_lax_friedrichs_flux"])
+@pytest.mark.parametrize("flux", ["numerical_upwind_flux", "numerical_lax_friedrichs_flux", "numerical_engquist_osher_flux"])
 def test_burgers_1d_fv_tables(oracle, golden, flux):
     # dune/gdt/test/burgers/burgers__1d__explicit__fv.{cc,mini}: 16 and 32 cells, reference on 128
     O = oracle
     case = golden["burgers_1d"][flux]
     res = case["results"]
-    nf = O.NUMFLUX_UPWIND if "upwind" in flux else O.NUMFLUX_LAX_FRIEDRICHS
+    nf = {"numerical_upwind_flux": O.NUMFLUX_UPWIND, "numerical_lax_friedrichs_flux": O.NUMFLUX_LAX_FRIEDRICHS,
+          "numerical_engquist_osher_flux": O.NUMFLUX_ENGQUIST_OSHER}[flux]
     runs = {n: _burgers_run(O, n, nf, case["setup"]["use_fixed_dt"]) for n in (16, 32, 128)}
     for lvl, n in enumerate((16, 32)):
         sols, cfl = runs[n]
