@@ -24,8 +24,9 @@ __all__ = [
     "LocalIPDGBoundaryPenalty", "LocalCouplingIntersectionIntegralBilinearForm",
     "LocalIntersectionIntegralBilinearForm", "MatrixOperator", "VectorFunctional", "DirichletConstraints",
     "Walker", "DiscreteFunction", "BurgersFlux", "LinearTransportFlux", "NumericalLaxFriedrichsFlux",
-    "NumericalUpwindFlux", "NumericalEngquistOsherFlux", "AdvectionFvOperator", "ExplicitRungeKuttaTimeStepper",
-    "estimate_dt_for_hyperbolic_system", "GdtError", "element_error",
+    "NumericalUpwindFlux", "NumericalEngquistOsherFlux", "AdvectionFvOperator", "BoundaryTreatmentByCustomExtrapolation",
+    "BoundaryTreatmentByCustomNumericalFlux", "ExplicitRungeKuttaTimeStepper",
+    "estimate_dt_for_hyperbolic_system", "GdtError", "element_error", "LincombOperator", "lincomb",
 ]
 
 
@@ -544,6 +545,59 @@ class MatrixOperator:
         return source
 
 
+class LincombOperator:
+    """pyMOR's LincombOperator over assembled MatrixOperators that share one space and stencil, as the
+    parametric examples build it (python/dune/gdt/gamm-2019-talk-on-conservative-rb.cc:74-95,
+    examples/gamm_2019_talk_on_conservative_rb_OS2015_academic_example.py:62-77): the operator at mu is
+    sum_q theta_q(mu) A_q. `coefficients` are numbers or callables of mu (parameter functionals).
+    `assemble(mu)` forms the combined matrix on the device (one streaming kernel over the values) into
+    a MatrixOperator that is reused across parameters; `apply` and `apply_inverse` act on it."""
+
+    def __init__(self, operators, coefficients):
+        if not operators or len(operators) != len(coefficients) or len(operators) > 8:
+            raise GdtError(capi.EINVAL, "LincombOperator: 1..8 operators, one coefficient each")
+        self.operators, self.coefficients = list(operators), list(coefficients)
+        op0 = self.operators[0]
+        self.ctx = op0.ctx
+        self._target = None
+        self._mu = object()
+
+    def evaluate_coefficients(self, mu=None):
+        return [float(c(mu)) if callable(c) else float(c) for c in self.coefficients]
+
+    def assemble(self, mu=None):
+        theta = self.evaluate_coefficients(mu)
+        op0 = self.operators[0]
+        if self._target is None:
+            self._target = MatrixOperator(op0.grid, op0.source_space, op0.range_space, op0.stencil, ctx=self.ctx)
+        handles = (C.c_void_p * len(self.operators))(*[op.handle.value for op in self.operators])
+        th = (C.c_double * len(theta))(*theta)
+        self.ctx.call("gdt_matrix_lincomb", self._target.handle, len(theta), handles, th)
+        self._mu = mu
+        return self._target
+
+    def apply(self, U, mu=None, range=None):
+        return self.assemble(mu).apply(U, range)
+
+    def apply_inverse(self, V, mu=None, source=None, opts=None):
+        return self.assemble(mu).apply_inverse(V, source, opts)
+
+
+def lincomb(vectors, coefficients, out=None):
+    """sum_q coefficients[q] vectors[q] over FP64 device vectors of one length (gdt_lincomb)."""
+    if not vectors or len(vectors) != len(coefficients) or len(vectors) > 8:
+        raise GdtError(capi.EINVAL, "lincomb: 1..8 vectors, one coefficient each")
+    n = vectors[0].numel()
+    for v in vectors:
+        _f64(v, n, "vector")
+    if out is None:
+        out = torch.empty(n, dtype=torch.float64, device=vectors[0].device)
+    ptrs = (C.c_void_p * len(vectors))(*[v.data_ptr() for v in vectors])
+    th = (C.c_double * len(coefficients))(*[float(c) for c in coefficients])
+    default_context().call("gdt_lincomb", C.c_int64(n), len(vectors), ptrs, th, _ptr(_f64(out, n, "out")))
+    return out
+
+
 def _wrap(ptr, n, dtype, device):
     """Zero-copy CUDA tensor over library-owned device memory (lifetime: the owning handle)."""
     if n == 0:
@@ -699,14 +753,53 @@ def _fv_desc(numerical_flux):
     return d
 
 
+FV_SIDES = ("-x", "+x", "-y", "+y", "-z", "+z")
+
+
+class BoundaryTreatmentByCustomExtrapolation:
+    """LocalAdvectionFvBoundaryTreatmentByCustomExtrapolationOperator (local/operators/advection-fv.hh:
+    307-454) with its extrapolation lowered: the ghost state is the inside state (state=None, outflow)
+    or a prescribed state (inflow); the boundary flux is the operator's numerical flux g(u, v, n)."""
+
+    def __init__(self, state=None):
+        self.kind = capi.FV_BOUNDARY_EXTRAPOLATE if state is None else capi.FV_BOUNDARY_DIRICHLET
+        self.value = 0.0 if state is None else float(state)
+
+
+class BoundaryTreatmentByCustomNumericalFlux:
+    """LocalAdvectionFvBoundaryTreatmentByCustomNumericalFluxOperator (local/operators/advection-fv.hh:
+    187-305) with a constant boundary flux g = f.n in the outer normal direction (0: impermeable wall)."""
+
+    def __init__(self, flux=0.0):
+        self.kind = capi.FV_BOUNDARY_FLUX
+        self.value = float(flux)
+
+
 class AdvectionFvOperator:
-    """AdvectionFvOperator(grid_view, numerical_flux, source_space, range_space) on a periodic grid."""
+    """AdvectionFvOperator(grid_view, numerical_flux, source_space, range_space): the coupling on inner
+    and periodic intersections; `append` adds a boundary treatment on sides of the domain (on a
+    periodic grid those sides stop being periodic, as with the reference's periodicity restriction)."""
 
     def __init__(self, grid, numerical_flux, source_space, range_space=None, ctx: Context | None = None):
         self.grid, self.numerical_flux = grid, numerical_flux
         self.space = source_space
         self.ctx = ctx or default_context()
         self.desc = _fv_desc(numerical_flux)
+
+    def append(self, treatment, filter=None):
+        """append(boundary_treatment, filter): filter = the sides ("-x", "+x", "-y", ...) it applies
+        to; None: every boundary side of the grid (ApplyOn::BoundaryIntersections)."""
+        dim = self.grid.dimension
+        sides = FV_SIDES[: 2 * dim] if filter is None else ([filter] if isinstance(filter, str) else list(filter))
+        for side in sides:
+            if side not in FV_SIDES[: 2 * dim]:
+                raise GdtError(capi.EINVAL, f"no side {side!r} on a {dim}D grid")
+            k = FV_SIDES.index(side)
+            self.desc.boundary[k] = treatment.kind
+            self.desc.boundary_value[k] = treatment.value
+        return self
+
+    __iadd__ = append
 
     def apply(self, source, range=None, param=None):
         n = self.space.num_DoFs

@@ -21,6 +21,7 @@ PREC_NONE, PREC_JACOBI, PREC_ILU0 = 0, 1, 2
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 FLUX_BURGERS, FLUX_TRANSPORT = 0, 1
 NUMFLUX_LAX_FRIEDRICHS, NUMFLUX_UPWIND, NUMFLUX_ENGQUIST_OSHER = 0, 1, 2
+FV_BOUNDARY_NONE, FV_BOUNDARY_EXTRAPOLATE, FV_BOUNDARY_DIRICHLET, FV_BOUNDARY_FLUX = 0, 1, 2, 3
 TIMESTEPPER_EXPLICIT_EULER, TIMESTEPPER_SSPRK2 = 0, 1
 
 
@@ -60,7 +61,8 @@ class NewtonInfo(C.Structure):
 
 
 class FvDesc(C.Structure):
-    _fields_ = [("flux", C.c_int), ("velocity", C.c_double * 3), ("numflux", C.c_int), ("lf_lambda", C.c_double)]
+    _fields_ = [("flux", C.c_int), ("velocity", C.c_double * 3), ("numflux", C.c_int), ("lf_lambda", C.c_double),
+                ("boundary", C.c_int * 6), ("boundary_value", C.c_double * 6)]
 
 
 class BatchInfo(C.Structure):
@@ -115,6 +117,8 @@ _SIGNATURES = {
     "gdt_space_quadrature_order": (C.c_int, [P, C.c_int, P, P]),
     "gdt_element_error": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P, C.POINTER(C.c_double)]),
     "gdt_assemble_swipdg": (C.c_int, [P, P, C.POINTER(IpdgDesc), P]),
+    "gdt_lincomb": (C.c_int, [P, C.c_int64, C.c_int, C.POINTER(P), C.POINTER(C.c_double), P]),
+    "gdt_matrix_lincomb": (C.c_int, [P, P, C.c_int, C.POINTER(P), C.POINTER(C.c_double)]),
     "gdt_spmv": (C.c_int, [P, P, P, P]),
     "gdt_solve": (C.c_int, [P, P, P, P, C.POINTER(SolverOpts), C.POINTER(SolveInfo)]),
     "gdt_newton_default_opts": (NewtonOpts, []),

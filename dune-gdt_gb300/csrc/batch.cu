@@ -10,8 +10,12 @@
 // in rank order by every CTA (deterministic, no extra barrier); an iteration needs three cluster
 // barriers and no grid-wide synchronisation or software spin-wait. Matrix rows live in a 7-point
 // stencil layout (the CSR row order of the P1 triangle pattern) in per-cluster scratch sized for the
-// largest problem. Mixed precision: FP32 stencil/vectors in the inner CG, FP64 residual b - A x from
-// the FP64 stencil and FP64 correction of x between inner solves.
+// largest problem. Mixed precision: one FP32 CG sequence (FP32 stencil and vectors) with reliable
+// updates: whenever the iterated residual has dropped 10x since the last update, the FP32 correction is
+// added to the FP64 solution and the FP32 residual is replaced by the true residual b - A x from the
+// FP64 stencil (no restarts, so the Krylov sequence keeps its convergence rate). A problem whose
+// true residual stops following (the FP32 operator too inaccurate for its condition number) falls
+// back to restarted FP64 iterative refinement.
 #include <cooperative_groups.h>
 
 #include <cmath>
@@ -55,7 +59,6 @@ struct BatchArgs {
   double force;
   int mixed;
   double tol2;
-  double inner_tol2;
   int max_iter;
   double* x;
   double* stencil_out;
@@ -158,6 +161,115 @@ __device__ void cg_solve(const BatchArgs& a, cg::cluster_group& cl, double* slot
   }
 }
 
+// Mixed-precision CG with reliable updates for one problem: x (FP64) = 0 on entry, b the FP64 load;
+// the FP32 sequence iterates d32 (correction), r32, p32, q32. Convergence is decided on the true FP64
+// residual only; relres = ||b - A x|| / ||b|| of the returned x.
+__device__ void cg_reliable(const BatchArgs& a, cg::cluster_group& cl, double* slots, int n, long long lo, long long hi,
+                            const double* __restrict__ S, const double* __restrict__ b, double* __restrict__ x,
+                            const float* __restrict__ S32, const float* __restrict__ dinv, float* __restrict__ d,
+                            float* __restrict__ r, float* __restrict__ p, float* __restrict__ q, int& iters, int& conv,
+                            double& relres) {
+  const int nv = n + 1;
+  double v2[2] = {0.0, 0.0};
+  for (long long i = lo + threadIdx.x; i < hi; i += BT) {
+    const float ri = float(b[i]), zi = dinv[i] * ri;
+    r[i] = ri;
+    p[i] = zi;
+    d[i] = 0.0f;
+    v2[0] += double(ri) * double(zi);
+    v2[1] += b[i] * b[i];
+  }
+  cluster_reduce<2>(v2, slots, cl);
+  double rho = v2[0], rho_prev = rho;
+  const double rr0 = v2[1];
+  double rr_ref = rr0;       // true residual at the last replacement
+  double drop = 0.01;        // replace when the iterated residual has dropped by this factor (squared)
+  bool restarting = false;   // the FP32 operator is too far from the FP64 one to continue the sequence
+  conv = (rr0 == 0.0) ? 1 : 0;
+  relres = 0.0;
+  iters = 0;
+  cl.sync();  // p complete before the first SpMV
+  while (!conv && iters < a.max_iter) {
+    double v1[1] = {0.0};
+    for (long long i = lo + threadIdx.x; i < hi; i += BT) {
+      const long long ix = i % nv, iy = i / nv;
+      const float qi = stencil_row<float>(S32, p, i, nv, vbnd(ix, iy, n));
+      q[i] = qi;
+      v1[0] += double(p[i]) * double(qi);
+    }
+    cluster_reduce<1>(v1, slots + 2, cl);
+    if (!(v1[0] > 0.0)) break;  // breakdown: not SPD in FP32; the true residual below decides
+    const float alpha = float(rho / v1[0]);
+    double w2[2] = {0.0, 0.0};
+    for (long long i = lo + threadIdx.x; i < hi; i += BT) {
+      d[i] = fmaf(alpha, p[i], d[i]);
+      const float ri = fmaf(-alpha, q[i], r[i]);
+      r[i] = ri;
+      w2[0] += double(ri) * double(dinv[i] * ri);
+      w2[1] += double(ri) * double(ri);
+    }
+    cluster_reduce<2>(w2, slots + 4, cl);
+    ++iters;
+    double beta = w2[0] / rho;
+    rho_prev = rho;
+    rho = w2[0];
+    if (w2[1] <= drop * rr_ref || w2[1] <= a.tol2 * rr0 || iters >= a.max_iter) {
+      // reliable update: x += d, d = 0; r = b - A x (FP64), r32 = r; beta from the replaced residual
+      for (long long i = lo + threadIdx.x; i < hi; i += BT) {
+        x[i] += double(d[i]);
+        d[i] = 0.0f;
+      }
+      cl.sync();  // x complete before the FP64 residual reads the neighbours' rows
+      double t2[2] = {0.0, 0.0};
+      for (long long i = lo + threadIdx.x; i < hi; i += BT) {
+        const long long ix = i % nv, iy = i / nv;
+        const double ri = b[i] - stencil_row<double>(S, x, i, nv, vbnd(ix, iy, n));
+        const float rf = float(ri);
+        r[i] = rf;
+        t2[0] += double(rf) * double(dinv[i] * rf);
+        t2[1] += ri * ri;
+      }
+      cluster_reduce<2>(t2, slots + 6, cl);
+      // Stagnation guard: when a whole cycle gained less than 2x on the true residual, the gap between
+      // the FP32 and FP64 operators dominates (cond(A) times the FP32 rounding of A near 1). From then
+      // on every replacement restarts the direction (beta = 0) and waits for a 1000x drop: FP64
+      // iterative refinement around FP32 CG, which converges while the Krylov continuation stalls.
+      if (!restarting && t2[1] > 0.25 * rr_ref) {
+        restarting = true;
+        drop = 1e-6;
+      }
+      rr_ref = t2[1];
+      relres = rr0 > 0.0 ? sqrt(t2[1] / rr0) : 0.0;
+      beta = restarting ? 0.0 : t2[0] / rho_prev;
+      rho = t2[0];
+      if (t2[1] <= a.tol2 * rr0) {
+        conv = 1;
+        break;
+      }
+    }
+    const float bf = float(beta);
+    for (long long i = lo + threadIdx.x; i < hi; i += BT) p[i] = fmaf(bf, p[i], dinv[i] * r[i]);
+    cl.sync();
+  }
+  if (!conv) {  // stopped by breakdown or the iteration limit: fold in the correction, report the true residual
+    cl.sync();
+    for (long long i = lo + threadIdx.x; i < hi; i += BT) {
+      x[i] += double(d[i]);
+      d[i] = 0.0f;
+    }
+    cl.sync();
+    double t1[1] = {0.0};
+    for (long long i = lo + threadIdx.x; i < hi; i += BT) {
+      const long long ix = i % nv, iy = i / nv;
+      const double ri = b[i] - stencil_row<double>(S, x, i, nv, vbnd(ix, iy, n));
+      t1[0] += ri * ri;
+    }
+    cluster_reduce<1>(t1, slots + 6, cl);
+    relres = rr0 > 0.0 ? sqrt(t1[0] / rr0) : 0.0;
+    if (t1[0] <= a.tol2 * rr0) conv = 1;
+  }
+}
+
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BT) batch_kernel(BatchArgs a) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = int(cl.block_rank());
@@ -244,37 +356,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BT) batch_kernel(Ba
       cluster_reduce<2>(v2, slots, cl);
       relres = v2[1] > 0 ? sqrt(v2[0] / v2[1]) : 0.0;
     } else {
-      // FP64 iterative refinement around FP32 CG; x0 = 0, r = b
-      double rr0 = -1.0;
-      for (int outer = 0; outer < 100; ++outer) {
-        double v1[1] = {0.0};
-        for (long long i = lo + threadIdx.x; i < hi; i += BT) {
-          const long long ix = i % nv, iy = i / nv;
-          const double ri = b[i] - stencil_row<double>(S, x, i, nv, vbnd(ix, iy, n));
-          r[i] = ri;
-          v1[0] += ri * ri;
-        }
-        cluster_reduce<1>(v1, slots, cl);
-        if (rr0 < 0) rr0 = v1[0];
-        relres = rr0 > 0 ? sqrt(v1[0] / rr0) : 0.0;
-        if (v1[0] <= a.tol2 * rr0 || v1[0] == 0.0) {
-          conv = 1;
-          break;
-        }
-        if (iters >= a.max_iter) break;
-        const double scale = sqrt(v1[0]), inv = 1.0 / scale;
-        for (long long i = lo + threadIdx.x; i < hi; i += BT) {
-          r32[i] = float(r[i] * inv);
-          d32[i] = 0.0f;
-        }
-        cl.sync();
-        int it = 0, c = 0;
-        cg_solve<float>(a, cl, slots, n, lo, hi, S32, dinv32, d32, r32, p32, q32, a.inner_tol2, a.max_iter - iters, it,
-                        c);
-        iters += it;
-        for (long long i = lo + threadIdx.x; i < hi; i += BT) x[i] = fma(scale, double(d32[i]), x[i]);
-        cl.sync();
-      }
+      cg_reliable(a, cl, slots, n, lo, hi, S, b, x, S32, dinv32, d32, r32, p32, q32, iters, conv, relres);
     }
     if (rank == 0 && threadIdx.x == 0) {
       a.iters[prob] = conv ? iters : -iters - 1;
@@ -388,7 +470,6 @@ gdt_status gdt_batch_solve(gdt_context ctx, gdt_batch b, const double* mu, doubl
   a.force = force;
   a.mixed = precision == GDT_PRECISION_MIXED;
   a.tol2 = tol * tol;
-  a.inner_tol2 = 1e-3 * 1e-3;
   a.max_iter = max_iter;
   a.x = x;
   a.stencil_out = stencil_out;

@@ -392,7 +392,16 @@ gdt_status gdt_solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, 
 static gdt_status fv_check(gdt_context ctx, gdt_space s, const gdt_fv_desc* d) {
   if (!ctx || !s || !d) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_FV) return fail(ctx, GDT_ESHAPE, "not a finite-volume space");
-  if (!s->g.periodic) return fail(ctx, GDT_EUNSUPPORTED, "finite volumes need a periodic grid");
+  for (int side = 0; side < 6; ++side) {
+    if (d->boundary[side] < GDT_FV_BOUNDARY_NONE || d->boundary[side] > GDT_FV_BOUNDARY_FLUX)
+      return fail(ctx, GDT_EINVAL, "unknown boundary treatment");
+    if (side >= 2 * s->g.dim && d->boundary[side] != GDT_FV_BOUNDARY_NONE)
+      return fail(ctx, GDT_EINVAL, "boundary treatment on a side the grid does not have");
+  }
+  if (s->g.periodic)
+    for (int k = 0; k < s->g.dim; ++k)
+      if ((d->boundary[2 * k] == GDT_FV_BOUNDARY_NONE) != (d->boundary[2 * k + 1] == GDT_FV_BOUNDARY_NONE))
+        return fail(ctx, GDT_EINVAL, "periodic grid: treat both sides of a direction or neither");
   if (d->flux != GDT_FLUX_BURGERS && d->flux != GDT_FLUX_TRANSPORT) return fail(ctx, GDT_EINVAL, "unknown flux");
   if (d->numflux != GDT_NUMFLUX_LAX_FRIEDRICHS && d->numflux != GDT_NUMFLUX_UPWIND &&
       d->numflux != GDT_NUMFLUX_ENGQUIST_OSHER)

@@ -1,6 +1,7 @@
-// Finite volumes on periodic structured cube grids (m = 1):
+// Finite volumes on structured cube grids (m = 1):
 //   AdvectionFvOperator::apply (operators/advection-fv.hh:66-115) = LocalAdvectionFvCouplingOperator on
-//   every inner/periodic intersection once (local/operators/advection-fv.hh:127-153) with
+//   every inner/periodic intersection once (local/operators/advection-fv.hh:127-153), the boundary
+//   treatments by extrapolation or by a boundary flux on the non-periodic sides (:187-457), with
 //   NumericalLaxFriedrichsFlux (local/numerical-fluxes/lax-friedrichs.hh:61-87), NumericalUpwindFlux
 //   (upwind.hh:61-73) or NumericalEngquistOsherFlux (engquist-osher.hh:72-103);
 //   estimate_dt_for_hyperbolic_system (tools/hyperbolic.hh:38-86); explicit Euler
@@ -28,6 +29,8 @@ struct FvParams {
   int numflux;    // GDT_NUMFLUX_*
   double vel[3];
   double lf_inv_lambda;  // 0: local LF; else the reference's fixed lambda_ (coefficient 0.5 / lambda_)
+  int bkind[6];          // per side (-x, +x, -y, +y, -z, +z): GDT_FV_BOUNDARY_*, or -1 for a periodic side
+  double bval[6];
 };
 
 __device__ __forceinline__ double f_of(const FvParams& p, double u, int d) {
@@ -37,8 +40,9 @@ __device__ __forceinline__ double df_of(const FvParams& p, double u, int d) {
   return p.flux == GDT_FLUX_BURGERS ? u : p.vel[d];
 }
 
-// numerical flux across a face with unit normal +e_k, seen from the lower cell (value u) to the upper (v)
-__device__ __forceinline__ double face_flux(const FvParams& p, int dim, int k, double u, double v) {
+// numerical flux g(u, v, n) for the unit normal n = sgn e_k (sgn = +-1), u the state on the side n
+// points away from
+__device__ __forceinline__ double normal_flux(const FvParams& p, int dim, int k, double sgn, double u, double v) {
   if (p.numflux == GDT_NUMFLUX_LAX_FRIEDRICHS) {
     double lam;
     if (p.lf_inv_lambda != 0.0) {
@@ -49,23 +53,50 @@ __device__ __forceinline__ double face_flux(const FvParams& p, int dim, int k, d
       lam = 0.0;
       for (int d = 0; d < dim; ++d) lam = fmax(lam, fabs(p.vel[d]));
     }
-    const double fsum = f_of(p, u, k) + f_of(p, v, k);
+    const double fsum = sgn * (f_of(p, u, k) + f_of(p, v, k));
     return 0.5 * fma(u - v, lam, fsum);
   }
   if (p.numflux == GDT_NUMFLUX_ENGQUIST_OSHER) {
-    // f(0).n + int_0^u max(f'(s), 0) ds + int_0^v min(f'(s), 0) ds, each integral only for a positive
-    // state (the reference integrates over [0, state] only then); in closed form for both fluxes,
-    // f(0) = 0: Burgers f'(s) = s, transport f'(s) = v_k
-    if (p.flux == GDT_FLUX_BURGERS) return u > 0.0 ? 0.5 * u * u : 0.0;
-    const double a = p.vel[k];
+    // f(0).n + int_0^u max(n.f'(s), 0) ds + int_0^v min(n.f'(s), 0) ds, each integral only for a
+    // positive state (the reference integrates over [0, state] only then); in closed form for both
+    // fluxes, f(0) = 0: Burgers n.f'(s) = sgn s, transport n.f'(s) = sgn v_k
+    if (p.flux == GDT_FLUX_BURGERS) {
+      if (sgn > 0.0) return u > 0.0 ? 0.5 * u * u : 0.0;
+      return v > 0.0 ? -0.5 * v * v : 0.0;
+    }
+    const double a = sgn * p.vel[k];
     return (u > 0.0 ? u * fmax(a, 0.0) : 0.0) + (v > 0.0 ? v * fmin(a, 0.0) : 0.0);
   }
   const double w = (u + v) * 0.5;
-  return df_of(p, w, k) > 0.0 ? f_of(p, u, k) : f_of(p, v, k);
+  return sgn * df_of(p, w, k) > 0.0 ? sgn * f_of(p, u, k) : sgn * f_of(p, v, k);
+}
+
+// numerical flux across a face with unit normal +e_k, seen from the lower cell (value u) to the upper (v)
+__device__ __forceinline__ double face_flux(const FvParams& p, int dim, int k, double u, double v) {
+  return normal_flux(p, dim, k, 1.0, u, v);
+}
+
+// flux through the boundary face on `side` (2k: -e_k, 2k+1: +e_k) of a cell with value u, in the
+// direction of the outer normal (what the boundary operator adds as g |I| / |E|)
+__device__ __forceinline__ double boundary_flux(const FvParams& p, int dim, int side, double u) {
+  const int kind = p.bkind[side];
+  const int k = side >> 1;
+  const double sgn = (side & 1) ? 1.0 : -1.0;
+  if (kind == GDT_FV_BOUNDARY_EXTRAPOLATE) return normal_flux(p, dim, k, sgn, u, u);
+  if (kind == GDT_FV_BOUNDARY_DIRICHLET) return normal_flux(p, dim, k, sgn, u, p.bval[side]);
+  if (kind == GDT_FV_BOUNDARY_FLUX) return p.bval[side];
+  return 0.0;  // GDT_FV_BOUNDARY_NONE on a non-periodic grid: no operator on this side
+}
+
+// flux in +e_k direction through the lower (upper = false) or upper boundary face of a cell
+__device__ __forceinline__ double boundary_face_flux(const FvParams& p, int dim, int k, bool upper, double u) {
+  const double g = boundary_flux(p, dim, 2 * k + (upper ? 1 : 0), u);
+  return upper ? g : -g;
 }
 
 // ------------------------------------------------------------------------- generic (any dim) ---
-// range[c] = sum over the 2d faces of c of +-flux * |I| / |E| (periodic neighbours)
+// range[c] = sum over the 2d faces of c of +-flux * |I| / |E| (periodic neighbours, or the boundary
+// treatment of the side)
 __global__ void fv_apply_kernel(GridDesc g, FvParams p, long long nbatch, const double* __restrict__ u,
                                 double* __restrict__ out, const double* __restrict__ ubase, double a_u1,
                                 int mode, double* __restrict__ u_next, double dt_coef) {
@@ -91,6 +122,22 @@ __global__ void fv_apply_kernel(GridDesc g, FvParams p, long long nbatch, const 
     double vol = 1.0;
     for (int j = 0; j < g.dim; ++j) vol *= g.h[j];
     const double coef = area / vol;
+    if (p.bkind[2 * k] >= 0) {  // boundary treatments on both sides of direction k
+      const double fl = ci[k] == 0 ? boundary_face_flux(p, g.dim, k, false, uc) : 0.0;
+      const double fu = ci[k] == g.n[k] - 1 ? boundary_face_flux(p, g.dim, k, true, uc) : 0.0;
+      long long cm[3] = {ci[0], ci[1], ci[2]}, cp[3] = {ci[0], ci[1], ci[2]};
+      double lo = fl, hi = fu;
+      if (ci[k] > 0) {
+        cm[k] = ci[k] - 1;
+        lo = face_flux(p, g.dim, k, val(cell_index(g, cm)), uc);
+      }
+      if (ci[k] < g.n[k] - 1) {
+        cp[k] = ci[k] + 1;
+        hi = face_flux(p, g.dim, k, uc, val(cell_index(g, cp)));
+      }
+      acc += coef * (hi - lo);
+      continue;
+    }
     long long cm[3] = {ci[0], ci[1], ci[2]}, cp[3] = {ci[0], ci[1], ci[2]};
     cm[k] = (ci[k] + g.n[k] - 1) % g.n[k];
     cp[k] = (ci[k] + 1) % g.n[k];
@@ -108,7 +155,8 @@ constexpr int TX = 32, TY = 32, BY = 8;  // tile TX x TY cells, block TX x BY th
 
 // STAGE 0: k = L(u) ; STAGE 1 (Euler): u_next = u - dt L(u) ;
 // STAGE 2: u1 = u - dt k0 on the tile + halo, u_next = u + (-dt/2) (k0 + L(u1))
-template <int STAGE>
+// BND: some side has a boundary treatment; the faces on those sides are then replaced by it
+template <int STAGE, bool BND>
 __global__ void __launch_bounds__(TX* BY) fv2d_tile(GridDesc g, FvParams p, const double* __restrict__ u,
                                                     const double* __restrict__ k0, double* __restrict__ out,
                                                     double dt, double cx, double cy) {
@@ -133,9 +181,21 @@ __global__ void __launch_bounds__(TX* BY) fv2d_tile(GridDesc g, FvParams p, cons
   __syncthreads();
   // x faces: between tile columns i-1 and i (i = 0..TX), rows 0..TY-1
   for (int j = ty; j < TY; j += BY)
-    for (int i = tx; i <= TX; i += TX) gx[j][i] = face_flux(p, 2, 0, s[j + 1][i], s[j + 1][i + 1]);
+    for (int i = tx; i <= TX; i += TX) {
+      double f;
+      if (BND && p.bkind[0] >= 0 && x0 + i == 0) f = boundary_face_flux(p, 2, 0, false, s[j + 1][i + 1]);
+      else if (BND && p.bkind[0] >= 0 && x0 + i == nx) f = boundary_face_flux(p, 2, 0, true, s[j + 1][i]);
+      else f = face_flux(p, 2, 0, s[j + 1][i], s[j + 1][i + 1]);
+      gx[j][i] = f;
+    }
   // y faces: between tile rows j-1 and j (j = 0..TY)
-  for (int j = ty; j <= TY; j += BY) gy[j][tx] = face_flux(p, 2, 1, s[j][tx + 1], s[j + 1][tx + 1]);
+  for (int j = ty; j <= TY; j += BY) {
+    double f;
+    if (BND && p.bkind[2] >= 0 && y0 + j == 0) f = boundary_face_flux(p, 2, 1, false, s[j + 1][tx + 1]);
+    else if (BND && p.bkind[2] >= 0 && y0 + j == ny) f = boundary_face_flux(p, 2, 1, true, s[j][tx + 1]);
+    else f = face_flux(p, 2, 1, s[j][tx + 1], s[j + 1][tx + 1]);
+    gy[j][tx] = f;
+  }
   __syncthreads();
   const long long gxi = x0 + tx;
   if (gxi >= nx) return;
@@ -150,13 +210,25 @@ __global__ void __launch_bounds__(TX* BY) fv2d_tile(GridDesc g, FvParams p, cons
   }
 }
 
-FvParams make_params(const gdt_fv_desc* d) {
+FvParams make_params(const GridDesc& g, const gdt_fv_desc* d) {
   FvParams p;
   p.flux = d->flux;
   p.numflux = d->numflux;
   for (int i = 0; i < 3; ++i) p.vel[i] = d->velocity[i];
   p.lf_inv_lambda = d->lf_lambda;
+  for (int side = 0; side < 6; ++side) {
+    // a side is periodic when the grid is and no treatment is given; otherwise the treatment (or none)
+    const bool periodic = g.periodic && d->boundary[side] == GDT_FV_BOUNDARY_NONE;
+    p.bkind[side] = periodic ? -1 : d->boundary[side];
+    p.bval[side] = d->boundary_value[side];
+  }
   return p;
+}
+
+bool has_boundary(const FvParams& p, int dim) {
+  for (int side = 0; side < 2 * dim; ++side)
+    if (p.bkind[side] >= 0) return true;
+  return false;
 }
 
 bool tiled_ok(const GridDesc& g) { return g.dim == 2 && g.n[0] >= 2 && g.n[1] >= 2; }
@@ -165,10 +237,13 @@ bool tiled_ok(const GridDesc& g) { return g.dim == 2 && g.n[0] >= 2 && g.n[1] >=
 
 gdt_status fv_apply(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc* d, const double* u, double* out) {
   const GridDesc& g = sp.g;
-  FvParams p = make_params(d);
+  FvParams p = make_params(g, d);
   if (tiled_ok(g)) {
     dim3 grid((unsigned)((g.n[0] + TX - 1) / TX), (unsigned)((g.n[1] + TY - 1) / TY), 1);
-    fv2d_tile<0><<<grid, dim3(TX, BY), 0, ctx->stream>>>(g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
+    if (has_boundary(p, 2))
+      fv2d_tile<0, true><<<grid, dim3(TX, BY), 0, ctx->stream>>>(g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
+    else
+      fv2d_tile<0, false><<<grid, dim3(TX, BY), 0, ctx->stream>>>(g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
   } else {
     fv_apply_kernel<<<grid_blocks(g.nelem, 256), 256, 0, ctx->stream>>>(g, p, 1, u, out, nullptr, 0.0, 0, nullptr,
                                                                         0.0);
@@ -232,26 +307,32 @@ gdt_status fv_timestep(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc
                        long long steps, long long nbatch, double* u, double* work) {
   // work holds 2 * nbatch * N doubles for SSP-RK2 (k0 and the next state), nbatch * N for Euler
   const GridDesc& g = sp.g;
-  const FvParams p = make_params(d);
+  const FvParams p = make_params(g, d);
   cudaStream_t s = ctx->stream;
   const long long N = g.nelem * nbatch;
   double* cur = u;
   double* nxt = (stepper == GDT_TIMESTEPPER_SSPRK2) ? work + N : work;
   double* k0 = work;
   const bool tiled = tiled_ok(g);
+  const bool bnd = has_boundary(p, g.dim);
   dim3 grid((unsigned)((g.n[0] + TX - 1) / TX), (unsigned)((g.n[1] + TY - 1) / TY), (unsigned)nbatch);
   const double cx = 1.0 / g.h[0], cy = g.dim >= 2 ? 1.0 / g.h[1] : 0.0;
   for (long long st = 0; st < steps; ++st) {
     if (stepper == GDT_TIMESTEPPER_EXPLICIT_EULER) {
-      if (tiled)
-        fv2d_tile<1><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, nxt, dt, cx, cy);
+      if (tiled && bnd)
+        fv2d_tile<1, true><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, nxt, dt, cx, cy);
+      else if (tiled)
+        fv2d_tile<1, false><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, nxt, dt, cx, cy);
       else
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, nullptr, nullptr, 0.0, 1, nxt, dt);
       ctx->launches++;
     } else {
-      if (tiled) {
-        fv2d_tile<0><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, k0, dt, cx, cy);
-        fv2d_tile<2><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, k0, nxt, dt, cx, cy);
+      if (tiled && bnd) {
+        fv2d_tile<0, true><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, k0, dt, cx, cy);
+        fv2d_tile<2, true><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, k0, nxt, dt, cx, cy);
+      } else if (tiled) {
+        fv2d_tile<0, false><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, k0, dt, cx, cy);
+        fv2d_tile<2, false><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, k0, nxt, dt, cx, cy);
       } else {
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, k0, nullptr, 0.0, 0, nullptr, 0.0);
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, nullptr, k0, cur, -dt, 2, nxt, -0.5 * dt);

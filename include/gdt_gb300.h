@@ -210,6 +210,21 @@ typedef struct gdt_ipdg_desc {
  * DirichletCoupling/BoundaryPenalty (homogeneous Dirichlet boundary), penalty length h = |I|. */
 gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* desc, double* rhs);
 
+/* ------------------------------------------------------ parametric lincomb --- */
+/* The assembled form of pyMOR's LincombOperator over dune-gdt matrices, as the parametric examples
+ * build it (one matrix per coefficient function of an affine decomposition,
+ * python/dune/gdt/gamm-2019-talk-on-conservative-rb.cc:74-95, combined with the parameter
+ * functionals' values theta_q(mu),
+ * examples/gamm_2019_talk_on_conservative_rb_OS2015_academic_example.py:62-77).
+ * gdt_lincomb: out[i] = sum_q theta[q] terms[q][i] over n FP64 values (device arrays; out may be one
+ * of the terms). gdt_matrix_lincomb: the values of `out` = sum_q theta[q] values of terms[q]; every
+ * term must have the pattern of `out` (same spaces and stencil), else GDT_ESHAPE. 1..8 terms. */
+#define GDT_LINCOMB_MAX_TERMS 8
+gdt_status gdt_lincomb(gdt_context ctx, int64_t n, int nterms, const double* const* terms, const double* theta,
+                       double* out);
+gdt_status gdt_matrix_lincomb(gdt_context ctx, gdt_matrix out, int nterms, const gdt_matrix* terms,
+                              const double* theta);
+
 /* ------------------------------------------------------------ apply / solve --- */
 gdt_status gdt_spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y);
 
@@ -273,14 +288,31 @@ gdt_status gdt_solve_cg_jacobi_noalloc(const int32_t* row_ptr, const int32_t* co
                                        gdt_solve_info* info);
 
 /* --------------------------------------------------------------- finite volume --- */
+/* Treatment of the intersections on one side of the domain (sides -x, +x, -y, +y, -z, +z). The
+ * reference appends a boundary operator to AdvectionFvOperator for them (operators/advection-fv.hh:95-115:
+ * LocalAdvectionFvBoundaryTreatmentByCustomExtrapolationOperator, local/operators/advection-fv.hh:307-454,
+ * and ...ByCustomNumericalFluxOperator, :187-305, on the boundary intersections, with the periodic
+ * coupling restricted away from them). Its user lambdas are lowered to these kinds; g is added to the
+ * inside cell as g |I| / |E|, n the unit outer normal:
+ *   NONE: periodic coupling on a periodic grid; on a non-periodic grid no operator (no flux)
+ *   EXTRAPOLATE: ghost state v = u (outflow), g = numerical flux(u, v, n)
+ *   DIRICHLET: ghost state v = value (prescribed inflow state), g = numerical flux(u, v, n)
+ *   FLUX: g = value, the boundary flux f.n itself (value 0: impermeable wall)
+ * On a periodic grid both sides of a direction are NONE or both are not. */
+enum { GDT_FV_BOUNDARY_NONE = 0, GDT_FV_BOUNDARY_EXTRAPOLATE = 1, GDT_FV_BOUNDARY_DIRICHLET = 2,
+       GDT_FV_BOUNDARY_FLUX = 3 };
+
 typedef struct gdt_fv_desc {
   int flux;              /* GDT_FLUX_BURGERS: f(u) = u^2/2 (1,..,1); GDT_FLUX_TRANSPORT: f(u) = v u */
   double velocity[3];
   int numflux;           /* GDT_NUMFLUX_* */
   double lf_lambda;      /* 0: local Lax-Friedrichs (max_d |f_d'|); else the reference's fixed lambda */
+  int boundary[6];       /* GDT_FV_BOUNDARY_* per side (-x, +x, -y, +y, -z, +z); zero-filled: NONE */
+  double boundary_value[6];
 } gdt_fv_desc;
 
-/* range = AdvectionFvOperator(u) on a periodic cube grid (FV space, m = 1) */
+/* range = AdvectionFvOperator(u) on a cube grid (FV space, m = 1): inner and periodic intersections
+ * once, boundary intersections by the treatment of their side */
 gdt_status gdt_fv_apply(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, const double* u, double* range);
 /* dt of estimate_dt_for_hyperbolic_system for initial data u0 (host result) */
 gdt_status gdt_fv_estimate_dt(gdt_context ctx, gdt_space fv, const gdt_fv_desc* desc, const double* u0, double* dt);

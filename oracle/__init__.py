@@ -101,9 +101,10 @@ def lib():
             "orc_h1_semi_error_esv2007": (C.c_double, [g, C.c_int, C.c_int, dp]),
             "orc_l2_norm": (C.c_double, [g, C.c_int, C.c_int, dp]),
             "orc_fv_estimate_dt": (C.c_double, [g, C.c_int, dp, dp]),
-            "orc_fv_apply": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, dp]),
-            "orc_fv_explicit_euler": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, C.c_double, C.c_long]),
-            "orc_fv_ssprk2": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, C.c_double, C.c_long]),
+            "orc_fv_apply": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, dp, ip, dp]),
+            "orc_fv_explicit_euler": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, C.c_double, C.c_long, ip,
+                                             dp]),
+            "orc_fv_ssprk2": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, C.c_double, C.c_long, ip, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -274,20 +275,35 @@ def fv_estimate_dt(g, flux, u0, velocity=None):
                                           _dp(np.ascontiguousarray(u0, np.float64))))
 
 
-def fv_apply(g, flux, numflux, u, velocity=None, lf_lambda=0.0):
+def _boundary(boundary, boundary_value):
+    """(kinds, values) per side (-x, +x, -y, +y, -z, +z) as C arrays, or (None, None)"""
+    if boundary is None:
+        return None, None
+    kinds = (C.c_int * 6)(*([int(k) for k in boundary] + [0] * (6 - len(boundary))))
+    vals = list(boundary_value) if boundary_value is not None else []
+    values = (C.c_double * 6)(*([float(v) for v in vals] + [0.0] * (6 - len(vals))))
+    return kinds, C.cast(values, C.POINTER(C.c_double))
+
+
+def fv_apply(g, flux, numflux, u, velocity=None, lf_lambda=0.0, boundary=None, boundary_value=None):
     out = np.empty(len(u))
+    bk, bv = _boundary(boundary, boundary_value)
     lib().orc_fv_apply(C.byref(g), flux, _dp(_vel(velocity)), numflux, lf_lambda,
-                       _dp(np.ascontiguousarray(u, np.float64)), _dp(out))
+                       _dp(np.ascontiguousarray(u, np.float64)), _dp(out), bk, bv)
     return out
 
 
-def fv_explicit_euler(g, flux, numflux, u, dt, steps, velocity=None, lf_lambda=0.0):
+def fv_explicit_euler(g, flux, numflux, u, dt, steps, velocity=None, lf_lambda=0.0, boundary=None,
+                      boundary_value=None):
     x = np.array(u, dtype=np.float64)
-    lib().orc_fv_explicit_euler(C.byref(g), flux, _dp(_vel(velocity)), numflux, lf_lambda, _dp(x), dt, steps)
+    bk, bv = _boundary(boundary, boundary_value)
+    lib().orc_fv_explicit_euler(C.byref(g), flux, _dp(_vel(velocity)), numflux, lf_lambda, _dp(x), dt, steps, bk,
+                                bv)
     return x
 
 
-def fv_ssprk2(g, flux, numflux, u, dt, steps, velocity=None, lf_lambda=0.0):
+def fv_ssprk2(g, flux, numflux, u, dt, steps, velocity=None, lf_lambda=0.0, boundary=None, boundary_value=None):
     x = np.array(u, dtype=np.float64)
-    lib().orc_fv_ssprk2(C.byref(g), flux, _dp(_vel(velocity)), numflux, lf_lambda, _dp(x), dt, steps)
+    bk, bv = _boundary(boundary, boundary_value)
+    lib().orc_fv_ssprk2(C.byref(g), flux, _dp(_vel(velocity)), numflux, lf_lambda, _dp(x), dt, steps, bk, bv)
     return x

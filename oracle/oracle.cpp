@@ -1109,9 +1109,16 @@ double numerical_flux(int flux, const double* vel, int numflux, double lf_lambda
 }
 
 // LocalizableOperator::apply with LocalAdvectionFvCouplingOperator on inner and periodic
-// intersections, each once (operators/advection-fv.hh:77-82, local/operators/advection-fv.hh:127-153)
+// intersections, each once (operators/advection-fv.hh:77-82, local/operators/advection-fv.hh:127-153),
+// and the boundary treatments appended for the other boundary intersections
+// (operators/advection-fv.hh:95-115): by extrapolation, g = numerical flux(u, v, n) with the ghost
+// state v = u or v = value (LocalAdvectionFvBoundaryTreatmentByCustomExtrapolationOperator::apply,
+// local/operators/advection-fv.hh:411-436), or by a boundary flux g = value
+// (...ByCustomNumericalFluxOperator::apply, :279-297); range[inside] += g |I| / |E|. bkind / bval per
+// side (-x, +x, -y, +y, -z, +z), null: none. A treated direction of a periodic grid is not periodic
+// (the reference's periodicity restriction).
 void fv_apply(const Grid& g, int flux, const double* vel, int numflux, double lf_lambda, const double* u,
-              double* out) {
+              double* out, const int* bkind, const double* bval) {
   std::fill(out, out + g.nelem, 0.0);
   const double vol = g.element_volume();
   const double hinv = 1. / vol;
@@ -1123,8 +1130,27 @@ void fv_apply(const Grid& g, int flux, const double* vel, int numflux, double lf
       long cj[3] = {ci[0], ci[1], ci[2]};
       cj[k] += side ? 1 : -1;
       if (cj[k] < 0 || cj[k] >= g.n[k]) {
-        if (!g.periodic) continue;
-        cj[k] = (cj[k] + g.n[k]) % g.n[k];
+        const int kind = bkind ? bkind[f] : ORC_FV_BOUNDARY_NONE;
+        const bool treated = bkind && (bkind[2 * k] != ORC_FV_BOUNDARY_NONE || bkind[2 * k + 1] != ORC_FV_BOUNDARY_NONE);
+        if (g.periodic && !treated) {
+          cj[k] = (cj[k] + g.n[k]) % g.n[k];
+        } else {
+          if (kind == ORC_FV_BOUNDARY_NONE) continue;  // no operator on this boundary
+          double n[3] = {0, 0, 0};
+          n[k] = side ? 1.0 : -1.0;
+          double gb;
+          if (kind == ORC_FV_BOUNDARY_FLUX) {
+            gb = bval[f];
+          } else {
+            const double v = kind == ORC_FV_BOUNDARY_EXTRAPOLATE ? u[e] : bval[f];
+            gb = numerical_flux(flux, vel, numflux, lf_lambda, g.dim, u[e], v, n);
+          }
+          double h_int = 1.0;
+          for (int j = 0; j < g.dim; ++j)
+            if (j != k) h_int *= g.h[j];
+          out[e] += gb * (h_int / vol);
+          continue;
+        }
       }
       long nb = g.cell_index(cj);
       if (!(e < nb)) continue;
@@ -1172,25 +1198,26 @@ extern "C" double orc_fv_estimate_dt(const orc_grid* gd, int flux, const double*
 }
 
 extern "C" void orc_fv_apply(const orc_grid* gd, int flux, const double* vel, int numflux, double lf_lambda,
-                             const double* u, double* out) {
+                             const double* u, double* out, const int* bkind, const double* bval) {
   Grid g = make_grid(gd);
-  fv_apply(g, flux, vel, numflux, lf_lambda, u, out);
+  fv_apply(g, flux, vel, numflux, lf_lambda, u, out, bkind, bval);
 }
 
 extern "C" void orc_fv_explicit_euler(const orc_grid* gd, int flux, const double* vel, int numflux,
-                                      double lf_lambda, double* u, double dt, long steps) {
+                                      double lf_lambda, double* u, double dt, long steps, const int* bkind,
+                                      const double* bval) {
   // solve_instationary_system_explicit_euler (test/instationary-eocstudies/base.hh:428-447):
   // u_{n+1} = u_n - op.apply(u_n) * dt
   Grid g = make_grid(gd);
   std::vector<double> L(g.nelem);
   for (long s = 0; s < steps; ++s) {
-    fv_apply(g, flux, vel, numflux, lf_lambda, u, L.data());
+    fv_apply(g, flux, vel, numflux, lf_lambda, u, L.data(), bkind, bval);
     for (long i = 0; i < g.nelem; ++i) u[i] = u[i] - L[i] * dt;
   }
 }
 
 extern "C" void orc_fv_ssprk2(const orc_grid* gd, int flux, const double* vel, int numflux, double lf_lambda,
-                              double* u, double dt, long steps) {
+                              double* u, double dt, long steps, const int* bkind, const double* bval) {
   // ExplicitRungeKuttaTimeStepper::step (tools/timestepper/explicit-rungekutta.hh:237-270) with the
   // second-order SSP tableau A = {{0,0},{1,0}}, b = {1/2,1/2} (:82-97) and r = -1.
   Grid g = make_grid(gd);
@@ -1198,10 +1225,10 @@ extern "C" void orc_fv_ssprk2(const orc_grid* gd, int flux, const double* vel, i
   long N = g.nelem;
   std::vector<double> k0(N), k1(N), ui(N);
   for (long s = 0; s < steps; ++s) {
-    fv_apply(g, flux, vel, numflux, lf_lambda, u, k0.data());
+    fv_apply(g, flux, vel, numflux, lf_lambda, u, k0.data(), bkind, bval);
     const double a10 = dt * r * 1.0;
     for (long i = 0; i < N; ++i) ui[i] = u[i] + k0[i] * a10;
-    fv_apply(g, flux, vel, numflux, lf_lambda, ui.data(), k1.data());
+    fv_apply(g, flux, vel, numflux, lf_lambda, ui.data(), k1.data(), bkind, bval);
     const double bb = r * dt * 0.5;
     for (long i = 0; i < N; ++i) u[i] += k0[i] * bb;
     for (long i = 0; i < N; ++i) u[i] += k1[i] * bb;

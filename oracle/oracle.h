@@ -88,14 +88,17 @@ double orc_h1_semi_error_esv2007(const orc_grid* g, int kind, int order, const d
 /* L2 norm of a discrete function */
 double orc_l2_norm(const orc_grid* g, int kind, int order, const double* u);
 
-/* finite volumes on a structured (periodic) cube grid, m = 1 */
+/* finite volumes on a structured cube grid, m = 1; boundary treatment per side (-x, +x, -y, +y, -z,
+ * +z): bkind ORC_FV_BOUNDARY_*, bval its value; bkind null: none (periodic grids wrap) */
+enum { ORC_FV_BOUNDARY_NONE = 0, ORC_FV_BOUNDARY_EXTRAPOLATE = 1, ORC_FV_BOUNDARY_DIRICHLET = 2,
+       ORC_FV_BOUNDARY_FLUX = 3 };
 double orc_fv_estimate_dt(const orc_grid* g, int flux, const double* velocity, const double* u0);
 void orc_fv_apply(const orc_grid* g, int flux, const double* velocity, int numflux, double lf_lambda,
-                  const double* u, double* out);
+                  const double* u, double* out, const int* bkind, const double* bval);
 void orc_fv_explicit_euler(const orc_grid* g, int flux, const double* velocity, int numflux, double lf_lambda,
-                           double* u, double dt, long steps);
+                           double* u, double dt, long steps, const int* bkind, const double* bval);
 void orc_fv_ssprk2(const orc_grid* g, int flux, const double* velocity, int numflux, double lf_lambda, double* u,
-                   double dt, long steps);
+                   double dt, long steps, const int* bkind, const double* bval);
 
 #ifdef __cplusplus
 }

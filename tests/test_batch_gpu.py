@@ -76,3 +76,28 @@ def test_batch_reports_non_convergence(gdt):
     assert e.value.status == gdt._capi.ENOCONV
     its, _ = b.iterations()
     assert (its < 0).all()
+
+
+def test_batch_mixed_keeps_the_krylov_rate(gdt):
+    # one FP32 sequence with reliable updates: no restarts, so the iteration count stays near the FP64 one
+    cells = [64, 40, 24]
+    rng = np.random.default_rng(5)
+    mu = torch.tensor(rng.uniform(0.1, 10.0, (len(cells), 4)), device="cuda")
+    b = gdt.BatchedDiffusion(cells)
+    x64 = b.solve(mu, tol=1e-10, precision="fp64").cpu().numpy()
+    its64, _ = b.iterations()
+    xmx = b.solve(mu, tol=1e-10, precision="mixed").cpu().numpy()
+    itsmx, rr = b.iterations()
+    assert (itsmx > 0).all() and (rr <= 1e-10).all()
+    assert (itsmx <= 1.3 * its64 + 10).all(), (itsmx, its64)
+    assert rel_err(xmx, x64) < 1e-8
+
+
+def test_batch_mixed_reports_non_convergence(gdt):
+    b = gdt.BatchedDiffusion([16, 8])
+    mu = torch.ones(8, dtype=torch.float64, device="cuda")
+    with pytest.raises(gdt.GdtError) as e:
+        b.solve(mu, tol=1e-12, max_iter=3, precision="mixed")
+    assert e.value.status == gdt._capi.ENOCONV
+    its, rr = b.iterations()
+    assert (its < 0).all() and (rr > 1e-12).all()

@@ -157,3 +157,94 @@ def test_fv_timestep_stays_inside_its_work_buffer(gdt, oracle, dim, n, method):
     out = u.cpu().numpy().reshape(nbatch, -1)
     for b, s in enumerate(states):
         assert rel_err(out[b], step_ref(og, oracle.FLUX_BURGERS, oracle.NUMFLUX_LAX_FRIEDRICHS, s, dt, 7)) < 1e-12
+
+
+# ------------------------------------------------------------------ non-periodic boundaries ---
+# (grid periodic?, per-side treatment: None, ("extrapolate",), ("inflow", state) or ("flux", g))
+BOUNDARY_SETUPS = {
+    "walls_by_absence": (False, {}),
+    "outflow_all": (False, {s: ("extrapolate",) for s in ("-x", "+x", "-y", "+y", "-z", "+z")}),
+    "inflow_outflow_walls": (False, {"-x": ("inflow", 0.8), "+x": ("extrapolate",), "-y": ("flux", 0.0),
+                                     "+y": ("flux", 0.0), "-z": ("inflow", -0.3), "+z": ("extrapolate",)}),
+    "periodic_but_x": (True, {"-x": ("inflow", 0.6), "+x": ("flux", 0.25)}),
+}
+
+
+def _apply_setup(gdt, op, dim, setup):
+    kinds, vals = [0] * 6, [0.0] * 6
+    sides = ("-x", "+x", "-y", "+y", "-z", "+z")[: 2 * dim]
+    for side, t in setup.items():
+        if side not in sides:
+            continue
+        if t[0] == "extrapolate":
+            tr = gdt.BoundaryTreatmentByCustomExtrapolation()
+        elif t[0] == "inflow":
+            tr = gdt.BoundaryTreatmentByCustomExtrapolation(state=t[1])
+        else:
+            tr = gdt.BoundaryTreatmentByCustomNumericalFlux(t[1])
+        op.append(tr, filter=side)
+        kinds[sides.index(side)], vals[sides.index(side)] = tr.kind, tr.value
+    return kinds, vals
+
+
+BND_CASES = [(1, [37]), (2, [40, 33]), (2, [1, 9]), (3, [9, 7, 6])]
+
+
+@pytest.mark.parametrize("dim,n", BND_CASES)
+@pytest.mark.parametrize("flux,numflux", FLUXES)
+@pytest.mark.parametrize("setup", list(BOUNDARY_SETUPS))
+def test_fv_boundary_treatments_match_oracle(gdt, oracle, dim, n, flux, numflux, setup):
+    periodic, sides = BOUNDARY_SETUPS[setup]
+    g = gdt.make_cube_grid([0] * dim, [1] * dim, n, periodic=periodic)
+    og = oracle.grid(dim, n, 0.0, 1.0, periodic=periodic)
+    op, space = _op(gdt, g, flux, numflux, dim)
+    kinds, vals = _apply_setup(gdt, op, dim, sides)
+    u = _bumps(dim, n, 6) + 0.2
+    a = _orc_args(oracle, flux, numflux, dim)
+    ref = oracle.fv_apply(og, a["flux"], a["numflux"], u, velocity=a["velocity"], boundary=kinds, boundary_value=vals)
+    out = op.apply(torch.tensor(u, device="cuda")).cpu().numpy()
+    assert rel_err(out, ref) < 1e-13
+
+
+@pytest.mark.parametrize("flux,numflux", FLUXES)
+@pytest.mark.parametrize("method", ["euler", "ssp2"])
+@pytest.mark.parametrize("setup", ["inflow_outflow_walls", "periodic_but_x"])
+def test_fv_boundary_timesteppers_match_oracle(gdt, oracle, flux, numflux, method, setup):
+    dim, n = 2, [70, 45]  # tiled 2D stepper, partial tiles on both axes
+    periodic, sides = BOUNDARY_SETUPS[setup]
+    g = gdt.make_cube_grid([0, 0], [1, 1], n, periodic=periodic)
+    og = oracle.grid(dim, n, 0.0, 1.0, periodic=periodic)
+    op, space = _op(gdt, g, flux, numflux, dim)
+    kinds, vals = _apply_setup(gdt, op, dim, sides)
+    u0 = _bumps(dim, n, 11) + 0.2
+    a = _orc_args(oracle, flux, numflux, dim)
+    dt = 0.4 * oracle.fv_estimate_dt(og, a["flux"], u0, velocity=a["velocity"])
+    ut = torch.tensor(np.concatenate([u0, u0[::-1].copy()]), device="cuda")  # a batch of two states
+    gdt.ExplicitRungeKuttaTimeStepper(op, ut, method=method).step(dt, 20)
+    run = oracle.fv_explicit_euler if method == "euler" else oracle.fv_ssprk2
+    out = ut.cpu().numpy().reshape(2, -1)
+    for b, s in enumerate([u0, u0[::-1].copy()]):
+        ref = run(og, a["flux"], a["numflux"], s, dt, 20, velocity=a["velocity"], boundary=kinds, boundary_value=vals)
+        assert rel_err(out[b], ref) < 1e-12
+
+
+def test_fv_impermeable_walls_conserve_mass(gdt):
+    n = [96, 80]
+    g = gdt.make_cube_grid([0, 0], [1, 1], n)
+    op, space = _op(gdt, g, "burgers", "lf", 2)
+    op.append(gdt.BoundaryTreatmentByCustomNumericalFlux(0.0))
+    u0 = torch.tensor(_bumps(2, n, 3), device="cuda")
+    ut = u0.clone()
+    dt = 0.4 * gdt.estimate_dt_for_hyperbolic_system(g, ut, op)
+    gdt.ExplicitRungeKuttaTimeStepper(op, ut, method="ssp2").step(dt, 50)
+    assert abs(float(ut.sum() - u0.sum())) <= 1e-12 * float(u0.abs().sum())
+    assert float((ut - u0).abs().max()) > 1e-3  # the state did move
+
+
+def test_fv_boundary_treatment_rejects_half_periodic_directions(gdt):
+    g = gdt.make_cube_grid([0, 0], [1, 1], [8, 8], periodic=True)
+    op, space = _op(gdt, g, "burgers", "lf", 2)
+    op.append(gdt.BoundaryTreatmentByCustomExtrapolation(), filter="-x")
+    with pytest.raises(gdt.GdtError) as e:
+        op.apply(torch.zeros(64, dtype=torch.float64, device="cuda"))
+    assert e.value.status == gdt._capi.EINVAL
