@@ -38,18 +38,24 @@ __global__ void __launch_bounds__(TH) k_spmv(int n, const int* __restrict__ rp, 
                                             unsigned int* ticket) {
   if (stopped(st)) return;
   T a0 = T(0), a1 = T(0);
-  for_rows_csr<G, PL, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
-    if (leader) {
-      y[row] = s;
-      if (MODE == 1) a0 = fma(x[row], s, a0);
-      if (MODE == 2) a0 = fma(w[row], s, a0);
-      if (MODE == 3) {
-        a0 = fma(s, w[row], a0);
-        a1 = fma(s, s, a1);
+  if constexpr (MODE == 0) {
+    for_rows_csr<G, PL, T>(n, rp, col, val, x, [&](int row, bool leader, T s) {
+      if (leader) y[row] = s;
+    });
+    return;
+  } else {
+    // the dot partner of row `row` (x for CG's p.Ap, w otherwise) is prefetched with the row bounds
+    for_rows_csr_w<G, PL, T>(n, rp, col, val, x, MODE == 1 ? x : w, [&](int row, bool leader, T s, T wr) {
+      if (leader) {
+        y[row] = s;
+        if (MODE == 1 || MODE == 2) a0 = fma(wr, s, a0);
+        if (MODE == 3) {
+          a0 = fma(s, wr, a0);
+          a1 = fma(s, s, a1);
+        }
       }
-    }
-  });
-  if (MODE == 0) return;
+    });
+  }
   double v[2] = {double(a0), double(a1)};
   if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
     if (MODE == 1) {

@@ -26,20 +26,32 @@ __device__ __forceinline__ T csr_row(int beg, int end, int lane, const int* __re
   return s;
 }
 
+// calls body(row, active, s) or, with a prefetched per-row value, body(row, active, s, w[row])
+template <bool HASW, class T, class Body>
+__device__ __forceinline__ void row_body(Body& body, int row, bool active, T s, T wr) {
+  if constexpr (HASW) body(row, active, s, wr);
+  else body(row, active, s);
+}
+
 // Warp-uniform loop over the rows of a CSR matrix, G lanes per row: the loop bound depends only on
 // the block, so whole warps iterate together and every lane reaches the shuffles of csr_row.
-// body(row, active, s) runs in every lane; `active` is false for lanes past the last row.
-template <int G, class T, class Body>
+// body(row, active, s) runs in every lane; `active` is false for lanes past the last row. With HASW
+// the value w[row] (a vector the body combines with the row result, e.g. for a fused dot product) is
+// loaded together with the row bounds, before the row's gathers, and passed as a fourth argument:
+// loading it after the row reduction would add one dependent memory latency to every row.
+template <int G, class T, bool HASW = false, class Body>
 __device__ __forceinline__ void for_rows(int n, const int* __restrict__ rp, const int* __restrict__ col,
-                                         const T* __restrict__ val, const T* __restrict__ x, Body body) {
+                                         const T* __restrict__ val, const T* __restrict__ x, Body body,
+                                         const T* __restrict__ w = nullptr) {
   const int lane = threadIdx.x & (G - 1);
   const int rpb = blockDim.x / G;
   for (int row0 = blockIdx.x * rpb; row0 < n; row0 += gridDim.x * rpb) {
     const int row = row0 + threadIdx.x / G;
     const bool active = row < n;
     const int beg = active ? rp[row] : 0, end = active ? rp[row + 1] : 0;
+    const T wr = (HASW && active && lane == 0) ? w[row] : T(0);
     const T s = csr_row<G, T>(beg, end, lane, col, val, x);
-    body(row, active && lane == 0, s);
+    row_body<HASW>(body, row, active && lane == 0, s, wr);
   }
 }
 
@@ -50,9 +62,10 @@ extern __shared__ __align__(16) unsigned char gdt_dyn_smem[];
 // registers, then stores them to the warp's shared-memory window, so a lane has up to 2 PL loads in
 // flight. Lane i then reduces row r0 + i from the window, unrolled over PL with two accumulators so
 // the x gathers are independent. PL >= longest row. body(row, active, s) runs in every lane.
-template <class T, int PL, class Body>
+template <class T, int PL, bool HASW = false, class Body>
 __device__ __forceinline__ void for_rows_pipelined(int n, const int* __restrict__ rp, const int* __restrict__ col,
-                                                   const T* __restrict__ val, const T* __restrict__ x, Body body) {
+                                                   const T* __restrict__ val, const T* __restrict__ x, Body body,
+                                                   const T* __restrict__ w = nullptr) {
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   constexpr int cap = 32 * PL;
@@ -63,6 +76,7 @@ __device__ __forceinline__ void for_rows_pipelined(int n, const int* __restrict_
     const bool active = row < n;
     const int rbeg = active ? rp[row] : 0;
     const int rend = active ? rp[row + 1] : 0;
+    const T wr = (HASW && active) ? w[row] : T(0);
     const int last = (n - 1 - r0) < 31 ? (n - 1 - r0) : 31;
     const int beg = __shfl_sync(0xffffffffu, rbeg, 0);
     const int end = __shfl_sync(0xffffffffu, rend, last);
@@ -93,7 +107,7 @@ __device__ __forceinline__ void for_rows_pipelined(int n, const int* __restrict_
       if (j < len) s0 = fma(wv[a + j], x[wc[a + j]], s0);
       if (j + 1 < len) s1 = fma(wv[a + j + 1], x[wc[a + j + 1]], s1);
     }
-    body(row, active, s0 + s1);
+    row_body<HASW>(body, row, active, s0 + s1, wr);
     __syncwarp();
   }
 }
@@ -128,9 +142,10 @@ struct AsyncWindow {
   static constexpr size_t bytes_per_warp = 2 * (VCAP * sizeof(T) + CCAP * sizeof(int));
 };
 
-template <class T, int CAP, class Body>
+template <class T, int CAP, bool HASW = false, class Body>
 __device__ __forceinline__ void for_rows_async(int n, const int* __restrict__ rp, const int* __restrict__ col,
-                                               const T* __restrict__ val, const T* __restrict__ x, Body body) {
+                                               const T* __restrict__ val, const T* __restrict__ x, Body body,
+                                               const T* __restrict__ w = nullptr) {
   using W = AsyncWindow<T, CAP>;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
@@ -170,9 +185,10 @@ __device__ __forceinline__ void for_rows_async(int n, const int* __restrict__ rp
     } else {
       cp_async_wait<0>();
     }
-    __syncwarp();
     const int row = r0 + lane;
     const bool active = row < n;
+    const T wr = (HASW && active) ? w[row] : T(0);
+    __syncwarp();
     const T* wv = vbuf(cur) + (rb - vb);
     const int* wc = cbuf(cur) + (rb - cb);
     const int len = re - rb;
@@ -182,7 +198,7 @@ __device__ __forceinline__ void for_rows_async(int n, const int* __restrict__ rp
       if (j < len) s0 = fma(wv[j], __ldg(x + wc[j]), s0);
       if (j + 1 < len) s1 = fma(wv[j + 1], __ldg(x + wc[j + 1]), s1);
     }
-    body(row, active, s0 + s1);
+    row_body<HASW>(body, row, active, s0 + s1, wr);
     __syncwarp();  // the buffer just read is refilled by the next stage
     rb = rb2, re = re2, vb = vb2, cb = cb2;
   }
@@ -197,6 +213,16 @@ __device__ __forceinline__ void for_rows_csr(int n, const int* __restrict__ rp, 
   if constexpr (PL > 0) for_rows_pipelined<T, PL>(n, rp, col, val, x, body);
   else if constexpr (PL < 0) for_rows_async<T, -PL>(n, rp, col, val, x, body);
   else for_rows<G, T>(n, rp, col, val, x, body);
+}
+
+// the same with w[row] prefetched and passed to body(row, active, s, w[row])
+template <int G, int PL, class T, class Body>
+__device__ __forceinline__ void for_rows_csr_w(int n, const int* __restrict__ rp, const int* __restrict__ col,
+                                               const T* __restrict__ val, const T* __restrict__ x,
+                                               const T* __restrict__ w, Body body) {
+  if constexpr (PL > 0) for_rows_pipelined<T, PL, true>(n, rp, col, val, x, body, w);
+  else if constexpr (PL < 0) for_rows_async<T, -PL, true>(n, rp, col, val, x, body, w);
+  else for_rows<G, T, true>(n, rp, col, val, x, body, w);
 }
 
 // the schedule table: index -> (G, PL)

@@ -17,7 +17,9 @@
 // the iterated residual has dropped by 10x since the last update (or reached the tolerance), the
 // correction is added to the FP64 solution, the true residual r = b - A x is recomputed from the FP64
 // CSR matrix and replaces the FP32 residual, and beta is recomputed from it. Convergence is decided
-// only on the true FP64 residual.
+// only on the true FP64 residual. A solve whose true residual stops following (less than 2x gained over
+// a cycle) falls back to restarted iterative refinement: direction reset at every replacement, which
+// then waits for a 1000x drop.
 #include <cudaTypedefs.h>
 
 #include <cmath>
@@ -38,7 +40,9 @@ constexpr int MAXU = 13;  // upper slots of the 27-point stencil
 
 struct MState {
   double rho, rho_prev, alpha, beta, rr, rr0, rr_ref, tol2;
+  double drop;  // replacement when the iterated residual (squared) has dropped by this factor
   int iter, max_iter, converged, flag, breakdown, updates;
+  int restarting;  // stagnation guard tripped: every replacement restarts the direction
   int fault;  // a bounded device wait ran out (tile loads of the 3D SpMV)
 };
 
@@ -309,7 +313,7 @@ __global__ void __launch_bounds__(TH) k_mx_update(int n, float* __restrict__ x32
     st->rho = v[0];
     st->rr = v[1];
     st->iter += 1;
-    st->flag = (v[1] <= 0.01 * st->rr_ref || v[1] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) ? 1 : 0;
+    st->flag = (v[1] <= st->drop * st->rr_ref || v[1] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) ? 1 : 0;
     if (!isfinite(v[1])) {
       st->breakdown = 1;
       st->converged = 1;
@@ -350,9 +354,17 @@ __global__ void __launch_bounds__(TH) k_mx_true_residual(int n, Pitch pt, const 
   });
   double v[2] = {a0, a1};
   if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
+    // stagnation guard: a cycle that gained less than 2x on the true residual means the FP32 operator
+    // is too far from the FP64 one (cond(A) times its rounding near 1) for the sequence to continue;
+    // from then on each replacement restarts the direction and waits for a 1000x drop (restarted
+    // FP64 iterative refinement around FP32 CG)
+    if (!st->restarting && v[1] > 0.25 * st->rr_ref) {
+      st->restarting = 1;
+      st->drop = 1e-6;
+    }
     st->rr_ref = v[1];
     st->rr = v[1];
-    st->beta = v[0] / st->rho_prev;
+    st->beta = st->restarting ? 0.0 : v[0] / st->rho_prev;
     st->rho = v[0];
     st->flag = 0;
     st->updates += 1;
@@ -407,6 +419,8 @@ __global__ void __launch_bounds__(TH) k_mx_init(int n, Pitch pt, const int* __re
     st->rho = v[0];
     st->rho_prev = v[0];
     st->rr = st->rr0 = st->rr_ref = v[1];
+    st->drop = 0.01;
+    st->restarting = 0;
     st->iter = 0;
     st->flag = 0;
     st->updates = 0;
