@@ -74,6 +74,8 @@ struct gdt_matrix_s {
   int max_row = 0;     // longest row
   int spmv_sched = 1;  // SpMV schedule (see linalg.cuh), picked by tune_spmv on first use
   int tuned = 0;
+  int pinned = 0;      // schedule set by gdt_matrix_set_schedule: no autotuning
+  int cg_sched = -1;   // schedule of the fused FP64 CG iteration, timed inside that iteration (krylov.cu)
   int mx_tiled = -1;   // mixed solver, 3D grids: plane-tiled (1) or linear (0) FP32 stencil SpMV, timed on first use
   void* ho = nullptr;  // element-batched assembly data (order-2 spaces), owned (highorder.cu)
 };

@@ -10,6 +10,7 @@
 // per chunk, and kernels of iterations past convergence return immediately.
 // Mixed precision: FP32 inner CG (FP32 CSR values, FP32 vectors, FP32 Jacobi) inside FP64
 // iterative refinement with an FP64 residual r = b - A x from the FP64 matrix.
+#include <cfloat>
 #include <cmath>
 #include <vector>
 
@@ -167,6 +168,69 @@ __global__ void __launch_bounds__(TH) k_cg_update_jacobi(int n, TX* __restrict__
       st->converged = 1;
     }
   }
+}
+
+// The same two FP64 kernels on pairs of rows (16-byte loads and stores, twice the bytes in flight
+// per instruction); for vectors that all start on a 16-byte boundary. The odd last row, if any, is
+// done by the first thread of the grid.
+__global__ void __launch_bounds__(TH) k_cg_update_jacobi2(int n, double* __restrict__ x, const double* __restrict__ p,
+                                                         double* __restrict__ r, const double* __restrict__ q,
+                                                         const double* __restrict__ dinv, KState* st,
+                                                         double* partials, unsigned int* ticket) {
+  if (stopped(st)) return;
+  const double alpha = st->alpha;
+  double a0 = 0.0, a1 = 0.0;
+  const int n2 = n >> 1;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
+    double2 xv = reinterpret_cast<const double2*>(x)[k], rv = reinterpret_cast<const double2*>(r)[k];
+    const double2 pv = reinterpret_cast<const double2*>(p)[k], qv = reinterpret_cast<const double2*>(q)[k],
+                  dv = reinterpret_cast<const double2*>(dinv)[k];
+    xv.x = fma(alpha, pv.x, xv.x);
+    xv.y = fma(alpha, pv.y, xv.y);
+    rv.x = fma(-alpha, qv.x, rv.x);
+    rv.y = fma(-alpha, qv.y, rv.y);
+    a0 = fma(rv.x, dv.x * rv.x, a0);
+    a1 = fma(rv.x, rv.x, a1);
+    a0 = fma(rv.y, dv.y * rv.y, a0);
+    a1 = fma(rv.y, rv.y, a1);
+    reinterpret_cast<double2*>(x)[k] = xv;
+    reinterpret_cast<double2*>(r)[k] = rv;
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const int i = n - 1;
+    x[i] = fma(alpha, p[i], x[i]);
+    const double ri = fma(-alpha, q[i], r[i]);
+    r[i] = ri;
+    a0 = fma(ri, dinv[i] * ri, a0);
+    a1 = fma(ri, ri, a1);
+  }
+  double v[2] = {a0, a1};
+  if (grid_reduce<2>(v, partials, ticket) && threadIdx.x == 0) {
+    st->beta = v[0] / st->rho;
+    st->rho = v[0];
+    st->rr = v[1];
+    st->iter += 1;
+    if (v[1] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) st->converged = 1;
+    if (!isfinite(v[1])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TH) k_cg_p_jacobi2(int n, double* __restrict__ p, const double* __restrict__ r,
+                                                    const double* __restrict__ dinv, const KState* st) {
+  if (stopped(st)) return;
+  const double beta = st->beta;
+  const int n2 = n >> 1;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
+    double2 pv = reinterpret_cast<const double2*>(p)[k];
+    const double2 rv = reinterpret_cast<const double2*>(r)[k], dv = reinterpret_cast<const double2*>(dinv)[k];
+    pv.x = fma(beta, pv.x, dv.x * rv.x);
+    pv.y = fma(beta, pv.y, dv.y * rv.y);
+    reinterpret_cast<double2*>(p)[k] = pv;
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) p[n - 1] = fma(beta, p[n - 1], dinv[n - 1] * r[n - 1]);
 }
 
 template <class T>
@@ -539,6 +603,91 @@ void ilu_apply(gdt_context ctx, gdt_matrix m, const Ilu& f, const double* r, dou
 
 }  // namespace
 
+__global__ void k_fill(int n, double* __restrict__ v, double value) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = value;
+}
+__global__ void k_probe(int n, double* __restrict__ a, double* __restrict__ b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    a[i] = b[i] = 1.0 + 0.001 * double(i % 997);
+}
+
+// Picks the SpMV schedule of the fused FP64 CG iteration by timing each valid schedule inside that
+// iteration (SpMV + update + direction on scratch vectors, a few real CG steps on A x = probe), not
+// back to back: inside the loop the SpMV starts with the vectors the other two kernels just wrote
+// dirty in L2, and the schedules rank differently there (128^3 Q1: the staged cp.async schedule
+// wins in the loop while 4-lane vector CSR wins back to back). Once per matrix; temporary memory of
+// 5 n doubles.
+gdt_status tune_cg(gdt_context ctx, gdt_matrix m, const Launch& L0, cudaStream_t s) {
+  if (m->cg_sched >= 0) return GDT_OK;
+  if (m->pinned) {
+    m->cg_sched = m->spmv_sched;
+    return GDT_OK;
+  }
+  const int n = int(m->rows);
+  const size_t vb = sizeof(double) * std::max(n, 1);
+  double *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *d = nullptr;
+  KState* st = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&x, vb, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&r, vb, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&p, vb, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&q, vb, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&d, vb, s));
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&st, sizeof(KState), s));
+  const int pair_blocks = std::max(1, std::min(grid_blocks((n + 1) / 2, TH), ctx->num_sms * 8));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int timing = ctx->timing;
+  ctx->timing = 0;
+  float best = FLT_MAX;
+  int best_sched = m->spmv_sched;
+  for (int sched = 0; sched < kSchedules; ++sched) {
+    if (!schedule_valid(sched, m->max_row)) continue;
+    Launch L = L0;
+    L.sched = sched;
+    KState init{};
+    init.rho = 1.0;
+    init.rr0 = 1.0;
+    init.max_iter = 1 << 30;
+    cudaMemcpyAsync(st, &init, sizeof(KState), cudaMemcpyHostToDevice, s);
+    k_fill<<<L.vec_blocks, TH, 0, s>>>(n, x, 0.0);
+    k_fill<<<L.vec_blocks, TH, 0, s>>>(n, d, 1.0);
+    k_probe<<<L.vec_blocks, TH, 0, s>>>(n, r, p);
+    float total = 0.f;
+    bool ok = true;
+    for (int it = 0; it < 5; ++it) {
+      cudaEventRecord(e0, s);
+      spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
+      cudaEventRecord(e1, s);
+      k_cg_update_jacobi2<<<pair_blocks, TH, 0, s>>>(n, x, p, r, q, d, st, L.partials, L.ticket);
+      k_cg_p_jacobi2<<<pair_blocks, TH, 0, s>>>(n, p, r, d, st);
+      if (it >= 2) {
+        float ms = 0.f;
+        ok = ok && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+        total += ms;
+      }
+    }
+    ok = ok && cudaGetLastError() == cudaSuccess;
+    ctx->launches += 18;
+    if (ok && total < best) {
+      best = total;
+      best_sched = sched;
+    }
+  }
+  ctx->timing = timing;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(x, s);
+  cudaFreeAsync(r, s);
+  cudaFreeAsync(p, s);
+  cudaFreeAsync(q, s);
+  cudaFreeAsync(d, s);
+  cudaFreeAsync(st, s);
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+  m->cg_sched = best_sched;
+  return GDT_OK;
+}
+
 gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
                  gdt_solve_info* info) {
   cudaStream_t s = ctx->stream;
@@ -627,14 +776,27 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
           GDT_TRY_CUDA(ctx, cudaMemcpyAsync(one, ones.data(), vb, cudaMemcpyHostToDevice, s));
           GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
         }
+        GDT_CHECK(ctx, tune_cg(ctx, m, L, s));
+        L.sched = m->cg_sched;
         residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
+        // pairs of rows per thread when every vector is 16-byte aligned (the solver's own are; x is
+        // the caller's)
+        const bool pairs = (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
+        const int pair_blocks = std::max(1, std::min(grid_blocks((n + 1) / 2, TH), ctx->num_sms * 8));
         GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
           spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
           timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);
-          k_cg_update_jacobi<double, double><<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);
+          if (pairs)
+            k_cg_update_jacobi2<<<pair_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);
+          else
+            k_cg_update_jacobi<double, double><<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials,
+                                                                           L.ticket);
           timing_end(ctx, s);
           timing_begin(ctx, s, GDT_TIMING_CG_DIRECTION);
-          k_cg_p_jacobi<double><<<L.vec_blocks, TH, 0, s>>>(n, p, r, one, st);
+          if (pairs)
+            k_cg_p_jacobi2<<<pair_blocks, TH, 0, s>>>(n, p, r, one, st);
+          else
+            k_cg_p_jacobi<double><<<L.vec_blocks, TH, 0, s>>>(n, p, r, one, st);
           timing_end(ctx, s);
           ctx->launches += 2;
         }));

@@ -95,6 +95,8 @@ gdt_status spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y) {
 extern "C" gdt_status gdt_matrix_tune(gdt_context ctx, gdt_matrix m, int* schedule, double* times_ms) {
   if (!ctx || !m) return GDT_EINVAL;
   m->tuned = 0;
+  m->pinned = 0;
+  m->cg_sched = -1;
   GDT_CHECK(ctx, gdt::tune_spmv(ctx, m, times_ms));
   if (schedule) *schedule = m->spmv_sched;
   return GDT_OK;
@@ -106,5 +108,7 @@ extern "C" gdt_status gdt_matrix_set_schedule(gdt_matrix m, int schedule) {
     return GDT_EINVAL;
   m->spmv_sched = schedule;
   m->tuned = 1;
+  m->pinned = 1;
+  m->cg_sched = schedule;
   return GDT_OK;
 }
