@@ -31,7 +31,14 @@ struct FvParams {
   double lf_inv_lambda;  // 0: local LF; else the reference's fixed lambda_ (coefficient 0.5 / lambda_)
   int bkind[6];          // per side (-x, +x, -y, +y, -z, +z): GDT_FV_BOUNDARY_*, or -1 for a periodic side
   double bval[6];
+  // the tiled kernels' form of the flux, 4 g (see face_flux4)
+  int form4;             // FORM4_*
+  double lam2;           // Burgers LF: 2 lambda_ for a fixed lambda_, 0 for the local one
+  double tu[3], tv[3];   // linear transport: 4 g = tu u + tv v (EO: each term only for a positive state)
 };
+
+enum { FORM4_GENERIC = 0, FORM4_BURGERS_LF = 1, FORM4_TRANSPORT_LINEAR = 2, FORM4_BURGERS_EO = 3,
+       FORM4_TRANSPORT_EO = 4, FORM4_BURGERS_UPWIND = 5, FORM4_BURGERS_LF_FIXED = 6 };
 
 __device__ __forceinline__ double f_of(const FvParams& p, double u, int d) {
   return p.flux == GDT_FLUX_BURGERS ? 0.5 * u * u : p.vel[d] * u;
@@ -92,6 +99,40 @@ __device__ __forceinline__ double boundary_flux(const FvParams& p, int dim, int 
 __device__ __forceinline__ double boundary_face_flux(const FvParams& p, int dim, int k, bool upper, double u) {
   const double g = boundary_flux(p, dim, 2 * k + (upper ? 1 : 0), u);
   return upper ? g : -g;
+}
+
+// 4 g(u, v, +e_k), the numerical flux in a form with fewer FP64 instructions (GB300's FP64 pipe
+// bounds the FV update): the factors 1/2 of the flux formulas move into the 1/4 of the update
+// coefficients (scaling by powers of two is exact), the transport fluxes collapse to precomputed
+// linear combinations, and max(|u|, |v|) and the sign tests run on the integer bit patterns (for
+// non-negative doubles the integer order is the floating-point order). Equal to 4 face_flux() up
+// to the rounding of the rearranged sums.
+__device__ __forceinline__ bool positive(double u) { return __double_as_longlong(u) > 0; }
+__device__ __forceinline__ double abs_max(double u, double v) {
+  const long long a = __double_as_longlong(u) & 0x7fffffffffffffffLL, b = __double_as_longlong(v) & 0x7fffffffffffffffLL;
+  return __longlong_as_double(a > b ? a : b);
+}
+
+template <int FORM>
+__device__ __forceinline__ double face_flux4(const FvParams& p, int k, double u, double v) {
+  if constexpr (FORM == FORM4_BURGERS_LF) {  // 2 (f(u) + f(v)) + 2 lambda (u - v), f(u) = u^2 / 2
+    const double lam = abs_max(u, v);
+    return fma(lam + lam, u - v, fma(u, u, v * v));
+  } else if constexpr (FORM == FORM4_BURGERS_LF_FIXED) {
+    return fma(p.lam2, u - v, fma(u, u, v * v));
+  } else if constexpr (FORM == FORM4_TRANSPORT_LINEAR) {
+    return fma(p.tu[k], u, p.tv[k] * v);
+  } else if constexpr (FORM == FORM4_BURGERS_EO) {  // 4 * (u > 0 ? u^2 / 2 : 0)
+    return positive(u) ? (u + u) * u : 0.0;
+  } else if constexpr (FORM == FORM4_TRANSPORT_EO) {
+    return (positive(u) ? p.tu[k] * u : 0.0) + (positive(v) ? p.tv[k] * v : 0.0);
+  } else if constexpr (FORM == FORM4_BURGERS_UPWIND) {  // f'((u + v) / 2) > 0 ? 4 f(u) : 4 f(v)
+    const double w = (u + v) * 0.5;
+    const double sel = positive(w) ? u : v;
+    return (sel + sel) * sel;
+  } else {
+    return 4.0 * face_flux(p, 2, k, u, v);
+  }
 }
 
 // ------------------------------------------------------------------------- generic (any dim) ---
@@ -155,8 +196,9 @@ constexpr int TX = 32, TY = 32, BY = 8;  // tile TX x TY cells, block TX x BY th
 
 // STAGE 0: k = L(u) ; STAGE 1 (Euler): u_next = u - dt L(u) ;
 // STAGE 2: u1 = u - dt k0 on the tile + halo, u_next = u + (-dt/2) (k0 + L(u1))
-// BND: some side has a boundary treatment; the faces on those sides are then replaced by it
-template <int STAGE, bool BND>
+// BND: some side has a boundary treatment; the faces on those sides are then replaced by it. FORM:
+// the numerical flux (FORM4_*), a template parameter so that each flux is straight-line code
+template <int STAGE, bool BND, int FORM>
 __global__ void __launch_bounds__(TX* BY) fv2d_tile(GridDesc g, FvParams p, const double* __restrict__ u,
                                                     const double* __restrict__ k0, double* __restrict__ out,
                                                     double dt, double cx, double cy) {
@@ -167,42 +209,44 @@ __global__ void __launch_bounds__(TX* BY) fv2d_tile(GridDesc g, FvParams p, cons
   const long long off = (long long)blockIdx.z * nx * ny;
   const long long x0 = (long long)blockIdx.x * TX, y0 = (long long)blockIdx.y * TY;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  // stage tile + halo (periodic)
+  // stage tile + halo (periodic wrap by compare and select: a 64-bit modulo would cost more FP64-pipe
+  // time than the flux arithmetic)
   for (int j = ty; j < TY + 2; j += BY)
     for (int i = tx; i < TX + 2; i += TX) {
-      long long gxi = (x0 + i - 1 + nx) % nx, gyj = (y0 + j - 1 + ny) % ny;
-      if (x0 + i - 1 > nx) gxi = nx - 1;  // beyond a partial tile: clamp (values unused)
-      if (y0 + j - 1 > ny) gyj = ny - 1;
+      long long gxi = x0 + i - 1, gyj = y0 + j - 1;
+      gxi = gxi < 0 ? nx - 1 : (gxi == nx ? 0 : (gxi > nx ? nx - 1 : gxi));  // beyond a partial tile: unused
+      gyj = gyj < 0 ? ny - 1 : (gyj == ny ? 0 : (gyj > ny ? ny - 1 : gyj));
       const long long cidx = off + gyj * nx + gxi;
       double v = u[cidx];
       if (STAGE == 2) v = fma(k0[cidx], -dt, v);
       s[j][i] = v;
     }
   __syncthreads();
-  // x faces: between tile columns i-1 and i (i = 0..TX), rows 0..TY-1
+  // x faces: between tile columns i-1 and i (i = 0..TX), rows 0..TY-1; fluxes kept as 4 g
   for (int j = ty; j < TY; j += BY)
     for (int i = tx; i <= TX; i += TX) {
       double f;
-      if (BND && p.bkind[0] >= 0 && x0 + i == 0) f = boundary_face_flux(p, 2, 0, false, s[j + 1][i + 1]);
-      else if (BND && p.bkind[0] >= 0 && x0 + i == nx) f = boundary_face_flux(p, 2, 0, true, s[j + 1][i]);
-      else f = face_flux(p, 2, 0, s[j + 1][i], s[j + 1][i + 1]);
+      if (BND && p.bkind[0] >= 0 && x0 + i == 0) f = 4.0 * boundary_face_flux(p, 2, 0, false, s[j + 1][i + 1]);
+      else if (BND && p.bkind[0] >= 0 && x0 + i == nx) f = 4.0 * boundary_face_flux(p, 2, 0, true, s[j + 1][i]);
+      else f = face_flux4<FORM>(p, 0, s[j + 1][i], s[j + 1][i + 1]);
       gx[j][i] = f;
     }
   // y faces: between tile rows j-1 and j (j = 0..TY)
   for (int j = ty; j <= TY; j += BY) {
     double f;
-    if (BND && p.bkind[2] >= 0 && y0 + j == 0) f = boundary_face_flux(p, 2, 1, false, s[j + 1][tx + 1]);
-    else if (BND && p.bkind[2] >= 0 && y0 + j == ny) f = boundary_face_flux(p, 2, 1, true, s[j][tx + 1]);
-    else f = face_flux(p, 2, 1, s[j][tx + 1], s[j + 1][tx + 1]);
+    if (BND && p.bkind[2] >= 0 && y0 + j == 0) f = 4.0 * boundary_face_flux(p, 2, 1, false, s[j + 1][tx + 1]);
+    else if (BND && p.bkind[2] >= 0 && y0 + j == ny) f = 4.0 * boundary_face_flux(p, 2, 1, true, s[j][tx + 1]);
+    else f = face_flux4<FORM>(p, 1, s[j][tx + 1], s[j + 1][tx + 1]);
     gy[j][tx] = f;
   }
   __syncthreads();
   const long long gxi = x0 + tx;
   if (gxi >= nx) return;
+  const double cx4 = 0.25 * cx, cy4 = 0.25 * cy;
   for (int j = ty; j < TY; j += BY) {
     const long long gyj = y0 + j;
     if (gyj >= ny) break;
-    const double L = cx * (gx[j][tx + 1] - gx[j][tx]) + cy * (gy[j + 1][tx] - gy[j][tx]);
+    const double L = fma(cx4, gx[j][tx + 1] - gx[j][tx], cy4 * (gy[j + 1][tx] - gy[j][tx]));
     const long long cidx = off + gyj * nx + gxi;
     if (STAGE == 0) out[cidx] = L;
     else if (STAGE == 1) out[cidx] = fma(-dt, L, u[cidx]);
@@ -216,6 +260,37 @@ FvParams make_params(const GridDesc& g, const gdt_fv_desc* d) {
   p.numflux = d->numflux;
   for (int i = 0; i < 3; ++i) p.vel[i] = d->velocity[i];
   p.lf_inv_lambda = d->lf_lambda;
+  p.form4 = FORM4_GENERIC;
+  p.lam2 = 0.0;
+  for (int k = 0; k < 3; ++k) p.tu[k] = p.tv[k] = 0.0;
+  if (d->flux == GDT_FLUX_BURGERS) {
+    if (d->numflux == GDT_NUMFLUX_LAX_FRIEDRICHS) {
+      p.form4 = d->lf_lambda != 0.0 ? FORM4_BURGERS_LF_FIXED : FORM4_BURGERS_LF;
+      p.lam2 = d->lf_lambda != 0.0 ? 2.0 / d->lf_lambda : 0.0;
+    } else if (d->numflux == GDT_NUMFLUX_ENGQUIST_OSHER) {
+      p.form4 = FORM4_BURGERS_EO;
+    } else {
+      p.form4 = FORM4_BURGERS_UPWIND;
+    }
+  } else {
+    double lam = 0.0;
+    for (int k = 0; k < g.dim; ++k) lam = std::max(lam, std::fabs(d->velocity[k]));
+    if (d->lf_lambda != 0.0) lam = 1.0 / d->lf_lambda;
+    p.form4 = d->numflux == GDT_NUMFLUX_ENGQUIST_OSHER ? FORM4_TRANSPORT_EO : FORM4_TRANSPORT_LINEAR;
+    for (int k = 0; k < 3; ++k) {
+      const double a = d->velocity[k];
+      if (d->numflux == GDT_NUMFLUX_LAX_FRIEDRICHS) {  // 2 (a (u + v) + lambda (u - v))
+        p.tu[k] = 2.0 * (a + lam);
+        p.tv[k] = 2.0 * (a - lam);
+      } else if (d->numflux == GDT_NUMFLUX_UPWIND) {  // 4 a u if a > 0 else 4 a v
+        p.tu[k] = a > 0.0 ? 4.0 * a : 0.0;
+        p.tv[k] = a > 0.0 ? 0.0 : 4.0 * a;
+      } else {  // EO: 4 (u max(a, 0) + v min(a, 0)), each for a positive state
+        p.tu[k] = 4.0 * std::max(a, 0.0);
+        p.tv[k] = 4.0 * std::min(a, 0.0);
+      }
+    }
+  }
   for (int side = 0; side < 6; ++side) {
     // a side is periodic when the grid is and no treatment is given; otherwise the treatment (or none)
     const bool periodic = g.periodic && d->boundary[side] == GDT_FV_BOUNDARY_NONE;
@@ -231,6 +306,37 @@ bool has_boundary(const FvParams& p, int dim) {
   return false;
 }
 
+template <int STAGE, bool BND>
+void launch_tile_b(dim3 grid, cudaStream_t s, const GridDesc& g, const FvParams& p, const double* u, const double* k0,
+                   double* out, double dt, double cx, double cy) {
+  const dim3 block(TX, BY);
+  switch (p.form4) {
+    case FORM4_BURGERS_LF: fv2d_tile<STAGE, BND, FORM4_BURGERS_LF><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy); break;
+    case FORM4_BURGERS_LF_FIXED:
+      fv2d_tile<STAGE, BND, FORM4_BURGERS_LF_FIXED><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      break;
+    case FORM4_TRANSPORT_LINEAR:
+      fv2d_tile<STAGE, BND, FORM4_TRANSPORT_LINEAR><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      break;
+    case FORM4_BURGERS_EO: fv2d_tile<STAGE, BND, FORM4_BURGERS_EO><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy); break;
+    case FORM4_TRANSPORT_EO:
+      fv2d_tile<STAGE, BND, FORM4_TRANSPORT_EO><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      break;
+    case FORM4_BURGERS_UPWIND:
+      fv2d_tile<STAGE, BND, FORM4_BURGERS_UPWIND><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      break;
+    default: fv2d_tile<STAGE, BND, FORM4_GENERIC><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy); break;
+  }
+}
+
+// one stage of the tiled 2D kernel, instantiated for the flux form and the boundary case
+template <int STAGE>
+void launch_tile(bool bnd, dim3 grid, cudaStream_t s, const GridDesc& g, const FvParams& p, const double* u,
+                 const double* k0, double* out, double dt, double cx, double cy) {
+  if (bnd) launch_tile_b<STAGE, true>(grid, s, g, p, u, k0, out, dt, cx, cy);
+  else launch_tile_b<STAGE, false>(grid, s, g, p, u, k0, out, dt, cx, cy);
+}
+
 bool tiled_ok(const GridDesc& g) { return g.dim == 2 && g.n[0] >= 2 && g.n[1] >= 2; }
 
 }  // namespace
@@ -240,10 +346,7 @@ gdt_status fv_apply(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc* d
   FvParams p = make_params(g, d);
   if (tiled_ok(g)) {
     dim3 grid((unsigned)((g.n[0] + TX - 1) / TX), (unsigned)((g.n[1] + TY - 1) / TY), 1);
-    if (has_boundary(p, 2))
-      fv2d_tile<0, true><<<grid, dim3(TX, BY), 0, ctx->stream>>>(g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
-    else
-      fv2d_tile<0, false><<<grid, dim3(TX, BY), 0, ctx->stream>>>(g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
+    launch_tile<0>(has_boundary(p, 2), grid, ctx->stream, g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
   } else {
     fv_apply_kernel<<<grid_blocks(g.nelem, 256), 256, 0, ctx->stream>>>(g, p, 1, u, out, nullptr, 0.0, 0, nullptr,
                                                                         0.0);
@@ -319,20 +422,15 @@ gdt_status fv_timestep(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc
   const double cx = 1.0 / g.h[0], cy = g.dim >= 2 ? 1.0 / g.h[1] : 0.0;
   for (long long st = 0; st < steps; ++st) {
     if (stepper == GDT_TIMESTEPPER_EXPLICIT_EULER) {
-      if (tiled && bnd)
-        fv2d_tile<1, true><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, nxt, dt, cx, cy);
-      else if (tiled)
-        fv2d_tile<1, false><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, nxt, dt, cx, cy);
+      if (tiled)
+        launch_tile<1>(bnd, grid, s, g, p, cur, nullptr, nxt, dt, cx, cy);
       else
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, nullptr, nullptr, 0.0, 1, nxt, dt);
       ctx->launches++;
     } else {
-      if (tiled && bnd) {
-        fv2d_tile<0, true><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, k0, dt, cx, cy);
-        fv2d_tile<2, true><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, k0, nxt, dt, cx, cy);
-      } else if (tiled) {
-        fv2d_tile<0, false><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, nullptr, k0, dt, cx, cy);
-        fv2d_tile<2, false><<<grid, dim3(TX, BY), 0, s>>>(g, p, cur, k0, nxt, dt, cx, cy);
+      if (tiled) {
+        launch_tile<0>(bnd, grid, s, g, p, cur, nullptr, k0, dt, cx, cy);
+        launch_tile<2>(bnd, grid, s, g, p, cur, k0, nxt, dt, cx, cy);
       } else {
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, k0, nullptr, 0.0, 0, nullptr, 0.0);
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, nullptr, k0, cur, -dt, 2, nxt, -0.5 * dt);
