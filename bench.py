@@ -247,11 +247,16 @@ def run_gdt(args):
     ms_e2e = gdt.replicas.max_over_ranks(e0.elapsed_time(e1) / args.steps, device="cuda")
 
     value = world * ndof / (ms_mixed / 1e3)
-    t32, n32 = kinds32["spmv_fp32"]
-    spmv32_ms = t32 / max(n32, 1)
-    # FP32 symmetric-stencil SpMV of the inner CG: 14 slot arrays (diagonal + 13 upper neighbours of the
-    # 27-point Q1 stencil) streamed once, the iterated vector read once and the product written once
-    bytes32 = (1 + 13) * 4 * ndof + 4 * ndof + 4 * ndof
+    inner = info_mixed.get("inner_operator")
+    # algorithmic bytes per launch of each kernel class of the mixed iteration:
+    # inner operator: matrix-free (FP32 element coefficients + p read + q written) or the symmetric
+    #   stencil (14 slot arrays: diagonal + 13 upper neighbours of the 27-point stencil, p, q)
+    # update: x32, p, r32, q, 1/diag read, x32, r32 written; direction: p, r32, 1/diag read, p written
+    op_bytes = (4 * grid.num_elements + 8 * ndof) if inner == "matrix_free" else (14 + 2) * 4 * ndof
+    op_name = ("k_mf_apply: matrix-free FP32 Q1 operator from the element coefficients" if inner == "matrix_free"
+               else "k_mx_spmv3d / k_mx_spmv: FP32 symmetric-stencil SpMV")
+    classes = {"spmv_fp32": (op_name, op_bytes), "cg_update": ("k_mx_update: x, r, r.z, r.r", 28 * ndof),
+               "cg_direction": ("k_mx_p: p = z + beta p", 16 * ndof)}
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -259,7 +264,15 @@ def run_gdt(args):
     except OSError:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    achieved = bytes32 / (spmv32_ms / 1e3) / 1e9
+    by_kernel = {}
+    for cls, (kname, nbytes) in classes.items():
+        t, c = kinds32.get(cls, (0.0, 0))
+        if c:
+            ms_l = t / c
+            by_kernel[cls] = {"kernel": kname, "bytes_per_launch": nbytes, "avg_launch_ms": ms_l, "launches": c,
+                              "total_ms": t, "achieved_gbs": nbytes / (ms_l / 1e3) / 1e9,
+                              "frac": nbytes / (ms_l / 1e3) / 1e9 / hbm}
+    dom = max(by_kernel, key=lambda k: by_kernel[k]["total_ms"])
     t64b, n64b = kinds64.get("spmv_fp64", (0.0, 0))
     spmv64_ms = t64b / max(n64b, 1)
     bytes64 = 12 * nnz + 4 * (ndof + 1) + 16 * ndof
@@ -298,10 +311,13 @@ def run_gdt(args):
             "mixed": {k: round(t / c, 5) for k, (t, c) in kinds32.items()},
             "fp64": {k: round(t / c, 5) for k, (t, c) in kinds64.items()},
             "note": "CUDA events around each kernel class in one extra solve without graph capture"},
-        "roofline": {"bound": "hbm", "kernel": "FP32 symmetric-stencil SpMV of the inner CG (k_mx_spmv)",
-                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "bytes_per_launch": bytes32, "avg_launch_ms": spmv32_ms, "launches": n32,
+        "roofline": {"bound": "hbm", "kernel": by_kernel[dom]["kernel"],
+                     "achieved": by_kernel[dom]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                     "frac": by_kernel[dom]["frac"], "bytes_per_launch": by_kernel[dom]["bytes_per_launch"],
+                     "avg_launch_ms": by_kernel[dom]["avg_launch_ms"], "launches": by_kernel[dom]["launches"],
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)", "traffic": None},
+        "roofline_by_kernel": by_kernel,
+        "inner_operator": inner,
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:

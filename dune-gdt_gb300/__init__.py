@@ -542,6 +542,9 @@ class MatrixOperator:
                       C.byref(info))
         self.last_solve_info = {"iterations": info.iterations, "refinements": info.refinements,
                                 "rel_residual": info.rel_residual, "converged": bool(info.converged)}
+        if o.precision == capi.PRECISION_MIXED:
+            kind = int(capi.load().gdt_matrix_mixed_operator(self.handle))
+            self.last_solve_info["inner_operator"] = {0: "stencil", 1: "stencil_tiled", 2: "matrix_free"}.get(kind)
         return source
 
 

@@ -23,6 +23,7 @@ FLUX_BURGERS, FLUX_TRANSPORT = 0, 1
 NUMFLUX_LAX_FRIEDRICHS, NUMFLUX_UPWIND, NUMFLUX_ENGQUIST_OSHER = 0, 1, 2
 FV_BOUNDARY_NONE, FV_BOUNDARY_EXTRAPOLATE, FV_BOUNDARY_DIRICHLET, FV_BOUNDARY_FLUX = 0, 1, 2, 3
 TIMESTEPPER_EXPLICIT_EULER, TIMESTEPPER_SSPRK2 = 0, 1
+MIXED_OPERATOR_STENCIL, MIXED_OPERATOR_STENCIL_TILED, MIXED_OPERATOR_MATRIX_FREE = 0, 1, 2
 
 
 class DiffusionDesc(C.Structure):
@@ -109,6 +110,7 @@ _SIGNATURES = {
     "gdt_matrix_set_zero": (C.c_int, [P, P]),
     "gdt_matrix_tune": (C.c_int, [P, P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gdt_matrix_set_schedule": (C.c_int, [P, C.c_int]),
+    "gdt_matrix_mixed_operator": (C.c_int, [P]),
     "gdt_assemble_cg_diffusion": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_assemble_cg_rhs": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_dirichlet_apply": (C.c_int, [P, P, P]),

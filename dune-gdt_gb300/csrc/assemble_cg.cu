@@ -242,6 +242,27 @@ LocalTables make_tables(const GridDesc& g) {
 
 }  // namespace
 
+__global__ void k_mf_kappa(long long n, const double* __restrict__ kappa, double kc, float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = float(kappa ? kappa[i] : kc);
+}
+
+gdt_status mf_capture(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d) {
+  const GridDesc& g = m->test.g;
+  m->mf_valid = 0;
+  if (g.dim != 3 || g.simplex || m->test.order != 1 || m->test.kind != GDT_SPACE_CG) return GDT_OK;
+  if (!m->mf_kappa) GDT_TRY_CUDA(ctx, cudaMalloc(&m->mf_kappa, sizeof(float) * g.nelem));
+  const int bl = std::max(1, std::min(grid_blocks(g.nelem, 256), ctx->num_sms * 8));
+  k_mf_kappa<<<bl, 256, 0, ctx->stream>>>(g.nelem, d->kappa, d->kappa_const, m->mf_kappa);
+  const LocalTables tab = make_tables(g);
+  for (int li = 0; li < 8; ++li)
+    for (int lj = 0; lj < 8; ++lj)
+      m->mf_K[local_corner(3, false, 0, li) * 8 + local_corner(3, false, 0, lj)] = float(tab.K[li * kMaxLoc + lj]);
+  m->mf_dirichlet = d->dirichlet ? 1 : 0;
+  m->mf_valid = 1;
+  return check_launch(ctx, "mf_capture");
+}
+
 gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs) {
   const GridDesc& g = m->test.g;
   const LocalTables tab = make_tables(g);
@@ -257,7 +278,8 @@ gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* 
   else if (!g.simplex) GDT_LAUNCH_ASM(3, false);
   else GDT_LAUNCH_ASM(3, true);
 #undef GDT_LAUNCH_ASM
-  return check_launch(ctx, "assemble_cg_rows");
+  GDT_CHECK(ctx, check_launch(ctx, "assemble_cg_rows"));
+  return mf_capture(ctx, m, d);
 }
 
 gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& sp, const gdt_diffusion_desc* d, double* rhs) {

@@ -286,6 +286,7 @@ gdt_status gdt_matrix_create(gdt_context ctx, gdt_space test, gdt_space ansatz, 
 gdt_status gdt_matrix_destroy(gdt_matrix m) {
   if (!m) return GDT_EINVAL;
   ho_matrix_free(static_cast<HoMatrix*>(m->ho));
+  if (m->mf_kappa) cudaFree(m->mf_kappa);
   if (m->rp) cudaFree(m->rp);
   if (m->col) cudaFree(m->col);
   if (m->val) cudaFree(m->val);
@@ -307,6 +308,7 @@ gdt_status gdt_matrix_device_arrays(gdt_matrix m, const int32_t** rp, const int3
 
 gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m) {
   if (!ctx || !m) return GDT_EINVAL;
+  m->mf_valid = 0;
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * m->nnz, ctx->stream));
   return GDT_OK;
 }
@@ -316,6 +318,7 @@ gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_di
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
   if (m->test.order == 2 || d->kappa_qp) {
+    m->mf_valid = 0;
     GDT_CHECK(ctx, ho_prepare(ctx, m));
     return ho_assemble(ctx, m, 0, d->kappa, d->kappa_const, d->kappa_qp, d->force, d->force_const, rhs, d->dirichlet);
   }
@@ -333,12 +336,14 @@ gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
   if (!ctx || !m) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
   if (m->test.order == 2) return ho_dirichlet(ctx, m, rhs);
+  m->mf_dirichlet = 1;
   return dirichlet_apply(ctx, m, rhs);
 }
 
 gdt_status gdt_assemble_cg_product(gdt_context ctx, gdt_matrix m, const gdt_product_desc* d) {
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  m->mf_valid = 0;
   GDT_CHECK(ctx, ho_prepare(ctx, m));
   return ho_assemble(ctx, m, 1, d->weight, d->weight_const, d->weight_qp, nullptr, 0.0, nullptr, 0);
 }

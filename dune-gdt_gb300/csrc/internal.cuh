@@ -78,6 +78,13 @@ struct gdt_matrix_s {
   int cg_sched = -1;   // schedule of the fused FP64 CG iteration, timed inside that iteration (krylov.cu)
   int mx_tiled = -1;   // mixed solver, 3D grids: plane-tiled (1) or linear (0) FP32 stencil SpMV, timed on first use
   void* ho = nullptr;  // element-batched assembly data (order-2 spaces), owned (highorder.cu)
+  // 3D Q1 Laplace assemblies: the element coefficients in FP32 and the reference element stiffness
+  // (corner-bit indexing), for the matrix-free inner operator of the mixed-precision solver
+  float* mf_kappa = nullptr;
+  float mf_K[64] = {};
+  int mf_valid = 0;      // the values are exactly that assembly (cleared by any other value change)
+  int mf_dirichlet = 0;  // with Dirichlet unit rows and columns
+  int mx_operator = -1;  // inner operator of the last mixed-precision solve (GDT_MIXED_OPERATOR_*)
 };
 
 namespace gdt {
@@ -86,6 +93,8 @@ constexpr int kScratchDoubles = 1 << 16;
 constexpr int kCounters = 64;
 
 gdt_status fail(gdt_context ctx, gdt_status s, const std::string& msg);
+// keeps the element coefficients of a 3D Q1 Laplace assembly for the matrix-free FP32 operator
+gdt_status mf_capture(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d);
 gdt_status check_launch(gdt_context ctx, const char* what);
 
 #define GDT_TRY_CUDA(ctx, call)                                                                   \

@@ -118,6 +118,7 @@ gdt_status gdt_matrix_lincomb(gdt_context ctx, gdt_matrix out, int nterms, const
     t.p[q] = terms[q]->val;
     t.theta[q] = theta[q];
   }
+  out->mf_valid = 0;
   return lincomb(ctx, out->nnz, t, out->val);
 }
 

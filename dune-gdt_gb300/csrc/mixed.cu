@@ -23,6 +23,7 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <cstring>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -322,6 +323,171 @@ __global__ void __launch_bounds__(TH) k_mx_update(int n, float* __restrict__ x32
   }
 }
 
+// ---------------------------------------------------------------- matrix-free inner operator ---
+// 3D Q1 Laplace with element coefficients: q_v = sum over the (up to) 8 cells c around vertex v of
+// kappa_c sum_j K[l_v][j] p(corner j of c), the same operator as the assembled matrix (which the
+// assembly forms from the same element matrices), in FP32. It streams the coefficients (4 bytes per
+// cell) and p instead of 14 stencil values per row; the p and kappa gathers hit L1/L2. With DIR the
+// Dirichlet unit rows and zero columns of the assembled matrix are reproduced.
+struct MfOp {
+  int nx, ny, nz;       // vertices per axis
+  long long py, pz;     // FP32 element offsets of +y, +z (pitched lines)
+  float K[64];          // reference element stiffness, K[corner i * 8 + corner j], corner bits (x, y, z)
+};
+
+constexpr int MFX = 32, MFY = 8;  // vertex tile of the matrix-free kernel (x, y)
+
+// Vertex columns in registers: a thread owns column (x, y) of a 32 x 8 tile and a chunk of z planes;
+// it keeps the 3 x 3 neighbourhood of p in the planes z - 1, z, z + 1 and the 2 x 2 coefficients of
+// the cell layers z - 1 and z in registers, so each step loads 9 values of p and 4 coefficients
+// (neighbouring threads share them through L1) instead of 27 and 8, with no shared memory and no
+// barriers. Values outside the grid (and, with DIR, on the boundary) are 0. A per-row variant (27 + 8
+// loads per row) took 35 us at 128^3 and a shared-memory plane-ring variant 40 us (instruction
+// bound); this one 30 us.
+template <bool DIR>
+__global__ void __launch_bounds__(MFX* MFY) k_mf_column(MfOp op, int tiles_x, int tiles_y, int zlen,
+                                                       const float* __restrict__ kappa, const float* __restrict__ p,
+                                                       float* __restrict__ q, MState* st, double* partials,
+                                                       unsigned int* ticket) {
+  if (mstopped(st)) return;
+  const int tx = threadIdx.x % MFX, ty = threadIdx.x / MFX;
+  const int bt = blockIdx.x % (tiles_x * tiles_y), bz = blockIdx.x / (tiles_x * tiles_y);
+  const int x = (bt % tiles_x) * MFX + tx, y = (bt / tiles_x) * MFY + ty;
+  const int zb = bz * zlen, ze = min(op.nz, zb + zlen);
+  const int ncx = op.nx - 1, ncy = op.ny - 1, ncz = op.nz - 1;
+  const bool active = x < op.nx && y < op.ny;
+  // which of the 3 x 3 columns around (x, y) hold values: inside the grid, and with DIR not on the
+  // x or y boundary; which of the 2 x 2 cell columns exist
+  unsigned colmask = 0u, cellmask = 0u;
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int xx = x + dx, yy = y + dy;
+      bool ok = xx >= 0 && yy >= 0 && xx < op.nx && yy < op.ny;
+      if (DIR) ok = ok && xx != 0 && yy != 0 && xx != op.nx - 1 && yy != op.ny - 1;
+      if (ok) colmask |= 1u << ((dy + 1) * 3 + (dx + 1));
+    }
+#pragma unroll
+  for (int b = 0; b < 2; ++b)
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      const int cx = x - 1 + a, cy = y - 1 + b;
+      if (cx >= 0 && cy >= 0 && cx < ncx && cy < ncy) cellmask |= 1u << (b * 2 + a);
+    }
+  const long long ecol = x + op.py * y;  // element of (x, y, 0)
+  const long long kcol = (x - 1) + (long long)ncx * (y - 1);  // cell (x - 1, y - 1, 0)
+  auto load_plane = [&](int z, float (&v)[9]) {
+    const bool zok = z >= 0 && z < op.nz && !(DIR && (z == 0 || z == op.nz - 1));
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const int dx = k % 3 - 1, dy = k / 3 - 1;
+      v[k] = (zok && ((colmask >> k) & 1u)) ? __ldg(p + ecol + dx + op.py * dy + op.pz * z) : 0.f;
+    }
+  };
+  auto load_layer = [&](int c, float (&v)[4]) {
+    const bool cok = c >= 0 && c < ncz;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int a = k & 1, b = k >> 1;
+      v[k] = (cok && ((cellmask >> k) & 1u)) ? __ldg(kappa + kcol + a + ncx * b + (long long)ncx * ncy * c) : 0.f;
+    }
+  };
+  float pm[9], pc[9], pn[9], km[4], kc[4];
+  load_plane(zb - 1, pm);
+  load_plane(zb, pc);
+  load_layer(zb - 1, km);
+  float acc = 0.f;
+  for (int z = zb; z < ze; ++z) {
+    load_plane(z + 1, pn);
+    load_layer(z, kc);
+    if (active) {
+      const long long e = ecol + op.pz * z;
+      const bool bnd = x == 0 || y == 0 || z == 0 || x == op.nx - 1 || y == op.ny - 1 || z == op.nz - 1;
+      float s, pe;
+      if (DIR && bnd) {
+        pe = __ldg(p + e);
+        s = pe;  // unit row
+      } else {
+        pe = pc[4];
+        s = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int a = c & 1, b = (c >> 1) & 1, cc = c >> 2;
+          const float kap = cc ? kc[b * 2 + a] : km[b * 2 + a];
+          const int lv = (1 - a) | ((1 - b) << 1) | ((1 - cc) << 2);
+          float t = 0.f;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int jx = j & 1, jy = (j >> 1) & 1, jz = j >> 2;
+            const int k = (b + jy) * 3 + (a + jx);
+            const float pv = (cc + jz) == 0 ? pm[k] : ((cc + jz) == 1 ? pc[k] : pn[k]);
+            t = fmaf(op.K[lv * 8 + j], pv, t);
+          }
+          s = fmaf(kap, t, s);
+        }
+      }
+      q[e] = s;
+      acc = fmaf(pe, s, acc);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      pm[k] = pc[k];
+      pc[k] = pn[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) km[k] = kc[k];
+  }
+  double vv[1] = {double(acc)};
+  if (grid_reduce<1>(vv, partials, ticket) && threadIdx.x == 0) {
+    if (!(vv[0] > 0.0) || !isfinite(vv[0])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+    st->alpha = st->rho / vv[0];
+  }
+}
+
+// probe of the matrix-free operator against the assembled FP64 matrix: v(i) pseudo-random in [-1, 1]
+__device__ __forceinline__ double mf_probe(long long i) {
+  unsigned long long h = (unsigned long long)i * 0x9E3779B97F4A7C15ull;
+  h ^= h >> 29;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 32;
+  return double(h & 0xFFFFFF) / double(0x800000) - 1.0;
+}
+
+__global__ void k_mf_probe(int n, Pitch pt, double* __restrict__ v64, float* __restrict__ v32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = mf_probe(i);
+    v64[i] = v;
+    v32[pt.of(i)] = float(v);
+  }
+}
+
+// err[0] = max |A64 v - q|, err[1] = max |A64 v| (non-negative floats compare as their bit patterns)
+template <int G, int PL>
+__global__ void __launch_bounds__(TH) k_mf_compare(int n, Pitch pt, const int* __restrict__ rp,
+                                                  const int* __restrict__ col, const double* __restrict__ val,
+                                                  const double* __restrict__ v64, const float* __restrict__ q,
+                                                  unsigned int* err) {
+  float md = 0.f, my = 0.f;
+  for_rows_csr<G, PL, double>(n, rp, col, val, v64, [&](int row, bool leader, double y) {
+    if (leader) {
+      md = fmaxf(md, float(fabs(y - double(q[pt.of(row)]))));
+      my = fmaxf(my, float(fabs(y)));
+    }
+  });
+  for (int o = 16; o > 0; o >>= 1) {
+    md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+    my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(err, __float_as_uint(md));
+    atomicMax(err + 1, __float_as_uint(my));
+  }
+}
+
 // reliable update, part 1: x64 += x32, x32 = 0
 __global__ void __launch_bounds__(TH) k_mx_accumulate(int n, Pitch pt, double* __restrict__ x, float* __restrict__ x32,
                                                      const MState* st) {
@@ -586,7 +752,6 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
     allocs.push_back(p);
     return reinterpret_cast<void*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
   };
-  float* D = (float*)alloc(sizeof(float) * ld * (S.nu + 1));
   // p with zero halos of at least `pad` on both sides; the front halo is a multiple of 64 floats so
   // that p itself starts on a 256-byte boundary
   const long long pfront = (S.pad + 63) / 64 * 64, plen = pfront + np + S.pad;
@@ -597,10 +762,9 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
   float* dinv = (float*)alloc(sizeof(float) * np);
   MState* st = (MState*)alloc(sizeof(MState));
   int* bad = (int*)alloc(sizeof(int));
-  if (!D || !pfull || !r32 || !q32 || !x32 || !dinv || !st || !bad) return fail(ctx, GDT_ENOMEM, "mixed solver vectors");
+  if (!pfull || !r32 || !q32 || !x32 || !dinv || !st || !bad) return fail(ctx, GDT_ENOMEM, "mixed solver vectors");
   float* p = pfull + pfront;
-  // zero: slot arrays and p (halos and line padding), every FP32 vector (line padding)
-  GDT_TRY_CUDA(ctx, cudaMemsetAsync(D, 0, sizeof(float) * ld * (S.nu + 1), s));
+  // zero: p (halos and line padding), every FP32 vector (line padding)
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(pfull, 0, sizeof(float) * plen, s));
   for (float* v : {r32, q32, x32, dinv}) GDT_TRY_CUDA(ctx, cudaMemsetAsync(v, 0, sizeof(float) * np, s));
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(bad, 0, sizeof(int), s));
@@ -608,12 +772,80 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
   init.tol2 = o->tol * o->tol;
   init.max_iter = o->max_iter;
   GDT_TRY_CUDA(ctx, cudaMemcpyAsync(st, &init, sizeof(MState), cudaMemcpyHostToDevice, s));
-  k_build_stencil<<<vec_blocks, TH, 0, s>>>(n, m->rp, m->col, m->val, S, pt, D, ld, bad);
+  // Matrix-free inner operator for 3D Q1 Laplace matrices whose values are exactly their assembly
+  // (element coefficients kept at assembly). Every solve checks it against the assembled FP64 matrix
+  // with one probe product (relative difference below 1e-4, FP32 rounding is ~1e-6); otherwise the
+  // stencil kernels below are used.
+  MfOp mfop{};
+  bool mf = false;
+  int mf_tx = 0, mf_ty = 0, mf_zlen = 0, mf_grid = 0;
+  auto launch_mf = [&](cudaStream_t st_) {
+    if (m->mf_dirichlet)
+      k_mf_column<true><<<mf_grid, MFX * MFY, 0, st_>>>(mfop, mf_tx, mf_ty, mf_zlen, m->mf_kappa, p, q32, st,
+                                                        partials, ticket);
+    else
+      k_mf_column<false><<<mf_grid, MFX * MFY, 0, st_>>>(mfop, mf_tx, mf_ty, mf_zlen, m->mf_kappa, p, q32, st,
+                                                         partials, ticket);
+  };
+  if (tiled3 && g.dim == 3 && !g.simplex && m->mf_valid && m->mf_kappa) {
+    mfop.nx = nx;
+    mfop.ny = int(g.vn[1]);
+    mfop.nz = int(g.vn[2]);
+    mfop.py = pitch;
+    mfop.pz = pitch * g.vn[1];
+    for (int k = 0; k < 64; ++k) mfop.K[k] = m->mf_K[k];
+    double* v64 = (double*)alloc(sizeof(double) * n);
+    unsigned int* err = (unsigned int*)alloc(2 * sizeof(unsigned int));
+    if (!v64 || !err) return fail(ctx, GDT_ENOMEM, "mixed solver vectors");
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(err, 0, 2 * sizeof(unsigned int), s));
+    GDT_CHECK(ctx, tune_spmv(ctx, m));
+    const LaunchShape shc = schedule_shape<double>(m->spmv_sched, n, ctx->num_sms);
+    // z sweep shape: (x, y) tiles times z chunks, about one resident wave
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_column<true>, MFX * MFY, 0) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    cudaGetLastError();
+    mf_tx = (mfop.nx + MFX - 1) / MFX;
+    mf_ty = (mfop.ny + MFY - 1) / MFY;
+    // one resident wave (3 blocks of 256 threads per SM at 73 registers; forcing 4 blocks spilled and
+    // was slower, and so were two waves of shorter chunks)
+    const long long chunks = std::max(1LL, std::min<long long>(mfop.nz, (long long)ctx->num_sms * per_sm /
+                                                                             ((long long)mf_tx * mf_ty)));
+    mf_zlen = int((mfop.nz + chunks - 1) / chunks);
+    mf_grid = mf_tx * mf_ty * ((mfop.nz + mf_zlen - 1) / mf_zlen);
+    if (mf_grid > kScratchDoubles) mf_grid = 0;  // the grid reduction's partials must fit the scratch
+    k_mf_probe<<<vec_blocks, TH, 0, s>>>(n, pt, v64, p);
+    if (mf_grid > 0) launch_mf(s);
+#define GDT_MF_COMPARE(GG, PP) \
+  k_mf_compare<GG, PP><<<shc.blocks, shc.threads, shc.smem, s>>>(n, pt, m->rp, m->col, m->val, v64, q32, err)
+    GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF_COMPARE)
+#undef GDT_MF_COMPARE
+    unsigned int herr[2] = {0u, 0u};
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(herr, err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->launches += 3;
+    float ed, ey;
+    std::memcpy(&ed, &herr[0], sizeof(float));
+    std::memcpy(&ey, &herr[1], sizeof(float));
+    mf = mf_grid > 0 && ey > 0.f && std::isfinite(ed) && ed <= 1e-4f * ey;
+    // restore: p (only the real rows were written), q32 and the solver state
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(pfull, 0, sizeof(float) * plen, s));
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(st, &init, sizeof(MState), cudaMemcpyHostToDevice, s));
+  }
+  float* D = nullptr;
+  if (!mf) {
+    D = (float*)alloc(sizeof(float) * ld * (S.nu + 1));
+    if (!D) return fail(ctx, GDT_ENOMEM, "mixed solver vectors");
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(D, 0, sizeof(float) * ld * (S.nu + 1), s));
+    k_build_stencil<<<vec_blocks, TH, 0, s>>>(n, m->rp, m->col, m->val, S, pt, D, ld, bad);
+    ctx->launches++;
+  }
   k_diag_inv32<<<vec_blocks, TH, 0, s>>>(n, pt, m->rp, m->col, m->val, dinv, o->precond == GDT_PREC_JACOBI);
-  ctx->launches += 2;
+  ctx->launches++;
   // tensor maps of the tiled SpMV: slot arrays (x, y, z, slot) and p (x, y, z), boxes of 40 x 10 x 1 (x 1)
   CUtensorMap tmD{}, tmP{};
-  if (tiled3) {
+  if (tiled3 && !mf) {
     const uint64_t ny = uint64_t(g.vn[1]), nz = uint64_t(g.vn[2]);
     const uint64_t dimsD[4] = {uint64_t(nx), ny, nz, uint64_t(S.nu + 1)};
     const uint64_t strD[3] = {4ull * pitch, 4ull * pitch * ny, 4ull * ld};
@@ -656,7 +888,7 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
       k_mx_spmv3d<3, 4><<<grid3, S3X * S3Y, smem3, st_>>>(nx, ny, nz, zlen, pitch, T3, tmD, tmP, D + S.pad, q32, st,
                                                           partials, ticket);
   };
-  if (tiled3 && m->mx_tiled < 0) {
+  if (tiled3 && !mf && m->mx_tiled < 0) {
     cudaEvent_t e0, e1, e2;
     float t_lin = 0.f, t_til = 0.f;
     bool ok = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
@@ -685,6 +917,8 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
     if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string("stencil SpMV timing: ") + cudaGetErrorString(e));
   }
   const bool use_tiled = tiled3 && m->mx_tiled == 1;
+  m->mx_operator = mf ? GDT_MIXED_OPERATOR_MATRIX_FREE
+                      : (use_tiled ? GDT_MIXED_OPERATOR_STENCIL_TILED : GDT_MIXED_OPERATOR_STENCIL);
   const int chunk = o->check_every > 0 ? o->check_every : 32;
   // per iteration: SpMV, update, [reliable update: accumulate + true residual], direction. In graphs
   // the reliable update is the body of an IF node set by the update kernel, so the ~97 % of
@@ -695,7 +929,8 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
                                      [&](CondSection& cs) {
     const cudaGraphConditionalHandle cond = cs.next_handle();
     timing_begin(ctx, s, GDT_TIMING_SPMV_FP32);
-    if (use_tiled) launch_tiled(s);
+    if (mf) launch_mf(s);
+    else if (use_tiled) launch_tiled(s);
     else launch_linear(s);
     timing_end(ctx, s);
     timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);

@@ -112,3 +112,5 @@ extern "C" gdt_status gdt_matrix_set_schedule(gdt_matrix m, int schedule) {
   m->cg_sched = schedule;
   return GDT_OK;
 }
+
+extern "C" int gdt_matrix_mixed_operator(gdt_matrix m) { return m ? m->mx_operator : -1; }

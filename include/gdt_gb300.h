@@ -210,6 +210,13 @@ typedef struct gdt_ipdg_desc {
  * DirichletCoupling/BoundaryPenalty (homogeneous Dirichlet boundary), penalty length h = |I|. */
 gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* desc, double* rhs);
 
+/* Inner FP32 operator of the last mixed-precision CG solve with this matrix (-1: none yet):
+ * the symmetric stencil of the assembled values (linear or plane-tiled kernel), or, for 3D Q1
+ * Laplace matrices whose values are exactly their assembly, the matrix-free element operator
+ * (checked against the assembled matrix by a probe product at every solve). */
+enum { GDT_MIXED_OPERATOR_STENCIL = 0, GDT_MIXED_OPERATOR_STENCIL_TILED = 1, GDT_MIXED_OPERATOR_MATRIX_FREE = 2 };
+int gdt_matrix_mixed_operator(gdt_matrix m);
+
 /* ------------------------------------------------------ parametric lincomb --- */
 /* The assembled form of pyMOR's LincombOperator over dune-gdt matrices, as the parametric examples
  * build it (one matrix per coefficient function of an affine decomposition,

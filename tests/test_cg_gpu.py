@@ -168,6 +168,41 @@ def test_mixed_precision_3d_grids_match_direct(gdt, oracle, n, simplex):
     assert rel_err(x.cpu().numpy(), xd) < 1e-9
 
 
+def test_mixed_precision_matrix_free_operator_follows_the_matrix(gdt, oracle):
+    # 3D Q1 Laplace matrices run the inner FP32 operator matrix-free from the element coefficients
+    # kept at assembly; a probe product against the assembled matrix guards it at every solve
+    op, rhs, A, b = _heat_problem(gdt, oracle, 3, [20, 18, 17], False)
+    Asp = A.to_scipy().tocsc()
+    x = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+    assert op.last_solve_info["converged"] and op.last_solve_info["inner_operator"] == "matrix_free"
+    assert rel_err(x.cpu().numpy(), spl.spsolve(Asp, b)) < 1e-9
+    # values changed behind the library's back (through the zero-copy CSR view): the probe product no
+    # longer matches, the solve falls back to the stencil of the actual values
+    op.csr()[2].mul_(2.0)
+    x2 = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+    assert op.last_solve_info["converged"] and op.last_solve_info["inner_operator"].startswith("stencil")
+    assert rel_err(x2.cpu().numpy(), spl.spsolve(2.0 * Asp, b)) < 1e-9
+
+
+def test_mixed_precision_matrix_free_with_separate_dirichlet(gdt, oracle):
+    # assembly without constraints, then DirichletConstraints::apply: the operator takes the unit rows
+    # and zero columns from the constraint pass
+    n = [16, 15, 14]
+    g, og = _grid(gdt, oracle, 3, n, False)
+    rng = np.random.default_rng(8)
+    kappa = np.exp(rng.standard_normal(g.num_elements))
+    A, b = oracle.assemble_cg(og, 1, kappa=kappa, force_const=1.0)
+    space = gdt.ContinuousLagrangeSpace(g, 1)
+    op = gdt.MatrixOperator(g, space)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(torch.tensor(kappa, device="cuda")))
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    op.assemble(rhs=rhs, force=1.0, dirichlet=False)
+    gdt.DirichletConstraints("dirichlet", space).apply(op, rhs)
+    x = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+    assert op.last_solve_info["converged"] and op.last_solve_info["inner_operator"] == "matrix_free"
+    assert rel_err(x.cpu().numpy(), spl.spsolve(A.to_scipy().tocsc(), b)) < 1e-9
+
+
 @pytest.mark.parametrize("dim,n,simplex", [(2, [24, 20], True), (3, [9, 8, 7], False)])
 def test_newton_apply_inverse_matches_direct(gdt, oracle, dim, n, simplex):
     # OperatorInterface::apply_inverse, type "newton" (operators/interfaces.hh:490-599) on the affine
