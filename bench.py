@@ -248,15 +248,19 @@ def run_gdt(args):
 
     value = world * ndof / (ms_mixed / 1e3)
     inner = info_mixed.get("inner_operator")
-    # algorithmic bytes per launch of each kernel class of the mixed iteration:
-    # inner operator: matrix-free (FP32 element coefficients + p read + q written) or the symmetric
-    #   stencil (14 slot arrays: diagonal + 13 upper neighbours of the 27-point stencil, p, q)
-    # update: x32, p, r32, q, 1/diag read, x32, r32 written; direction: p, r32, 1/diag read, p written
-    op_bytes = (4 * grid.num_elements + 8 * ndof) if inner == "matrix_free" else (14 + 2) * 4 * ndof
-    op_name = ("k_mf_apply: matrix-free FP32 Q1 operator from the element coefficients" if inner == "matrix_free"
-               else "k_mx_spmv3d / k_mx_spmv: FP32 symmetric-stencil SpMV")
-    classes = {"spmv_fp32": (op_name, op_bytes), "cg_update": ("k_mx_update: x, r, r.z, r.r", 28 * ndof),
-               "cg_direction": ("k_mx_p: p = z + beta p", 16 * ndof)}
+    # algorithmic bytes per launch of each kernel class of the mixed iteration (stencil path: 14 slot
+    # arrays = diagonal + 13 upper neighbours of the 27-point stencil, p read, q written; update x32,
+    # p, r32, q, 1/diag read, x32, r32 written; direction p, r32, 1/diag read, p written)
+    if inner == "matrix_free":
+        # Chronopoulos-Gear iteration: operator w = A z with r.z, z.w, r.r (coefficients, z, own r read,
+        # w written); one vector update p, s, x, r, z (z, p, w, s, x, r, 1/diag read; p, s, x, r, z written)
+        classes = {"spmv_fp32": ("k_mf_column: matrix-free FP32 Q1 operator from the element coefficients",
+                                 4 * grid.num_elements + 12 * ndof),
+                   "cg_update": ("k_cgcg_update: p, s, x, r, z", 48 * ndof)}
+    else:
+        classes = {"spmv_fp32": ("k_mx_spmv3d / k_mx_spmv: FP32 symmetric-stencil SpMV", (14 + 2) * 4 * ndof),
+                   "cg_update": ("k_mx_update: x, r, r.z, r.r", 28 * ndof),
+                   "cg_direction": ("k_mx_p: p = z + beta p", 16 * ndof)}
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:

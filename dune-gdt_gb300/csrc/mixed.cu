@@ -44,6 +44,8 @@ struct MState {
   double drop;  // replacement when the iterated residual (squared) has dropped by this factor
   int iter, max_iter, converged, flag, breakdown, updates;
   int restarting;  // stagnation guard tripped: every replacement restarts the direction
+  // Chronopoulos-Gear recurrences (matrix-free path): gamma = r.z, its previous value, previous alpha
+  double gamma, gamma_prev, alpha_prev;
   int fault;  // a bounded device wait ran out (tile loads of the 3D SpMV)
 };
 
@@ -344,11 +346,18 @@ constexpr int MFX = 32, MFY = 8;  // vertex tile of the matrix-free kernel (x, y
 // barriers. Values outside the grid (and, with DIR, on the boundary) are 0. A per-row variant (27 + 8
 // loads per row) took 35 us at 128^3 and a shared-memory plane-ring variant 40 us (instruction
 // bound); this one 30 us.
-template <bool DIR>
+// MODE (what the last block does with the reductions):
+//   MF_CG: q = A p with p.q -> alpha (standard CG; the probe check)
+//   MF_CGCG_INIT / MF_CGCG / MF_CGCG_REPLACE: w = A z with gamma = r.z, delta = z.w and r.r (the
+//   Chronopoulos-Gear form of CG: one reduction phase per iteration), p = the z argument, q = w
+enum { MF_CG = 0, MF_CGCG = 1, MF_CGCG_REPLACE = 2, MF_CGCG_INIT = 3 };
+
+template <bool DIR, int MODE>
 __global__ void __launch_bounds__(MFX* MFY) k_mf_column(MfOp op, int tiles_x, int tiles_y, int zlen,
                                                        const float* __restrict__ kappa, const float* __restrict__ p,
-                                                       float* __restrict__ q, MState* st, double* partials,
-                                                       unsigned int* ticket) {
+                                                       float* __restrict__ q, const float* __restrict__ r, MState* st,
+                                                       double* partials, unsigned int* ticket,
+                                                       cudaGraphConditionalHandle cond) {
   if (mstopped(st)) return;
   const int tx = threadIdx.x % MFX, ty = threadIdx.x / MFX;
   const int bt = blockIdx.x % (tiles_x * tiles_y), bz = blockIdx.x / (tiles_x * tiles_y);
@@ -397,7 +406,7 @@ __global__ void __launch_bounds__(MFX* MFY) k_mf_column(MfOp op, int tiles_x, in
   load_plane(zb - 1, pm);
   load_plane(zb, pc);
   load_layer(zb - 1, km);
-  float acc = 0.f;
+  float acc = 0.f, acc1 = 0.f, acc2 = 0.f;
   for (int z = zb; z < ze; ++z) {
     load_plane(z + 1, pn);
     load_layer(z, kc);
@@ -428,7 +437,14 @@ __global__ void __launch_bounds__(MFX* MFY) k_mf_column(MfOp op, int tiles_x, in
         }
       }
       q[e] = s;
-      acc = fmaf(pe, s, acc);
+      if (MODE == MF_CG) {
+        acc = fmaf(pe, s, acc);
+      } else {
+        const float re = __ldg(r + e);
+        acc = fmaf(re, pe, acc);   // gamma = r.z
+        acc1 = fmaf(pe, s, acc1);  // delta = z.w
+        acc2 = fmaf(re, re, acc2); // r.r
+      }
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
@@ -438,13 +454,81 @@ __global__ void __launch_bounds__(MFX* MFY) k_mf_column(MfOp op, int tiles_x, in
 #pragma unroll
     for (int k = 0; k < 4; ++k) km[k] = kc[k];
   }
-  double vv[1] = {double(acc)};
-  if (grid_reduce<1>(vv, partials, ticket) && threadIdx.x == 0) {
-    if (!(vv[0] > 0.0) || !isfinite(vv[0])) {
-      st->breakdown = 1;
-      st->converged = 1;
+  if constexpr (MODE == MF_CG) {
+    double vv[1] = {double(acc)};
+    if (grid_reduce<1>(vv, partials, ticket) && threadIdx.x == 0) {
+      if (!(vv[0] > 0.0) || !isfinite(vv[0])) {
+        st->breakdown = 1;
+        st->converged = 1;
+      }
+      st->alpha = st->rho / vv[0];
     }
-    st->alpha = st->rho / vv[0];
+  } else {
+    double vv[3] = {double(acc), double(acc1), double(acc2)};
+    if (grid_reduce<3>(vv, partials, ticket) && threadIdx.x == 0) {
+      const double gamma = vv[0], delta = vv[1], rr = vv[2];
+      double beta = 0.0, alpha;
+      if (MODE == MF_CGCG_INIT) {
+        st->gamma_prev = gamma;
+        alpha = gamma / delta;
+        st->alpha_prev = alpha;
+      } else {
+        if (MODE == MF_CGCG) {
+          st->gamma_prev = st->gamma;
+          st->alpha_prev = st->alpha;
+        }
+        beta = (MODE == MF_CGCG_REPLACE && st->restarting) ? 0.0 : gamma / st->gamma_prev;
+        alpha = gamma / (delta - beta * gamma / st->alpha_prev);
+      }
+      st->gamma = gamma;
+      st->beta = beta;
+      st->alpha = alpha;
+      if (MODE == MF_CGCG) {
+        st->iter += 1;
+        st->rr = rr;
+        st->flag = (rr <= st->drop * st->rr_ref || rr <= st->tol2 * st->rr0 || st->iter >= st->max_iter) ? 1 : 0;
+      }
+      if (!(delta > 0.0) || !isfinite(alpha) || !isfinite(rr)) {
+        st->breakdown = 1;
+        st->converged = 1;
+      }
+      if (MODE == MF_CGCG && cond) cudaGraphSetConditional(cond, (st->flag && !st->converged) ? 1u : 0u);
+    }
+  }
+}
+
+// Chronopoulos-Gear vector update (no reduction): p = z + beta p, s = w + beta s (s = A p),
+// x32 += alpha p, r32 -= alpha s, z = dinv r32. Quads of rows; every vector 16-byte aligned.
+__global__ void __launch_bounds__(TH) k_cgcg_update(int n4, float4* __restrict__ p, float4* __restrict__ s4,
+                                                   float4* __restrict__ x32, float4* __restrict__ r,
+                                                   float4* __restrict__ z, const float4* __restrict__ w,
+                                                   const float4* __restrict__ dinv, const MState* st) {
+  if (mstopped(st)) return;
+  const float a = float(st->alpha), b = float(st->beta);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += gridDim.x * blockDim.x) {
+    float4 pv = p[k], sv = s4[k], xv = x32[k], rv = r[k];
+    const float4 zv = z[k], wv = w[k], dv = dinv[k];
+    pv.x = fmaf(b, pv.x, zv.x);
+    pv.y = fmaf(b, pv.y, zv.y);
+    pv.z = fmaf(b, pv.z, zv.z);
+    pv.w = fmaf(b, pv.w, zv.w);
+    sv.x = fmaf(b, sv.x, wv.x);
+    sv.y = fmaf(b, sv.y, wv.y);
+    sv.z = fmaf(b, sv.z, wv.z);
+    sv.w = fmaf(b, sv.w, wv.w);
+    xv.x = fmaf(a, pv.x, xv.x);
+    xv.y = fmaf(a, pv.y, xv.y);
+    xv.z = fmaf(a, pv.z, xv.z);
+    xv.w = fmaf(a, pv.w, xv.w);
+    rv.x = fmaf(-a, sv.x, rv.x);
+    rv.y = fmaf(-a, sv.y, rv.y);
+    rv.z = fmaf(-a, sv.z, rv.z);
+    rv.w = fmaf(-a, sv.w, rv.w);
+    p[k] = pv;
+    s4[k] = sv;
+    x32[k] = xv;
+    r[k] = rv;
+    z[k] = make_float4(dv.x * rv.x, dv.y * rv.y, dv.z * rv.z, dv.w * rv.w);
   }
 }
 
@@ -505,7 +589,8 @@ __global__ void __launch_bounds__(TH) k_mx_true_residual(int n, Pitch pt, const 
                                                         const int* __restrict__ col, const double* __restrict__ val,
                                                         const double* __restrict__ x, const double* __restrict__ b,
                                                         float* __restrict__ r32, const float* __restrict__ dinv,
-                                                        MState* st, double* partials, unsigned int* ticket) {
+                                                        MState* st, double* partials, unsigned int* ticket,
+                                                        float* __restrict__ z32) {
   if (mstopped(st) || !*((volatile const int*)&st->flag)) return;
   double a0 = 0.0, a1 = 0.0;
   for_rows_csr<G, PL, double>(n, rp, col, val, x, [&](int row, bool leader, double s) {
@@ -514,6 +599,7 @@ __global__ void __launch_bounds__(TH) k_mx_true_residual(int n, Pitch pt, const 
       const float rf = float(ri);
       const long long ip = pt.of(row);
       r32[ip] = rf;
+      if (z32) z32[ip] = dinv[ip] * rf;  // z = M r for the Chronopoulos-Gear recurrences
       a0 = fma(double(rf), double(dinv[ip] * rf), a0);
       a1 = fma(ri, ri, a1);
     }
@@ -779,13 +865,23 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
   MfOp mfop{};
   bool mf = false;
   int mf_tx = 0, mf_ty = 0, mf_zlen = 0, mf_grid = 0;
-  auto launch_mf = [&](cudaStream_t st_) {
-    if (m->mf_dirichlet)
-      k_mf_column<true><<<mf_grid, MFX * MFY, 0, st_>>>(mfop, mf_tx, mf_ty, mf_zlen, m->mf_kappa, p, q32, st,
-                                                        partials, ticket);
-    else
-      k_mf_column<false><<<mf_grid, MFX * MFY, 0, st_>>>(mfop, mf_tx, mf_ty, mf_zlen, m->mf_kappa, p, q32, st,
-                                                         partials, ticket);
+  // the operator applied to the halo buffer `p` (which holds z in the Chronopoulos-Gear iteration)
+  auto launch_mf = [&](cudaStream_t st_, int mode, cudaGraphConditionalHandle c) {
+#define GDT_MF_LAUNCH(D, M)                                                                                 \
+  k_mf_column<D, M><<<mf_grid, MFX * MFY, 0, st_>>>(mfop, mf_tx, mf_ty, mf_zlen, m->mf_kappa, p, q32, r32, st, \
+                                                    partials, ticket, c)
+    if (m->mf_dirichlet) {
+      if (mode == MF_CG) GDT_MF_LAUNCH(true, MF_CG);
+      else if (mode == MF_CGCG) GDT_MF_LAUNCH(true, MF_CGCG);
+      else if (mode == MF_CGCG_REPLACE) GDT_MF_LAUNCH(true, MF_CGCG_REPLACE);
+      else GDT_MF_LAUNCH(true, MF_CGCG_INIT);
+    } else {
+      if (mode == MF_CG) GDT_MF_LAUNCH(false, MF_CG);
+      else if (mode == MF_CGCG) GDT_MF_LAUNCH(false, MF_CGCG);
+      else if (mode == MF_CGCG_REPLACE) GDT_MF_LAUNCH(false, MF_CGCG_REPLACE);
+      else GDT_MF_LAUNCH(false, MF_CGCG_INIT);
+    }
+#undef GDT_MF_LAUNCH
   };
   if (tiled3 && g.dim == 3 && !g.simplex && m->mf_valid && m->mf_kappa) {
     mfop.nx = nx;
@@ -802,7 +898,8 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
     const LaunchShape shc = schedule_shape<double>(m->spmv_sched, n, ctx->num_sms);
     // z sweep shape: (x, y) tiles times z chunks, about one resident wave
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_column<true>, MFX * MFY, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mf_column<true, MF_CGCG>, MFX * MFY, 0) !=
+            cudaSuccess ||
         per_sm < 1)
       per_sm = 1;
     cudaGetLastError();
@@ -816,7 +913,7 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
     mf_grid = mf_tx * mf_ty * ((mfop.nz + mf_zlen - 1) / mf_zlen);
     if (mf_grid > kScratchDoubles) mf_grid = 0;  // the grid reduction's partials must fit the scratch
     k_mf_probe<<<vec_blocks, TH, 0, s>>>(n, pt, v64, p);
-    if (mf_grid > 0) launch_mf(s);
+    if (mf_grid > 0) launch_mf(s, MF_CG, 0);
 #define GDT_MF_COMPARE(GG, PP) \
   k_mf_compare<GG, PP><<<shc.blocks, shc.threads, shc.smem, s>>>(n, pt, m->rp, m->col, m->val, v64, q32, err)
     GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF_COMPARE)
@@ -864,9 +961,22 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
                                                            partials, ticket)
 #define GDT_MX_TRUE_RESIDUAL(GG, PP)                                                                             \
   k_mx_true_residual<GG, PP><<<sh.blocks, sh.threads, sh.smem, cstream>>>(n, pt, m->rp, m->col, m->val, x, b, r32, \
-                                                                          dinv, st, partials, ticket)
+                                                                          dinv, st, partials, ticket, mf ? p : nullptr)
   GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MX_INIT)
   ctx->launches++;
+  // Chronopoulos-Gear form on the matrix-free path (one reduction phase per iteration): the halo
+  // buffer p holds z = M r (written by the init kernel), pd the search direction, s32 = A pd, q32 = A z
+  float* pd = nullptr;
+  float* s32 = nullptr;
+  if (mf) {
+    pd = (float*)alloc(sizeof(float) * np);
+    s32 = (float*)alloc(sizeof(float) * np);
+    if (!pd || !s32) return fail(ctx, GDT_ENOMEM, "mixed solver vectors");
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(pd, 0, sizeof(float) * np, s));
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(s32, 0, sizeof(float) * np, s));
+    launch_mf(s, MF_CGCG_INIT, 0);
+    ctx->launches++;
+  }
   // FP32 stencil SpMV of this matrix: on 3D grids the TMA-tiled and the linear kernel are timed
   // once (CUDA events, one warm-up and three launches each; they only rewrite q32 and alpha, which
   // the first iteration recomputes) and the faster is kept for the matrix
@@ -928,9 +1038,30 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
   GDT_CHECK(ctx, iterate_chunks_cond(ctx, s, &st->converged, chunk, o->max_iter / chunk + 2, &graphed,
                                      [&](CondSection& cs) {
     const cudaGraphConditionalHandle cond = cs.next_handle();
+    if (mf) {
+      // update (no reduction), operator + the three dots (alpha, beta, replacement test), [reliable
+      // update: accumulate, true residual and z, operator again for the replaced residual]
+      timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);
+      k_cgcg_update<<<quad_blocks, TH, 0, s>>>(npi / 4, reinterpret_cast<float4*>(pd), reinterpret_cast<float4*>(s32),
+                                               reinterpret_cast<float4*>(x32), reinterpret_cast<float4*>(r32),
+                                               reinterpret_cast<float4*>(p), reinterpret_cast<const float4*>(q32),
+                                               reinterpret_cast<const float4*>(dinv), st);
+      timing_end(ctx, s);
+      timing_begin(ctx, s, GDT_TIMING_SPMV_FP32);
+      launch_mf(s, MF_CGCG, cond);
+      timing_end(ctx, s);
+      timing_begin(ctx, s, GDT_TIMING_RELIABLE_UPDATE);
+      cstream = cs.begin(cond);
+      k_mx_accumulate<<<vec_blocks, TH, 0, cstream>>>(n, pt, x, x32, st);
+      GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MX_TRUE_RESIDUAL)
+      launch_mf(cstream, MF_CGCG_REPLACE, 0);
+      cs.end();
+      timing_end(ctx, s);
+      ctx->launches += cs.capturing ? 2 : 5;  // captured IF bodies are counted when they ran (below)
+      return;
+    }
     timing_begin(ctx, s, GDT_TIMING_SPMV_FP32);
-    if (mf) launch_mf(s);
-    else if (use_tiled) launch_tiled(s);
+    if (use_tiled) launch_tiled(s);
     else launch_linear(s);
     timing_end(ctx, s);
     timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);
@@ -960,7 +1091,7 @@ gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, d
   }
   if (hbad) return fail(ctx, GDT_EUNSUPPORTED, "matrix entry outside the vertex stencil");
   if (fin.fault) return fail(ctx, GDT_ETIMEOUT, "tiled stencil SpMV: a tile-load wait ran out");
-  if (graphed) ctx->launches += 2LL * fin.updates;
+  if (graphed) ctx->launches += (mf ? 3LL : 2LL) * fin.updates;
   gdt_solve_info res{};
   res.iterations = fin.iter;
   res.refinements = fin.updates;
