@@ -46,6 +46,7 @@ struct MState {
   int restarting;  // stagnation guard tripped: every replacement restarts the direction
   // Chronopoulos-Gear recurrences (matrix-free path): gamma = r.z, its previous value, previous alpha
   double gamma, gamma_prev, alpha_prev;
+  int replaced_iter;  // iteration of the last residual replacement (gates the operator that follows it)
   int fault;  // a bounded device wait ran out (tile loads of the 3D SpMV)
 };
 
@@ -359,6 +360,10 @@ __global__ void __launch_bounds__(MFX* MFY) k_mf_column(MfOp op, int tiles_x, in
                                                        double* partials, unsigned int* ticket,
                                                        cudaGraphConditionalHandle cond) {
   if (mstopped(st)) return;
+  // after a residual replacement only (outside graphs the reliable-update kernels run every iteration
+  // and exit early when there is nothing to do)
+  if (MODE == MF_CGCG_REPLACE && *((volatile const int*)&st->replaced_iter) != *((volatile const int*)&st->iter))
+    return;
   const int tx = threadIdx.x % MFX, ty = threadIdx.x / MFX;
   const int bt = blockIdx.x % (tiles_x * tiles_y), bz = blockIdx.x / (tiles_x * tiles_y);
   const int x = (bt % tiles_x) * MFX + tx, y = (bt / tiles_x) * MFY + ty;
@@ -620,6 +625,7 @@ __global__ void __launch_bounds__(TH) k_mx_true_residual(int n, Pitch pt, const 
     st->rho = v[0];
     st->flag = 0;
     st->updates += 1;
+    st->replaced_iter = st->iter;
     if (v[1] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) st->converged = 1;
     if (!isfinite(v[1])) {
       st->breakdown = 1;
@@ -673,6 +679,7 @@ __global__ void __launch_bounds__(TH) k_mx_init(int n, Pitch pt, const int* __re
     st->rr = st->rr0 = st->rr_ref = v[1];
     st->drop = 0.01;
     st->restarting = 0;
+    st->replaced_iter = -1;
     st->iter = 0;
     st->flag = 0;
     st->updates = 0;

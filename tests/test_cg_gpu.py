@@ -184,6 +184,24 @@ def test_mixed_precision_matrix_free_operator_follows_the_matrix(gdt, oracle):
     assert rel_err(x2.cpu().numpy(), spl.spsolve(2.0 * Asp, b)) < 1e-9
 
 
+@pytest.mark.parametrize("n", [[20, 18, 17], [12, 10, 14]])
+def test_mixed_precision_direct_launches_match_graphs(gdt, oracle, n):
+    # with kernel timing on, the iterations run as direct launches (no graph capture) and the
+    # reliable-update kernels run every iteration as early exits: same iterates as the graphs
+    op, rhs, A, b = _heat_problem(gdt, oracle, 3, n, False)
+    x1 = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12}).clone()
+    it1 = op.last_solve_info["iterations"]
+    lib = gdt._capi.load()
+    lib.gdt_context_set_timing(op.ctx.handle, 1)
+    try:
+        x2 = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+        it2 = op.last_solve_info["iterations"]
+    finally:
+        lib.gdt_context_set_timing(op.ctx.handle, 0)
+    assert it1 == it2
+    assert torch.equal(x1, x2)
+
+
 def test_mixed_precision_matrix_free_with_separate_dirichlet(gdt, oracle):
     # assembly without constraints, then DirichletConstraints::apply: the operator takes the unit rows
     # and zero columns from the constraint pass
