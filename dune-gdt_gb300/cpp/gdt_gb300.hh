@@ -412,6 +412,136 @@ Solver<d> make_solver(MatrixOperator<d>& m) {
   return Solver<d>(m);
 }
 
+// ------------------------------------------------------------------------ finite volumes ---
+// Flux functions of the FV tests (f(u) = u^2/2 (1, ..., 1) for Burgers, f(u) = v u for linear transport)
+// and the numerical fluxes of local/numerical-fluxes/ (lax-friedrichs.hh, upwind.hh, engquist-osher.hh),
+// lowered to gdt_fv_desc.
+struct BurgersFlux {
+  void lower(gdt_fv_desc& d) const { d.flux = GDT_FLUX_BURGERS; }
+};
+struct LinearTransportFlux {
+  std::array<double, 3> velocity{};
+  void lower(gdt_fv_desc& d) const {
+    d.flux = GDT_FLUX_TRANSPORT;
+    for (int k = 0; k < 3; ++k) d.velocity[k] = velocity[k];
+  }
+};
+template <class F>
+struct NumericalLaxFriedrichsFlux {
+  F flux;
+  double lambda = 0.0;  // 0: local speeds; else the reference's fixed lambda_
+  explicit NumericalLaxFriedrichsFlux(const F& f, double l = 0.0) : flux(f), lambda(l) {}
+  void lower(gdt_fv_desc& d) const {
+    flux.lower(d);
+    d.numflux = GDT_NUMFLUX_LAX_FRIEDRICHS;
+    d.lf_lambda = lambda;
+  }
+};
+template <class F>
+struct NumericalUpwindFlux {
+  F flux;
+  explicit NumericalUpwindFlux(const F& f) : flux(f) {}
+  void lower(gdt_fv_desc& d) const {
+    flux.lower(d);
+    d.numflux = GDT_NUMFLUX_UPWIND;
+  }
+};
+template <class F>
+struct NumericalEngquistOsherFlux {
+  F flux;
+  explicit NumericalEngquistOsherFlux(const F& f) : flux(f) {}
+  void lower(gdt_fv_desc& d) const {
+    flux.lower(d);
+    d.numflux = GDT_NUMFLUX_ENGQUIST_OSHER;
+  }
+};
+
+// LocalAdvectionFvBoundaryTreatmentByCustomExtrapolationOperator / ...ByCustomNumericalFluxOperator
+// (local/operators/advection-fv.hh:187-457) with their lambdas lowered to the GDT_FV_BOUNDARY_* kinds
+struct BoundaryTreatmentByCustomExtrapolation {  // ghost state v = u (outflow) or a prescribed state
+  int kind = GDT_FV_BOUNDARY_EXTRAPOLATE;
+  double value = 0.0;
+  BoundaryTreatmentByCustomExtrapolation() = default;
+  explicit BoundaryTreatmentByCustomExtrapolation(double state) : kind(GDT_FV_BOUNDARY_DIRICHLET), value(state) {}
+};
+struct BoundaryTreatmentByCustomNumericalFlux {  // boundary flux f.n = value (0: impermeable wall)
+  int kind = GDT_FV_BOUNDARY_FLUX;
+  double value = 0.0;
+  explicit BoundaryTreatmentByCustomNumericalFlux(double g = 0.0) : value(g) {}
+};
+enum class Side { minus_x = 0, plus_x = 1, minus_y = 2, plus_y = 3, minus_z = 4, plus_z = 5 };
+
+// AdvectionFvOperator(grid_view, numerical_flux, source_space, range_space) (operators/advection-fv.hh:66-115)
+template <int d>
+class AdvectionFvOperator {
+ public:
+  template <class NF>
+  AdvectionFvOperator(const CubeGrid<d>& /*grid_view*/, const NF& numerical_flux, const Space<d>& source_space,
+                      const Space<d>& /*range_space*/)
+      : space_(source_space) {
+    numerical_flux.lower(desc_);
+  }
+  // append(boundary treatment, filter): the sides it applies to (all boundary sides when empty)
+  template <class T>
+  AdvectionFvOperator& append(const T& treatment, std::vector<Side> sides = {}) {
+    if (sides.empty())
+      for (int k = 0; k < 2 * d; ++k) sides.push_back(Side(k));
+    for (Side sd : sides) {
+      desc_.boundary[int(sd)] = treatment.kind;
+      desc_.boundary_value[int(sd)] = treatment.value;
+    }
+    return *this;
+  }
+  void apply(const DeviceVector& source, DeviceVector& range) const {
+    check(gdt_fv_apply(default_context(), space_.handle(), &desc_, source.data(), range.data()), default_context(),
+          "AdvectionFvOperator::apply");
+  }
+  const gdt_fv_desc& desc() const { return desc_; }
+  const Space<d>& space() const { return space_; }
+
+ private:
+  Space<d> space_;
+  gdt_fv_desc desc_{};
+};
+
+// estimate_dt_for_hyperbolic_system(grid_view, initial_values, flux) (tools/hyperbolic.hh:38-86)
+template <int d>
+double estimate_dt_for_hyperbolic_system(const CubeGrid<d>& /*grid_view*/, const DeviceVector& initial_values,
+                                         const AdvectionFvOperator<d>& op) {
+  double dt = 0.0;
+  check(gdt_fv_estimate_dt(default_context(), op.space().handle(), &op.desc(), initial_values.data(), &dt),
+        default_context(), "estimate_dt_for_hyperbolic_system");
+  return dt;
+}
+
+// ExplicitRungeKuttaTimeStepper(op, initial_values, r = -1) with the explicit Euler or the second-order
+// SSP tableau (tools/timestepper/explicit-rungekutta.hh:82-97, 237-270); the state lives on the device
+template <int d>
+class ExplicitRungeKuttaTimeStepper {
+ public:
+  ExplicitRungeKuttaTimeStepper(const AdvectionFvOperator<d>& op, DeviceVector& initial_values,
+                                int method = GDT_TIMESTEPPER_SSPRK2)
+      : op_(op), u_(initial_values), method_(method),
+        work_(GDT_FV_WORK_DOUBLES(method, 1, initial_values.size())) {}
+  // one step of size dt (the reference's step(): u^{n+1} from u^n); returns dt
+  double step(double dt, int64_t steps = 1) {
+    check(gdt_fv_timestep(default_context(), op_.space().handle(), &op_.desc(), method_, dt, steps, 1, u_.data(),
+                          work_.data()),
+          default_context(), "ExplicitRungeKuttaTimeStepper::step");
+    t_ += dt * double(steps);
+    return dt;
+  }
+  double current_time() const { return t_; }
+  const DeviceVector& current_solution() const { return u_; }
+
+ private:
+  const AdvectionFvOperator<d>& op_;
+  DeviceVector& u_;
+  int method_;
+  DeviceVector work_;
+  double t_ = 0.0;
+};
+
 }  // namespace GB300
 }  // namespace GDT
 }  // namespace Dune

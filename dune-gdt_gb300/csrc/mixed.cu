@@ -346,7 +346,9 @@ constexpr int MFX = 32, MFY = 8;  // vertex tile of the matrix-free kernel (x, y
 // (neighbouring threads share them through L1) instead of 27 and 8, with no shared memory and no
 // barriers. Values outside the grid (and, with DIR, on the boundary) are 0. A per-row variant (27 + 8
 // loads per row) took 35 us at 128^3 and a shared-memory plane-ring variant 40 us (instruction
-// bound); this one 30 us.
+// bound); this one 30 us (37 us with the Chronopoulos-Gear dots). Unpredicated loads with 0/1 weights
+// plus the coefficient-sum form of the product (K[i][j] = f[i ^ j], 35 instead of 72 FP operations)
+// measured 38 us and was dropped.
 // MODE (what the last block does with the reductions):
 //   MF_CG: q = A p with p.q -> alpha (standard CG; the probe check)
 //   MF_CGCG_INIT / MF_CGCG / MF_CGCG_REPLACE: w = A z with gamma = r.z, delta = z.w and r.r (the

@@ -25,3 +25,24 @@ def test_stationary_heat_equation_example(gdt):
     # second-order convergence of the vertex error (element-barycentre source lowering)
     assert errs[1] < errs[0] / 3.0
     assert errs[1] < 2e-3
+
+
+@pytest.mark.parametrize("flux,name", [("numerical_upwind_flux", "upwind"),
+                                       ("numerical_lax_friedrichs_flux", "lax_friedrichs"),
+                                       ("numerical_engquist_osher_flux", "engquist_osher")])
+def test_burgers_1d_fv_example(gdt, golden, flux, name):
+    # test/burgers/burgers__1d__explicit__fv.mini through the C++ facade (AdvectionFvOperator,
+    # estimate_dt_for_hyperbolic_system, ExplicitRungeKuttaTimeStepper): step counts and CFL of the
+    # reference table, mass conserved
+    exes = gdt._build.build_examples()
+    exe = [e for e in exes if e.endswith("burgers_1d_fv")][0]
+    case = golden["burgers_1d"][flux]
+    res = case["results"]
+    dt = 0.99 * case["setup"]["use_fixed_dt"]
+    for lvl, n in enumerate((16, 32)):
+        out = subprocess.run([exe, name, str(n), repr(dt)], capture_output=True, text=True, timeout=300,
+                             check=True).stdout.split()
+        assert out[0] == "cells" and int(out[1]) == n
+        assert int(out[3]) == res["quantity.num_timesteps"][lvl]
+        assert float("%.2e" % float(out[5])) == pytest.approx(res["quantity.CFL"][lvl], rel=1e-12)
+        assert float(out[7]) < 1e-14
