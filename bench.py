@@ -321,7 +321,10 @@ def run_gdt(args):
                      "achieved": by_kernel[dom]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": by_kernel[dom]["frac"], "bytes_per_launch": by_kernel[dom]["bytes_per_launch"],
                      "avg_launch_ms": by_kernel[dom]["avg_launch_ms"], "launches": by_kernel[dom]["launches"],
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)", "traffic": None},
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)", "traffic": None,
+                     "note": ("the inner iteration's working set stays L2-resident; the matrix-free operator is "
+                              "bound by instruction issue and load latency, not HBM "
+                              "(profiles/k_mf_column_128cube_ncu_full.md)") if inner == "matrix_free" else None},
         "roofline_by_kernel": by_kernel,
         "inner_operator": inner,
         "clocks": clk,
@@ -722,8 +725,8 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lognormal kappa per cell)",
         "config": {"workload": f"3D heat equation, {n}^3 Q1 hexes, lognormal kappa, f=1, Dirichlet 0; "
-                               "assemble + CG-Jacobi solve", "dofs": nd, "precision": "fp64",
-                   "tol_rel_residual": args.tol},
+                               "assemble + CG-Jacobi solve to 1e-8 rel error", "dofs": nd, "precision": "fp64",
+                   "tol_rel_residual": args.tol, "parallelism": "host threads"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "DoF/s", "cores": threads, "kind": "port",
                          "sample": f"per step: full assembly + {args.cpu_iters} CG-Jacobi iterations, scaled to "
