@@ -270,7 +270,9 @@ __device__ void cg_reliable(const BatchArgs& a, cg::cluster_group& cl, double* s
   }
 }
 
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BT) batch_kernel(BatchArgs a) {
+// at most 64 registers: four CTAs per SM, so twice as many clusters (problems in flight) as at the
+// 128 registers the compiler would otherwise use; the iterations are latency-bound at low occupancy
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BT, 4) batch_kernel(BatchArgs a) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = int(cl.block_rank());
   const long long cid = blockIdx.x / CL;
