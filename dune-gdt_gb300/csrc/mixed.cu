@@ -348,7 +348,8 @@ constexpr int MFX = 32, MFY = 8;  // vertex tile of the matrix-free kernel (x, y
 // loads per row) took 35 us at 128^3 and a shared-memory plane-ring variant 40 us (instruction
 // bound); this one 30 us (37 us with the Chronopoulos-Gear dots). Unpredicated loads with 0/1 weights
 // plus the coefficient-sum form of the product (K[i][j] = f[i ^ j], 35 instead of 72 FP operations)
-// measured 38 us and was dropped.
+// measured 38 us and was dropped, and so was a form that keeps only two planes and carries the lower
+// layer's contribution (64 registers, four blocks per SM: 38 us).
 // MODE (what the last block does with the reductions):
 //   MF_CG: q = A p with p.q -> alpha (standard CG; the probe check)
 //   MF_CGCG_INIT / MF_CGCG / MF_CGCG_REPLACE: w = A z with gamma = r.z, delta = z.w and r.r (the
