@@ -349,7 +349,8 @@ constexpr int MFX = 32, MFY = 8;  // vertex tile of the matrix-free kernel (x, y
 // bound); this one 30 us (37 us with the Chronopoulos-Gear dots). Unpredicated loads with 0/1 weights
 // plus the coefficient-sum form of the product (K[i][j] = f[i ^ j], 35 instead of 72 FP operations)
 // measured 38 us and was dropped, and so was a form that keeps only two planes and carries the lower
-// layer's contribution (64 registers, four blocks per SM: 38 us).
+// layer's contribution (64 registers, four blocks per SM: 38 us; with the next plane's loads issued
+// one step ahead, 80 registers: 40 us).
 // MODE (what the last block does with the reductions):
 //   MF_CG: q = A p with p.q -> alpha (standard CG; the probe check)
 //   MF_CGCG_INIT / MF_CGCG / MF_CGCG_REPLACE: w = A z with gamma = r.z, delta = z.w and r.r (the
