@@ -75,6 +75,12 @@ class Context:
     def kernel_launches(self):
         return int(self.lib.gdt_context_kernel_launches(self.handle))
 
+    def set_solver_launch(self, mode):
+        """Launch form of FP64 CG solves: 'auto' (persistent where the system fits in L2), 'graph'
+        (one kernel per step, CUDA graphs) or 'persistent' (one cooperative launch for all iterations)."""
+        self.call("gdt_context_set_solver_launch", {"auto": capi.SOLVER_LAUNCH_AUTO, "graph": capi.SOLVER_LAUNCH_GRAPH,
+                                                    "persistent": capi.SOLVER_LAUNCH_PERSISTENT}[mode])
+
 
 _default = {}
 
@@ -542,6 +548,10 @@ class MatrixOperator:
                       C.byref(info))
         self.last_solve_info = {"iterations": info.iterations, "refinements": info.refinements,
                                 "rel_residual": info.rel_residual, "converged": bool(info.converged)}
+        launch = int(capi.load().gdt_context_last_solver_launch(self.ctx.handle))
+        if launch:
+            self.last_solve_info["launch"] = {capi.SOLVER_LAUNCH_GRAPH: "graph",
+                                              capi.SOLVER_LAUNCH_PERSISTENT: "persistent"}[launch]
         if o.precision == capi.PRECISION_MIXED:
             kind = int(capi.load().gdt_matrix_mixed_operator(self.handle))
             self.last_solve_info["inner_operator"] = {0: "stencil", 1: "stencil_tiled", 2: "matrix_free"}.get(kind)

@@ -24,6 +24,7 @@ NUMFLUX_LAX_FRIEDRICHS, NUMFLUX_UPWIND, NUMFLUX_ENGQUIST_OSHER = 0, 1, 2
 FV_BOUNDARY_NONE, FV_BOUNDARY_EXTRAPOLATE, FV_BOUNDARY_DIRICHLET, FV_BOUNDARY_FLUX = 0, 1, 2, 3
 TIMESTEPPER_EXPLICIT_EULER, TIMESTEPPER_SSPRK2 = 0, 1
 MIXED_OPERATOR_STENCIL, MIXED_OPERATOR_STENCIL_TILED, MIXED_OPERATOR_MATRIX_FREE = 0, 1, 2
+SOLVER_LAUNCH_AUTO, SOLVER_LAUNCH_GRAPH, SOLVER_LAUNCH_PERSISTENT = 0, 1, 2
 
 
 class DiffusionDesc(C.Structure):
@@ -88,6 +89,8 @@ _SIGNATURES = {
     "gdt_context_last_error": (C.c_char_p, [P]),
     "gdt_context_kernel_launches": (C.c_int64, [P]),
     "gdt_context_set_timing": (C.c_int, [P, C.c_int]),
+    "gdt_context_set_solver_launch": (C.c_int, [P, C.c_int]),
+    "gdt_context_last_solver_launch": (C.c_int, [P]),
     "gdt_context_spmv_timing": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                           C.POINTER(C.c_int64), C.c_int]),
     "gdt_context_kernel_timing": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int]),

@@ -101,6 +101,14 @@ gdt_status gdt_context_set_timing(gdt_context ctx, int enable) {
   return GDT_OK;
 }
 
+gdt_status gdt_context_set_solver_launch(gdt_context ctx, int mode) {
+  if (!ctx || mode < GDT_SOLVER_LAUNCH_AUTO || mode > GDT_SOLVER_LAUNCH_PERSISTENT) return GDT_EINVAL;
+  ctx->solver_launch = mode;
+  return GDT_OK;
+}
+
+int gdt_context_last_solver_launch(gdt_context ctx) { return ctx ? ctx->last_solver_launch : 0; }
+
 gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp64_launches, double* fp32_ms,
                                    int64_t* fp32_launches, int reset) {
   if (!ctx) return GDT_EINVAL;

@@ -44,6 +44,8 @@ struct gdt_context_s {
   // kernel class (GDT_TIMING_*) are bracketed by CUDA events on the launching stream; durations
   // accumulate per class
   int timing = 0;
+  int solver_launch = 0;       // GDT_SOLVER_LAUNCH_* requested for FP64 CG
+  int last_solver_launch = 0;  // the form the last FP64 CG solve ran in
   std::vector<cudaEvent_t> events;  // pairs (start, stop)
   std::vector<int> event_kind;      // GDT_TIMING_* class of each pair
   size_t events_used = 0;

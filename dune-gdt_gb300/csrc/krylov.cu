@@ -27,7 +27,7 @@ struct KState {
   int iter, max_iter, converged, breakdown;
 };
 
-__device__ __forceinline__ bool stopped(const KState* st) { return *((volatile const int*)&st->converged) != 0; }
+__device__ __forceinline__ bool stopped(const KState* st) { return entry_flag(&st->converged) != 0; }
 
 // ---------------------------------------------------------------- generic pieces ---
 // y = A x; optional dot(w, y) -> st->hden / alpha (mode 1: CG alpha = rho / (p.Ap); mode 2: BiCGStab
@@ -601,6 +601,285 @@ void ilu_apply(gdt_context ctx, gdt_matrix m, const Ilu& f, const double* r, dou
 }
 
 
+// ------------------------------------------------- persistent CG for systems that fit in L2 ---
+// One cooperative launch runs every iteration of Jacobi-preconditioned (or plain) CG. The kernel
+// boundaries of the graph form become grid barriers, three per iteration: after q = A p, after the
+// x/r update, after the direction update. Every block reduces the per-block partial sums itself, in
+// block order, so all blocks hold bit-identical alpha, beta and convergence decisions without a
+// broadcast step. This pays where an iteration is bound by launch, ramp-up and tail latency rather
+// than bandwidth: matrices and vectors that stay in the 129 MB L2. The SpMV stages each warp's
+// contiguous CSR slice (32 rows, coalesced) in shared memory and gives every lane one row, so a pass
+// over the rows costs three dependent memory latencies (row bounds, slice, gathers). The matrix
+// and the Jacobi diagonal are read-only in the kernel (non-coherent loads); the vectors are written
+// by other blocks between barriers and read with plain loads, which the barrier's fences order.
+constexpr int PT = 256;                                  // threads per block
+constexpr unsigned long long kBarrierNs = 1000000000ull;  // longest wait at a grid barrier (1 s)
+
+struct PcgArgs {
+  int n;
+  const int* rp;
+  const int* col;
+  const double* val;
+  const double* dinv;
+  double* x;
+  double* r;
+  double* p;
+  double* q;
+  KState* st;
+  double* part;       // 3 * gridDim.x doubles: p.q | r.z, r.r per block
+  unsigned int* bar;  // arrivals at bar[0], generation at bar[kBarGen], fault (a wait ran out) at bar[kBarFault]
+};
+// the arrival counter, the generation the waiting blocks poll and the fault flag sit 4 KB apart, so
+// the polls and the arrivals do not queue at the same L2 slice
+constexpr int kBarGen = 1024, kBarFault = 2048;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier (all blocks are co-resident: cooperative launch). Thread 0 of a block reads the
+// generation, arrives, and waits for the last arrival to advance it; the waits are bounded by time
+// and by count, after which bar[2] is set and every block returns false from then on.
+__device__ bool pcg_sync(unsigned int* bar) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = bar + kBarGen;
+    volatile unsigned int* vfault = bar + kBarFault;
+    const unsigned int g = *vgen;
+    __threadfence();
+    int good = *vfault == 0u;
+    if (good) {
+      if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        atomicAdd(bar + kBarGen, 1u);
+      } else {
+        const unsigned long long t0 = global_ns();
+        unsigned int spins = 0;
+        while (*vgen == g) {
+          ++spins;
+          if ((spins & 255u) == 0) {
+            if (*vfault) {
+              good = 0;
+              break;
+            }
+            if (spins > (1u << 26) || global_ns() - t0 > kBarrierNs) {
+              atomicExch(bar + kBarFault, 1u);
+              good = 0;
+              break;
+            }
+          }
+          __nanosleep(100);
+        }
+      }
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// sum of the per-block partials in block order, the same in every block; result in every thread
+template <int NV>
+__device__ __forceinline__ void pcg_allreduce(const double* part, double (&v)[NV], double* red, double* bc) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < gridDim.x; b += PT) s += part[k * gridDim.x + b];
+    v[k] = s;
+  }
+  block_reduce<NV>(v, red);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) bc[k] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = bc[k];
+}
+
+// q = A p over the block's warps' rows (PL >= the longest row); returns this thread's share of p.q
+template <int PL>
+__device__ __forceinline__ double pcg_spmv(const PcgArgs& a, double* wv, int* wc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = gridDim.x * (PT / 32);
+  double pq = 0.0;
+  for (int r0 = (blockIdx.x * (PT / 32) + warp) * 32; r0 < a.n; r0 += nw * 32) {
+    const int row = r0 + lane;
+    const bool act = row < a.n;
+    const int rb = act ? __ldg(a.rp + row) : 0, re = act ? __ldg(a.rp + row + 1) : 0;
+    const double pr = act ? a.p[row] : 0.0;
+    const int last = (a.n - 1 - r0) < 31 ? (a.n - 1 - r0) : 31;
+    const int beg = __shfl_sync(0xffffffffu, rb, 0), end = __shfl_sync(0xffffffffu, re, last);
+    // the slice in chunks of 8 entries per lane (loads of a chunk in flight together)
+#pragma unroll
+    for (int j0 = 0; j0 < PL; j0 += 8) {
+      if (beg + j0 * 32 >= end) break;  // warp-uniform
+      double v[8];
+      int c[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int k = beg + (j0 + j) * 32 + lane;
+        v[j] = k < end ? __ldg(a.val + k) : 0.0;
+        c[j] = k < end ? __ldg(a.col + k) : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        wv[(j0 + j) * 32 + lane] = v[j];
+        wc[(j0 + j) * 32 + lane] = c[j];
+      }
+    }
+    __syncwarp();
+    const int off = rb - beg, len = re - rb;
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int t0 = 0; t0 < PL; t0 += 8) {
+      if (t0 >= len) break;
+#pragma unroll
+      for (int t = t0; t < t0 + 8; t += 2) {
+        if (t < len) s0 = fma(wv[off + t], a.p[wc[off + t]], s0);
+        if (t + 1 < len) s1 = fma(wv[off + t + 1], a.p[wc[off + t + 1]], s1);
+      }
+    }
+    const double s = s0 + s1;
+    if (act) {
+      a.q[row] = s;
+      pq = fma(pr, s, pq);
+    }
+    __syncwarp();
+  }
+  return pq;
+}
+
+template <int PL>
+__global__ void __launch_bounds__(PT) k_pcg_persistent(PcgArgs a) {
+  extern __shared__ __align__(16) unsigned char pcg_smem[];
+  __shared__ double red[2 * 32];
+  __shared__ double bc[2];
+  const int warp = threadIdx.x >> 5;
+  double* wv = reinterpret_cast<double*>(pcg_smem) + warp * 32 * PL;
+  int* wc = reinterpret_cast<int*>(reinterpret_cast<double*>(pcg_smem) + (PT / 32) * 32 * PL) + warp * 32 * PL;
+  KState* st = a.st;
+  if (entry_flag(&st->converged)) return;
+  double rho = st->rho, alpha = st->alpha, beta = st->beta, rr = st->rr;
+  const double stop = st->tol2 * st->rr0;
+  const int max_iter = st->max_iter;
+  int iter = st->iter, conv = 0, brk = 0;
+  const int nb = gridDim.x;
+  const int stride = nb * PT;
+  while (true) {
+    // q = A p, p.q -> alpha
+    double v1[1] = {pcg_spmv<PL>(a, wv, wc)};
+    block_reduce<1>(v1, red);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = v1[0];
+    if (!pcg_sync(a.bar)) break;
+    pcg_allreduce<1>(a.part, v1, red, bc);
+    alpha = rho / v1[0];
+    if (!(v1[0] > 0.0) || !isfinite(v1[0])) {
+      brk = conv = 1;
+      break;
+    }
+    // x += alpha p, r -= alpha q; r.z (z = dinv r) and r.r
+    double v2[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * PT + threadIdx.x; i < a.n; i += stride) {
+      a.x[i] = fma(alpha, a.p[i], a.x[i]);
+      const double ri = fma(-alpha, a.q[i], a.r[i]);
+      a.r[i] = ri;
+      v2[0] = fma(ri, __ldg(a.dinv + i) * ri, v2[0]);
+      v2[1] = fma(ri, ri, v2[1]);
+    }
+    block_reduce<2>(v2, red);
+    if (threadIdx.x == 0) {
+      a.part[nb + blockIdx.x] = v2[0];
+      a.part[2 * nb + blockIdx.x] = v2[1];
+    }
+    if (!pcg_sync(a.bar)) break;
+    pcg_allreduce<2>(a.part + nb, v2, red, bc);
+    beta = v2[0] / rho;
+    rho = v2[0];
+    rr = v2[1];
+    iter += 1;
+    if (rr <= stop || iter >= max_iter) conv = 1;
+    if (!isfinite(rr)) brk = conv = 1;
+    if (conv) break;
+    // p = dinv r + beta p
+    for (int i = blockIdx.x * PT + threadIdx.x; i < a.n; i += stride)
+      a.p[i] = fma(beta, a.p[i], __ldg(a.dinv + i) * a.r[i]);
+    if (!pcg_sync(a.bar)) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->rho = rho;
+    st->alpha = alpha;
+    st->beta = beta;
+    st->rr = rr;
+    st->iter = iter;
+    st->breakdown = brk;
+    st->converged = 1;
+  }
+}
+
+// the matrix and the solver's vectors (x, b, r, p, q, dinv) within this many bytes stay in L2
+constexpr double kPersistentL2Bytes = 96.0e6;
+
+bool persistent_applies(gdt_context ctx, gdt_matrix m) {
+  if (ctx->timing || ctx->solver_launch == GDT_SOLVER_LAUNCH_GRAPH) return false;
+  if (m->max_row < 1 || m->max_row > 32 || m->rows < 1) return false;
+  if (ctx->solver_launch == GDT_SOLVER_LAUNCH_PERSISTENT) return true;
+  const double bytes = 12.0 * double(m->nnz) + 4.0 * double(m->rows + 1) + 48.0 * double(m->rows);
+  return bytes <= kPersistentL2Bytes;
+}
+
+// Runs the iterations after residual_init; the caller reads the final state from st.
+gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, double* p, double* q,
+                          const double* dinv, KState* st, cudaStream_t s) {
+  const bool wide = m->max_row > 16;
+  const void* fn = wide ? reinterpret_cast<const void*>(&k_pcg_persistent<32>)
+                        : reinterpret_cast<const void*>(&k_pcg_persistent<16>);
+  const size_t smem = size_t(PT / 32) * 32 * (wide ? 32 : 16) * (sizeof(double) + sizeof(int));
+  int dev = 0, coop = 0, per_sm = 0;
+  GDT_TRY_CUDA(ctx, cudaGetDevice(&dev));
+  GDT_TRY_CUDA(ctx, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: no cooperative launch on this device");
+  GDT_TRY_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, smem));
+  if (per_sm < 1) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: kernel does not fit an SM");
+  per_sm = std::min(per_sm, 4);
+  int blocks = per_sm * ctx->num_sms;
+  // no more blocks than warps have rows to stage
+  const int needed = int((m->rows + PT - 1) / PT);
+  if (needed < blocks) blocks = std::max(1, needed);
+  if (3 * blocks > kScratchDoubles) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: grid too large");
+  PcgArgs a;
+  a.n = int(m->rows);
+  a.rp = m->rp;
+  a.col = m->col;
+  a.val = m->val;
+  a.dinv = dinv;
+  a.x = x;
+  a.r = r;
+  a.p = p;
+  a.q = q;
+  a.st = st;
+  a.part = ctx->scratch;
+  // the barrier words live in the upper half of the scratch (the partials use its start)
+  a.bar = reinterpret_cast<unsigned int*>(ctx->scratch + kScratchDoubles / 2);
+  if (3 * blocks > kScratchDoubles / 2) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: grid too large");
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar, 0, sizeof(unsigned int), s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarGen, 0, sizeof(unsigned int), s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarFault, 0, sizeof(unsigned int), s));
+  void* args[] = {&a};
+  GDT_TRY_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(PT), args, smem, s));
+  ctx->launches++;
+  unsigned int fault = 0;
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fault, a.bar + kBarFault, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+  if (fault) return fail(ctx, GDT_ECUDA, "persistent solver: a grid barrier wait ran out");
+  return GDT_OK;
+}
+
 }  // namespace
 
 __global__ void k_fill(int n, double* __restrict__ v, double value) {
@@ -706,6 +985,7 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
     }
   } cleanup{own};
   const int n = int(m->rows);
+  ctx->last_solver_launch = 0;
   Launch L;
   L.ctx = ctx;
   L.n = n;
@@ -776,9 +1056,16 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
           GDT_TRY_CUDA(ctx, cudaMemcpyAsync(one, ones.data(), vb, cudaMemcpyHostToDevice, s));
           GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
         }
-        GDT_CHECK(ctx, tune_cg(ctx, m, L, s));
-        L.sched = m->cg_sched;
+        const bool persistent = persistent_applies(ctx, m);
+        if (!persistent) {
+          GDT_CHECK(ctx, tune_cg(ctx, m, L, s));
+          L.sched = m->cg_sched;
+        }
         residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
+        ctx->last_solver_launch = persistent ? GDT_SOLVER_LAUNCH_PERSISTENT : GDT_SOLVER_LAUNCH_GRAPH;
+        if (persistent) {
+          GDT_CHECK(ctx, pcg_persistent(ctx, m, x, r, p, q, one, st, s));
+        } else {
         // pairs of rows per thread when every vector is 16-byte aligned (the solver's own are; x is
         // the caller's)
         const bool pairs = (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
@@ -800,6 +1087,7 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
           timing_end(ctx, s);
           ctx->launches += 2;
         }));
+        }
       } else {
         double* z = (double*)alloc(vb);
         if (!z) return fail(ctx, GDT_ENOMEM, "solver vectors");

@@ -287,6 +287,12 @@ inline bool schedule_valid(int sched, int max_row) {
   return PL == 0 || (max_row > 0 && max_row <= PL);
 }
 
+// Solver flags (converged, replacement due, iteration numbers) are written by the last block of an
+// earlier kernel and read at the entry of later ones. A weak load cached in L1 sees them, because kernel
+// boundaries order memory; a volatile load would send one L2 request per warp to the same address and
+// serialise on that L2 slice (tens of thousands of requests per launch of a large grid).
+__device__ __forceinline__ int entry_flag(const int* p) { return __ldca(p); }
+
 // Two-level deterministic reduction of NV partial sums over the whole grid: every block writes its
 // partials, the last block to arrive (ticket) sums them in block order. Returns true in the last block;
 // the totals are then in v[] of thread 0. partials needs NV * gridDim.x doubles.

@@ -50,7 +50,7 @@ struct MState {
   int fault;  // a bounded device wait ran out (tile loads of the 3D SpMV)
 };
 
-__device__ __forceinline__ bool mstopped(const MState* st) { return *((volatile const int*)&st->converged) != 0; }
+__device__ __forceinline__ bool mstopped(const MState* st) { return entry_flag(&st->converged) != 0; }
 
 struct Stencil {
   int nu;               // upper slots
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(MFX* MFY) k_mf_column(MfOp op, int tiles_x, in
   if (mstopped(st)) return;
   // after a residual replacement only (outside graphs the reliable-update kernels run every iteration
   // and exit early when there is nothing to do)
-  if (MODE == MF_CGCG_REPLACE && *((volatile const int*)&st->replaced_iter) != *((volatile const int*)&st->iter))
+  if (MODE == MF_CGCG_REPLACE && entry_flag(&st->replaced_iter) != entry_flag(&st->iter))
     return;
   const int tx = threadIdx.x % MFX, ty = threadIdx.x / MFX;
   const int bt = blockIdx.x % (tiles_x * tiles_y), bz = blockIdx.x / (tiles_x * tiles_y);
@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(TH) k_mf_compare(int n, Pitch pt, const int* _
 // reliable update, part 1: x64 += x32, x32 = 0
 __global__ void __launch_bounds__(TH) k_mx_accumulate(int n, Pitch pt, double* __restrict__ x, float* __restrict__ x32,
                                                      const MState* st) {
-  if (mstopped(st) || !*((volatile const int*)&st->flag)) return;
+  if (mstopped(st) || !entry_flag(&st->flag)) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const long long ip = pt.of(i);
     x[i] += double(x32[ip]);
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(TH) k_mx_true_residual(int n, Pitch pt, const 
                                                         float* __restrict__ r32, const float* __restrict__ dinv,
                                                         MState* st, double* partials, unsigned int* ticket,
                                                         float* __restrict__ z32) {
-  if (mstopped(st) || !*((volatile const int*)&st->flag)) return;
+  if (mstopped(st) || !entry_flag(&st->flag)) return;
   double a0 = 0.0, a1 = 0.0;
   for_rows_csr<G, PL, double>(n, rp, col, val, x, [&](int row, bool leader, double s) {
     if (leader) {

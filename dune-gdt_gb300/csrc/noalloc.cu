@@ -44,7 +44,7 @@ struct NaScratch {
 static __device__ __align__(256) NaScratch g_noalloc_scratch;
 
 __device__ __forceinline__ bool na_stopped(const NaScratch* s) {
-  return *((volatile const int*)&s->state.converged) != 0;
+  return entry_flag(&s->state.converged) != 0;
 }
 
 // r = b - A x, dinv = 1 / diag, p = dinv r; rho = r.p, rr0 = r.r

@@ -97,6 +97,20 @@ gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp
  * reset by gdt_context_spmv_timing with reset = 1) */
 gdt_status gdt_context_kernel_timing(gdt_context ctx, int kind, double* ms, int64_t* launches, int reset);
 
+/* How gdt_solve runs FP64 CG with Jacobi or no preconditioner (no reference counterpart: the launch
+ * form of the device solver). GRAPH: one kernel per step (SpMV, update, direction), iterations
+ * captured in CUDA graphs. PERSISTENT: one cooperative launch runs every iteration, with grid
+ * barriers between the steps; it takes matrices whose rows hold at most 32 entries. AUTO (default):
+ * PERSISTENT where the matrix and the solver vectors fit in L2 (there an iteration is bound by
+ * launch and synchronisation latency, not by bandwidth), GRAPH otherwise. Timing mode always runs
+ * GRAPH's kernels launched one by one. */
+#define GDT_SOLVER_LAUNCH_AUTO 0
+#define GDT_SOLVER_LAUNCH_GRAPH 1
+#define GDT_SOLVER_LAUNCH_PERSISTENT 2
+gdt_status gdt_context_set_solver_launch(gdt_context ctx, int mode);
+/* launch form (GRAPH or PERSISTENT) of the context's last FP64 CG solve; 0 before the first */
+int gdt_context_last_solver_launch(gdt_context ctx);
+
 /* --------------------------------------------------------------------- grid --- */
 /* make_cube_grid(lower_left, upper_right, num_elements): equidistant YaspGrid-like cube grid
  * (elements and vertices lexicographic, x fastest) or its Kuhn split into d! simplices per cube

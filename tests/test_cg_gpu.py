@@ -147,6 +147,71 @@ def test_solvers_match_direct(gdt, oracle, solver, precond):
     assert abs(info["iterations"] - it) <= max(2, 0.05 * it)
 
 
+def _solve_in(op, rhs, launch, opts):
+    op.ctx.set_solver_launch(launch)
+    try:
+        x = op.apply_inverse(rhs, opts=opts).clone()
+    finally:
+        op.ctx.set_solver_launch("auto")
+    return x, dict(op.last_solve_info)
+
+
+def _scipy(op):
+    import scipy.sparse as sp
+
+    rp, col, val = (t.cpu().numpy() for t in op.csr())
+    return sp.csr_matrix((val, col, rp), shape=op.shape)
+
+
+@pytest.mark.parametrize("case", ["p1_2d", "q1_3d", "swipdg_2d", "q1_1d"])
+@pytest.mark.parametrize("precond", ["jacobi", "none"])
+def test_persistent_cg_matches_graph_and_direct(gdt, oracle, case, precond):
+    # FP64 CG in one cooperative launch (grid barriers between the steps, every block reducing the
+    # per-block partials itself) against the graph form of the same iteration and a direct solve;
+    # rows of 3 (1D), 7 (P1 triangles), 12 (SWIPDG) and 27 (Q1 hexahedra) entries
+    dim, n, simplex, dg = {"p1_2d": (2, [40, 33], True, False), "q1_3d": (3, [9, 8, 7], False, False),
+                           "swipdg_2d": (2, [12, 9], True, True), "q1_1d": (1, [1001], False, False)}[case]
+    g = gdt.make_cube_grid([0.0] * dim, [1.0] * dim, n, simplex=simplex)
+    kappa = torch.exp(torch.tensor(np.random.default_rng(8).standard_normal(g.num_elements), device="cuda"))
+    prob = gdt.DiffusionProblem(g, dg=dg)
+    prob.assemble(kappa)
+    op, rhs = prob.op, prob.rhs
+    opts = {"tol": 1e-12, "precond": precond, "max_iter": 100000}
+    xg, ig = _solve_in(op, rhs, "graph", opts)
+    xp, ip = _solve_in(op, rhs, "persistent", opts)
+    xa, ia = _solve_in(op, rhs, "auto", opts)
+    assert ig["launch"] == "graph" and ip["launch"] == "persistent" and ia["launch"] == "persistent"
+    assert ig["converged"] and ip["converged"]
+    assert abs(ig["iterations"] - ip["iterations"]) <= max(2, 0.02 * ig["iterations"])
+    assert rel_err(xp.cpu().numpy(), xg.cpu().numpy()) < 1e-9
+    xd = spl.spsolve(_scipy(op).tocsc(), rhs.cpu().numpy())
+    assert rel_err(xp.cpu().numpy(), xd) < 1e-9
+    # the reductions are deterministic: the same iterates launch after launch
+    assert ia["iterations"] == ip["iterations"] and torch.equal(xa, xp)
+
+
+def test_persistent_cg_reports_non_convergence_and_skips_long_rows(gdt, oracle):
+    op, rhs, A, b = _heat_problem(gdt, oracle, 2, [30, 30], False)
+    op.ctx.set_solver_launch("persistent")
+    try:
+        with pytest.raises(gdt.GdtError) as e:
+            op.apply_inverse(rhs, opts={"tol": 1e-12, "max_iter": 3})
+        assert e.value.status == gdt._capi.ENOCONV
+        # Q2 hexahedra: rows of up to 125 entries run in the graph form even when persistent is asked for
+        g = gdt.make_cube_grid([0.0] * 3, [1.0] * 3, [4, 3, 5])
+        space = gdt.ContinuousLagrangeSpace(g, 2)
+        op2 = gdt.MatrixOperator(g, space)
+        op2 += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(
+            torch.ones(g.num_elements, dtype=torch.float64, device="cuda")))
+        rhs2 = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+        op2.assemble(rhs=rhs2, force=1.0, dirichlet=True)
+        x2 = op2.apply_inverse(rhs2, opts={"tol": 1e-12})
+        assert op2.last_solve_info["launch"] == "graph" and op2.last_solve_info["converged"]
+        assert rel_err(x2.cpu().numpy(), spl.spsolve(_scipy(op2).tocsc(), rhs2.cpu().numpy())) < 1e-9
+    finally:
+        op.ctx.set_solver_launch("auto")
+
+
 def test_mixed_precision_refinement_reaches_fp64_accuracy(gdt, oracle):
     op, rhs, A, b = _heat_problem(gdt, oracle, 3, [12, 10, 14], False)
     xd = spl.spsolve(A.to_scipy().tocsc(), b)
