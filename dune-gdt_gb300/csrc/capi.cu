@@ -295,6 +295,9 @@ gdt_status gdt_matrix_destroy(gdt_matrix m) {
   if (!m) return GDT_EINVAL;
   ho_matrix_free(static_cast<HoMatrix*>(m->ho));
   if (m->mf_kappa) cudaFree(m->mf_kappa);
+  if (m->sell_meta) cudaFree(m->sell_meta);
+  if (m->sell_col) cudaFree(m->sell_col);
+  if (m->sell_val) cudaFree(m->sell_val);
   if (m->rp) cudaFree(m->rp);
   if (m->col) cudaFree(m->col);
   if (m->val) cudaFree(m->val);

@@ -83,6 +83,13 @@ struct gdt_matrix_s {
   // 3D Q1 Laplace assemblies: the element coefficients in FP32 and the reference element stiffness
   // (corner-bit indexing), for the matrix-free inner operator of the mixed-precision solver
   float* mf_kappa = nullptr;
+  // SELL-32 copy for the persistent solver: slices of 32 rows stored column-major, padded to the
+  // slice's longest row; (offset, width) per slice (from the pattern, built once), values and
+  // columns (refreshed at every persistent solve)
+  int* sell_meta = nullptr;
+  int* sell_col = nullptr;
+  double* sell_val = nullptr;
+  long long sell_len = 0;
   float mf_K[64] = {};
   int mf_valid = 0;      // the values are exactly that assembly (cleared by any other value change)
   int mf_dirichlet = 0;  // with Dirichlet unit rows and columns

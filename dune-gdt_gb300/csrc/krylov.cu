@@ -607,19 +607,26 @@ void ilu_apply(gdt_context ctx, gdt_matrix m, const Ilu& f, const double* r, dou
 // x/r update, after the direction update. Every block reduces the per-block partial sums itself, in
 // block order, so all blocks hold bit-identical alpha, beta and convergence decisions without a
 // broadcast step. This pays where an iteration is bound by launch, ramp-up and tail latency rather
-// than bandwidth: matrices and vectors that stay in the 129 MB L2. The SpMV stages each warp's
-// contiguous CSR slice (32 rows, coalesced) in shared memory and gives every lane one row, so a pass
-// over the rows costs three dependent memory latencies (row bounds, slice, gathers). The matrix
+// than bandwidth: matrices and vectors that stay in the 129 MB L2. The Chronopoulos-Gear form (one
+// reduction and two barriers per iteration) measured slower here (277 against 250 ms for the SWIPDG
+// system of 256^2 squares) and needed up to 65 % more iterations on badly conditioned 1D and 2D
+// systems, so the iteration stays the standard one of the graph form. The SpMV reads a SELL-32 copy
+// of the matrix (slices of 32 rows stored column-major, padded to the slice's longest row): a lane
+// owns one row and reads its entries with loads that are coalesced across the warp, so a pass over
+// 32 rows costs two dependent memory latencies (entries, gathers) and no shared memory. (Staging each
+// warp's CSR slice in shared memory instead cost three latencies per pass and 8-way bank conflicts
+// when the lanes read their rows: 17.6 us of a 43 us iteration on that SWIPDG system.) The matrix
 // and the Jacobi diagonal are read-only in the kernel (non-coherent loads); the vectors are written
 // by other blocks between barriers and read with plain loads, which the barrier's fences order.
-constexpr int PT = 256;                                  // threads per block
+constexpr int PT = 1024;                                 // threads per block (one block per SM)
 constexpr unsigned long long kBarrierNs = 1000000000ull;  // longest wait at a grid barrier (1 s)
 
 struct PcgArgs {
   int n;
-  const int* rp;
-  const int* col;
-  const double* val;
+  int nslices;
+  const int2* meta;   // SELL-32 (offset, width) per slice
+  const int* col;     // SELL-32 columns
+  const double* val;  // SELL-32 values
   const double* dinv;
   double* x;
   double* r;
@@ -627,7 +634,7 @@ struct PcgArgs {
   double* q;
   KState* st;
   double* part;       // 3 * gridDim.x doubles: p.q | r.z, r.r per block
-  unsigned int* bar;  // arrivals at bar[0], generation at bar[kBarGen], fault (a wait ran out) at bar[kBarFault]
+  unsigned int* bar;  // 64-bit arrival count at bar[0], generation at bar[kBarGen], fault at bar[kBarFault]
 };
 // the arrival counter, the generation the waiting blocks poll and the fault flag sit 4 KB apart, so
 // the polls and the arrivals do not queue at the same L2 slice
@@ -639,27 +646,29 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Grid barrier (all blocks are co-resident: cooperative launch). Thread 0 of a block reads the
-// generation, arrives, and waits for the last arrival to advance it; the waits are bounded by time
-// and by count, after which bar[2] is set and every block returns false from then on.
-__device__ bool pcg_sync(unsigned int* bar) {
+// Grid barrier (all blocks are co-resident: cooperative launch). Barrier number `epoch` (counted by
+// thread 0 of every block) is complete when the 64-bit arrival count reaches epoch * blocks; the last
+// block to arrive publishes the epoch as the generation the others poll (no reset of the count, so
+// the release is one store after the arrival). The waits are bounded by time and by count, after
+// which the fault flag is set and every block returns false from then on.
+__device__ bool pcg_sync(unsigned int* bar, unsigned int& epoch) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
+    ++epoch;
     volatile unsigned int* vgen = bar + kBarGen;
     volatile unsigned int* vfault = bar + kBarFault;
-    const unsigned int g = *vgen;
     __threadfence();
     int good = *vfault == 0u;
     if (good) {
-      if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-        atomicExch(bar, 0u);
+      const unsigned long long target = (unsigned long long)epoch * gridDim.x;
+      if (atomicAdd(reinterpret_cast<unsigned long long*>(bar), 1ull) == target - 1) {
         __threadfence();
-        atomicAdd(bar + kBarGen, 1u);
+        atomicExch(bar + kBarGen, epoch);
       } else {
         const unsigned long long t0 = global_ns();
         unsigned int spins = 0;
-        while (*vgen == g) {
+        while (*vgen != epoch) {
           ++spins;
           if ((spins & 255u) == 0) {
             if (*vfault) {
@@ -672,7 +681,7 @@ __device__ bool pcg_sync(unsigned int* bar) {
               break;
             }
           }
-          __nanosleep(100);
+          __nanosleep(40);
         }
       }
     }
@@ -701,47 +710,44 @@ __device__ __forceinline__ void pcg_allreduce(const double* part, double (&v)[NV
   for (int k = 0; k < NV; ++k) v[k] = bc[k];
 }
 
-// q = A p over the block's warps' rows (PL >= the longest row); returns this thread's share of p.q
-template <int PL>
-__device__ __forceinline__ double pcg_spmv(const PcgArgs& a, double* wv, int* wc) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// q = A p over the warp's slices (rows of at most 32 entries); returns this thread's share of p.q.
+// The slices of a warp are the same in every iteration: lane m holds the (offset, width) of the
+// warp's m-th slice, so a pass gets them by a shuffle instead of a load.
+__device__ __forceinline__ double pcg_spmv(const PcgArgs& a, int2 mymeta) {
+  const int lane = threadIdx.x & 31;
   const int nw = gridDim.x * (PT / 32);
   double pq = 0.0;
-  for (int r0 = (blockIdx.x * (PT / 32) + warp) * 32; r0 < a.n; r0 += nw * 32) {
-    const int row = r0 + lane;
-    const bool act = row < a.n;
-    const int rb = act ? __ldg(a.rp + row) : 0, re = act ? __ldg(a.rp + row + 1) : 0;
-    const double pr = act ? a.p[row] : 0.0;
-    const int last = (a.n - 1 - r0) < 31 ? (a.n - 1 - r0) : 31;
-    const int beg = __shfl_sync(0xffffffffu, rb, 0), end = __shfl_sync(0xffffffffu, re, last);
-    // the slice in chunks of 8 entries per lane (loads of a chunk in flight together)
-#pragma unroll
-    for (int j0 = 0; j0 < PL; j0 += 8) {
-      if (beg + j0 * 32 >= end) break;  // warp-uniform
-      double v[8];
-      int c[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int k = beg + (j0 + j) * 32 + lane;
-        v[j] = k < end ? __ldg(a.val + k) : 0.0;
-        c[j] = k < end ? __ldg(a.col + k) : 0;
-      }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        wv[(j0 + j) * 32 + lane] = v[j];
-        wc[(j0 + j) * 32 + lane] = c[j];
-      }
+  int m = 0;
+  for (int slice = blockIdx.x * (PT / 32) + (threadIdx.x >> 5); slice < a.nslices; slice += nw, ++m) {
+    int2 md;
+    if (m < 32) {
+      md.x = __shfl_sync(0xffffffffu, mymeta.x, m);
+      md.y = __shfl_sync(0xffffffffu, mymeta.y, m);
+    } else {
+      md = __ldg(a.meta + slice);
     }
-    __syncwarp();
-    const int off = rb - beg, len = re - rb;
+    const int row = slice * 32 + lane;
+    const bool act = row < a.n;
+    const double pr = act ? a.p[row] : 0.0;
+    const double* v = a.val + md.x + lane;
+    const int* c = a.col + md.x + lane;
     double s0 = 0.0, s1 = 0.0;
 #pragma unroll
-    for (int t0 = 0; t0 < PL; t0 += 8) {
-      if (t0 >= len) break;
+    for (int t0 = 0; t0 < 32; t0 += 12) {
+      if (t0 < md.y) {  // warp-uniform
+        double vv[12];
+        int cc[12];
 #pragma unroll
-      for (int t = t0; t < t0 + 8; t += 2) {
-        if (t < len) s0 = fma(wv[off + t], a.p[wc[off + t]], s0);
-        if (t + 1 < len) s1 = fma(wv[off + t + 1], a.p[wc[off + t + 1]], s1);
+        for (int j = 0; j < 12; ++j) {
+          const bool in = t0 + j < md.y;
+          vv[j] = in ? __ldg(v + (t0 + j) * 32) : 0.0;
+          cc[j] = in ? __ldg(c + (t0 + j) * 32) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 12; j += 2) {
+          if (t0 + j < md.y) s0 = fma(vv[j], a.p[cc[j]], s0);
+          if (t0 + j + 1 < md.y) s1 = fma(vv[j + 1], a.p[cc[j + 1]], s1);
+        }
       }
     }
     const double s = s0 + s1;
@@ -749,19 +755,18 @@ __device__ __forceinline__ double pcg_spmv(const PcgArgs& a, double* wv, int* wc
       a.q[row] = s;
       pq = fma(pr, s, pq);
     }
-    __syncwarp();
   }
   return pq;
 }
 
-template <int PL>
-__global__ void __launch_bounds__(PT) k_pcg_persistent(PcgArgs a) {
-  extern __shared__ __align__(16) unsigned char pcg_smem[];
+__global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
   __shared__ double red[2 * 32];
   __shared__ double bc[2];
-  const int warp = threadIdx.x >> 5;
-  double* wv = reinterpret_cast<double*>(pcg_smem) + warp * 32 * PL;
-  int* wc = reinterpret_cast<int*>(reinterpret_cast<double*>(pcg_smem) + (PT / 32) * 32 * PL) + warp * 32 * PL;
+  int2 mymeta = make_int2(0, 0);
+  {
+    const int slice = blockIdx.x * (PT / 32) + (threadIdx.x >> 5) + (threadIdx.x & 31) * gridDim.x * (PT / 32);
+    if (slice < a.nslices) mymeta = __ldg(a.meta + slice);
+  }
   KState* st = a.st;
   if (entry_flag(&st->converged)) return;
   double rho = st->rho, alpha = st->alpha, beta = st->beta, rr = st->rr;
@@ -770,12 +775,13 @@ __global__ void __launch_bounds__(PT) k_pcg_persistent(PcgArgs a) {
   int iter = st->iter, conv = 0, brk = 0;
   const int nb = gridDim.x;
   const int stride = nb * PT;
+  unsigned int epoch = 0;
   while (true) {
     // q = A p, p.q -> alpha
-    double v1[1] = {pcg_spmv<PL>(a, wv, wc)};
+    double v1[1] = {pcg_spmv(a, mymeta)};
     block_reduce<1>(v1, red);
     if (threadIdx.x == 0) a.part[blockIdx.x] = v1[0];
-    if (!pcg_sync(a.bar)) break;
+    if (!pcg_sync(a.bar, epoch)) break;
     pcg_allreduce<1>(a.part, v1, red, bc);
     alpha = rho / v1[0];
     if (!(v1[0] > 0.0) || !isfinite(v1[0])) {
@@ -783,20 +789,38 @@ __global__ void __launch_bounds__(PT) k_pcg_persistent(PcgArgs a) {
       break;
     }
     // x += alpha p, r -= alpha q; r.z (z = dinv r) and r.r
+    // (three elements per thread and pass, all their loads issued before the first store)
     double v2[2] = {0.0, 0.0};
-    for (int i = blockIdx.x * PT + threadIdx.x; i < a.n; i += stride) {
-      a.x[i] = fma(alpha, a.p[i], a.x[i]);
-      const double ri = fma(-alpha, a.q[i], a.r[i]);
-      a.r[i] = ri;
-      v2[0] = fma(ri, __ldg(a.dinv + i) * ri, v2[0]);
-      v2[1] = fma(ri, ri, v2[1]);
+    for (int i0 = blockIdx.x * PT + threadIdx.x; i0 < a.n; i0 += 3 * stride) {
+      double pv[3], qv[3], xv[3], rv[3], dv[3];
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int i = i0 + u * stride;
+        const bool in = i < a.n;
+        pv[u] = in ? a.p[i] : 0.0;
+        qv[u] = in ? a.q[i] : 0.0;
+        xv[u] = in ? a.x[i] : 0.0;
+        rv[u] = in ? a.r[i] : 0.0;
+        dv[u] = in ? __ldg(a.dinv + i) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int i = i0 + u * stride;
+        if (i < a.n) {
+          a.x[i] = fma(alpha, pv[u], xv[u]);
+          const double ri = fma(-alpha, qv[u], rv[u]);
+          a.r[i] = ri;
+          v2[0] = fma(ri, dv[u] * ri, v2[0]);
+          v2[1] = fma(ri, ri, v2[1]);
+        }
+      }
     }
     block_reduce<2>(v2, red);
     if (threadIdx.x == 0) {
       a.part[nb + blockIdx.x] = v2[0];
       a.part[2 * nb + blockIdx.x] = v2[1];
     }
-    if (!pcg_sync(a.bar)) break;
+    if (!pcg_sync(a.bar, epoch)) break;
     pcg_allreduce<2>(a.part + nb, v2, red, bc);
     beta = v2[0] / rho;
     rho = v2[0];
@@ -806,9 +830,23 @@ __global__ void __launch_bounds__(PT) k_pcg_persistent(PcgArgs a) {
     if (!isfinite(rr)) brk = conv = 1;
     if (conv) break;
     // p = dinv r + beta p
-    for (int i = blockIdx.x * PT + threadIdx.x; i < a.n; i += stride)
-      a.p[i] = fma(beta, a.p[i], __ldg(a.dinv + i) * a.r[i]);
-    if (!pcg_sync(a.bar)) break;
+    for (int i0 = blockIdx.x * PT + threadIdx.x; i0 < a.n; i0 += 3 * stride) {
+      double pv[3], rv[3], dv[3];
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int i = i0 + u * stride;
+        const bool in = i < a.n;
+        pv[u] = in ? a.p[i] : 0.0;
+        rv[u] = in ? a.r[i] : 0.0;
+        dv[u] = in ? __ldg(a.dinv + i) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int i = i0 + u * stride;
+        if (i < a.n) a.p[i] = fma(beta, pv[u], dv[u] * rv[u]);
+      }
+    }
+    if (!pcg_sync(a.bar, epoch)) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->rho = rho;
@@ -819,6 +857,81 @@ __global__ void __launch_bounds__(PT) k_pcg_persistent(PcgArgs a) {
     st->breakdown = brk;
     st->converged = 1;
   }
+}
+
+// SELL-32 widths: one warp per slice, the longest row of its 32
+__global__ void k_sell_width(int n, int nslices, const int* __restrict__ rp, int* __restrict__ width) {
+  const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (slice >= nslices) return;
+  const int row = slice * 32 + (threadIdx.x & 31);
+  const int len = row < n ? rp[row + 1] - rp[row] : 0;
+  const int w = __reduce_max_sync(0xffffffffu, len);
+  if ((threadIdx.x & 31) == 0) width[slice] = w;
+}
+
+// SELL-32 values and columns from the CSR arrays; padding entries are 0 * p[row] (row 0 past the end)
+__global__ void k_sell_fill(int n, int nslices, const int* __restrict__ rp, const int* __restrict__ col,
+                            const double* __restrict__ val, const int2* __restrict__ meta, int* __restrict__ scol,
+                            double* __restrict__ sval) {
+  const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (slice >= nslices) return;
+  const int lane = threadIdx.x & 31;
+  const int row = slice * 32 + lane;
+  const int2 md = meta[slice];
+  const int beg = row < n ? rp[row] : 0, len = row < n ? rp[row + 1] - beg : 0;
+  for (int t = 0; t < md.y; ++t) {
+    const long long k = md.x + (long long)t * 32 + lane;
+    scol[k] = t < len ? col[beg + t] : (row < n ? row : 0);
+    sval[k] = t < len ? val[beg + t] : 0.0;
+  }
+}
+
+// Builds the slice table once per matrix (the pattern never changes) and copies the current values.
+gdt_status sell_prepare(gdt_context ctx, gdt_matrix m, cudaStream_t s) {
+  const int n = int(m->rows);
+  const int nslices = (n + 31) / 32;
+  const int blocks = (nslices * 32 + 255) / 256;
+  if (!m->sell_meta) {
+    int* width = nullptr;
+    GDT_TRY_CUDA(ctx, cudaMalloc(&width, sizeof(int) * nslices));
+    k_sell_width<<<blocks, 256, 0, s>>>(n, nslices, m->rp, width);
+    ctx->launches++;
+    std::vector<int> w(nslices);
+    cudaError_t e = cudaMemcpyAsync(w.data(), width, sizeof(int) * nslices, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(width);
+    if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string("sell widths: ") + cudaGetErrorString(e));
+    std::vector<int> meta(2 * size_t(nslices));
+    long long off = 0;
+    for (int i = 0; i < nslices; ++i) {
+      meta[2 * i] = int(off);
+      meta[2 * i + 1] = w[i];
+      off += 32LL * w[i];
+    }
+    if (off >= (1LL << 31)) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: matrix too large");
+    int* dmeta = nullptr;
+    int* dcol = nullptr;
+    double* dval = nullptr;
+    e = cudaMalloc(&dmeta, sizeof(int) * meta.size());
+    if (e == cudaSuccess) e = cudaMalloc(&dcol, sizeof(int) * std::max(off, 1LL));
+    if (e == cudaSuccess) e = cudaMalloc(&dval, sizeof(double) * std::max(off, 1LL));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaFree(dmeta);
+      cudaFree(dcol);
+      cudaFree(dval);
+      return fail(ctx, GDT_ENOMEM, std::string("sell copy: ") + cudaGetErrorString(e));
+    }
+    m->sell_meta = dmeta;
+    m->sell_col = dcol;
+    m->sell_val = dval;
+    m->sell_len = off;
+  }
+  k_sell_fill<<<blocks, 256, 0, s>>>(n, nslices, m->rp, m->col, m->val, reinterpret_cast<const int2*>(m->sell_meta),
+                                     m->sell_col, m->sell_val);
+  ctx->launches++;
+  return check_launch(ctx, "sell fill");
 }
 
 // the matrix and the solver's vectors (x, b, r, p, q, dinv) within this many bytes stay in L2
@@ -835,28 +948,26 @@ bool persistent_applies(gdt_context ctx, gdt_matrix m) {
 // Runs the iterations after residual_init; the caller reads the final state from st.
 gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, double* p, double* q,
                           const double* dinv, KState* st, cudaStream_t s) {
-  const bool wide = m->max_row > 16;
-  const void* fn = wide ? reinterpret_cast<const void*>(&k_pcg_persistent<32>)
-                        : reinterpret_cast<const void*>(&k_pcg_persistent<16>);
-  const size_t smem = size_t(PT / 32) * 32 * (wide ? 32 : 16) * (sizeof(double) + sizeof(int));
+  const void* fn = reinterpret_cast<const void*>(&k_pcg_persistent);
   int dev = 0, coop = 0, per_sm = 0;
   GDT_TRY_CUDA(ctx, cudaGetDevice(&dev));
   GDT_TRY_CUDA(ctx, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: no cooperative launch on this device");
-  GDT_TRY_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, smem));
+  GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, 0));
   if (per_sm < 1) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: kernel does not fit an SM");
-  per_sm = std::min(per_sm, 4);
+  per_sm = 1;
   int blocks = per_sm * ctx->num_sms;
-  // no more blocks than warps have rows to stage
-  const int needed = int((m->rows + PT - 1) / PT);
+  // no more blocks than warps have slices
+  const int nslices = int((m->rows + 31) / 32);
+  const int needed = (nslices + PT / 32 - 1) / (PT / 32);
   if (needed < blocks) blocks = std::max(1, needed);
-  if (3 * blocks > kScratchDoubles) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: grid too large");
+  GDT_CHECK(ctx, sell_prepare(ctx, m, s));
   PcgArgs a;
   a.n = int(m->rows);
-  a.rp = m->rp;
-  a.col = m->col;
-  a.val = m->val;
+  a.nslices = nslices;
+  a.meta = reinterpret_cast<const int2*>(m->sell_meta);
+  a.col = m->sell_col;
+  a.val = m->sell_val;
   a.dinv = dinv;
   a.x = x;
   a.r = r;
@@ -867,11 +978,11 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   // the barrier words live in the upper half of the scratch (the partials use its start)
   a.bar = reinterpret_cast<unsigned int*>(ctx->scratch + kScratchDoubles / 2);
   if (3 * blocks > kScratchDoubles / 2) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: grid too large");
-  GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar, 0, sizeof(unsigned int), s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar, 0, sizeof(unsigned long long), s));
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarGen, 0, sizeof(unsigned int), s));
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarFault, 0, sizeof(unsigned int), s));
   void* args[] = {&a};
-  GDT_TRY_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(PT), args, smem, s));
+  GDT_TRY_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(PT), args, 0, s));
   ctx->launches++;
   unsigned int fault = 0;
   GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fault, a.bar + kBarFault, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
