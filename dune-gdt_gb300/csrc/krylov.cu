@@ -632,6 +632,7 @@ struct PcgArgs {
   double* r;
   double* p;
   double* q;
+  double* z;  // dinv r, kept by the update for the direction step
   KState* st;
   double* part;       // 3 * gridDim.x doubles: p.q | r.z, r.r per block
   unsigned int* bar;  // 64-bit arrival count at bar[0], generation at bar[kBarGen], fault at bar[kBarFault]
@@ -789,12 +790,12 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
       break;
     }
     // x += alpha p, r -= alpha q; r.z (z = dinv r) and r.r
-    // (three elements per thread and pass, all their loads issued before the first store)
+    // (two elements per thread and pass, all their loads issued before the first store)
     double v2[2] = {0.0, 0.0};
-    for (int i0 = blockIdx.x * PT + threadIdx.x; i0 < a.n; i0 += 3 * stride) {
-      double pv[3], qv[3], xv[3], rv[3], dv[3];
+    for (int i0 = blockIdx.x * PT + threadIdx.x; i0 < a.n; i0 += 2 * stride) {
+      double pv[2], qv[2], xv[2], rv[2], dv[2];
 #pragma unroll
-      for (int u = 0; u < 3; ++u) {
+      for (int u = 0; u < 2; ++u) {
         const int i = i0 + u * stride;
         const bool in = i < a.n;
         pv[u] = in ? a.p[i] : 0.0;
@@ -804,13 +805,15 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
         dv[u] = in ? __ldg(a.dinv + i) : 0.0;
       }
 #pragma unroll
-      for (int u = 0; u < 3; ++u) {
+      for (int u = 0; u < 2; ++u) {
         const int i = i0 + u * stride;
         if (i < a.n) {
           a.x[i] = fma(alpha, pv[u], xv[u]);
           const double ri = fma(-alpha, qv[u], rv[u]);
+          const double zi = dv[u] * ri;
           a.r[i] = ri;
-          v2[0] = fma(ri, dv[u] * ri, v2[0]);
+          a.z[i] = zi;
+          v2[0] = fma(ri, zi, v2[0]);
           v2[1] = fma(ri, ri, v2[1]);
         }
       }
@@ -831,19 +834,18 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
     if (conv) break;
     // p = dinv r + beta p
     for (int i0 = blockIdx.x * PT + threadIdx.x; i0 < a.n; i0 += 3 * stride) {
-      double pv[3], rv[3], dv[3];
+      double pv[3], zv[3];
 #pragma unroll
       for (int u = 0; u < 3; ++u) {
         const int i = i0 + u * stride;
         const bool in = i < a.n;
         pv[u] = in ? a.p[i] : 0.0;
-        rv[u] = in ? a.r[i] : 0.0;
-        dv[u] = in ? __ldg(a.dinv + i) : 0.0;
+        zv[u] = in ? a.z[i] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < 3; ++u) {
         const int i = i0 + u * stride;
-        if (i < a.n) a.p[i] = fma(beta, pv[u], dv[u] * rv[u]);
+        if (i < a.n) a.p[i] = fma(beta, pv[u], zv[u]);
       }
     }
     if (!pcg_sync(a.bar, epoch)) break;
@@ -946,7 +948,7 @@ bool persistent_applies(gdt_context ctx, gdt_matrix m) {
 }
 
 // Runs the iterations after residual_init; the caller reads the final state from st.
-gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, double* p, double* q,
+gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, double* p, double* q, double* z,
                           const double* dinv, KState* st, cudaStream_t s) {
   const void* fn = reinterpret_cast<const void*>(&k_pcg_persistent);
   int dev = 0, coop = 0, per_sm = 0;
@@ -973,6 +975,7 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   a.r = r;
   a.p = p;
   a.q = q;
+  a.z = z;
   a.st = st;
   a.part = ctx->scratch;
   // the barrier words live in the upper half of the scratch (the partials use its start)
@@ -1175,7 +1178,9 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
         residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
         ctx->last_solver_launch = persistent ? GDT_SOLVER_LAUNCH_PERSISTENT : GDT_SOLVER_LAUNCH_GRAPH;
         if (persistent) {
-          GDT_CHECK(ctx, pcg_persistent(ctx, m, x, r, p, q, one, st, s));
+          double* z = (double*)alloc(vb);
+          if (!z) return fail(ctx, GDT_ENOMEM, "solver vectors");
+          GDT_CHECK(ctx, pcg_persistent(ctx, m, x, r, p, q, z, one, st, s));
         } else {
         // pairs of rows per thread when every vector is 16-byte aligned (the solver's own are; x is
         // the caller's)
