@@ -947,16 +947,18 @@ bool persistent_applies(gdt_context ctx, gdt_matrix m) {
   return bytes <= kPersistentL2Bytes;
 }
 
-// Runs the iterations after residual_init; the caller reads the final state from st.
+// Runs the iterations after residual_init; the caller reads the final state from st. Returns
+// GDT_EUNSUPPORTED, before anything ran, where no cooperative launch of the kernel can be made
+// (the caller then runs the graph form).
 gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, double* p, double* q, double* z,
                           const double* dinv, KState* st, cudaStream_t s) {
   const void* fn = reinterpret_cast<const void*>(&k_pcg_persistent);
   int dev = 0, coop = 0, per_sm = 0;
   GDT_TRY_CUDA(ctx, cudaGetDevice(&dev));
   GDT_TRY_CUDA(ctx, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-  if (!coop) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: no cooperative launch on this device");
+  if (!coop) return GDT_EUNSUPPORTED;  // the caller runs the graph form
   GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, 0));
-  if (per_sm < 1) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: kernel does not fit an SM");
+  if (per_sm < 1) return GDT_EUNSUPPORTED;
   per_sm = 1;
   int blocks = per_sm * ctx->num_sms;
   // no more blocks than warps have slices
@@ -985,7 +987,12 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarGen, 0, sizeof(unsigned int), s));
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarFault, 0, sizeof(unsigned int), s));
   void* args[] = {&a};
-  GDT_TRY_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(PT), args, 0, s));
+  const cudaError_t le = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(PT), args, 0, s);
+  if (le == cudaErrorCooperativeLaunchTooLarge) {  // fewer SMs available than the device has
+    cudaGetLastError();
+    return GDT_EUNSUPPORTED;
+  }
+  GDT_TRY_CUDA(ctx, le);
   ctx->launches++;
   unsigned int fault = 0;
   GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fault, a.bar + kBarFault, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
@@ -1170,39 +1177,42 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
           GDT_TRY_CUDA(ctx, cudaMemcpyAsync(one, ones.data(), vb, cudaMemcpyHostToDevice, s));
           GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
         }
-        const bool persistent = persistent_applies(ctx, m);
-        if (!persistent) {
-          GDT_CHECK(ctx, tune_cg(ctx, m, L, s));
-          L.sched = m->cg_sched;
-        }
-        residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
-        ctx->last_solver_launch = persistent ? GDT_SOLVER_LAUNCH_PERSISTENT : GDT_SOLVER_LAUNCH_GRAPH;
+        bool persistent = persistent_applies(ctx, m);
         if (persistent) {
+          residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
           double* z = (double*)alloc(vb);
           if (!z) return fail(ctx, GDT_ENOMEM, "solver vectors");
-          GDT_CHECK(ctx, pcg_persistent(ctx, m, x, r, p, q, z, one, st, s));
-        } else {
-        // pairs of rows per thread when every vector is 16-byte aligned (the solver's own are; x is
-        // the caller's)
-        const bool pairs = (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
-        const int pair_blocks = std::max(1, std::min(grid_blocks((n + 1) / 2, TH), ctx->num_sms * 8));
-        GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
-          spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
-          timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);
-          if (pairs)
-            k_cg_update_jacobi2<<<pair_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);
-          else
-            k_cg_update_jacobi<double, double><<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials,
-                                                                           L.ticket);
-          timing_end(ctx, s);
-          timing_begin(ctx, s, GDT_TIMING_CG_DIRECTION);
-          if (pairs)
-            k_cg_p_jacobi2<<<pair_blocks, TH, 0, s>>>(n, p, r, one, st);
-          else
-            k_cg_p_jacobi<double><<<L.vec_blocks, TH, 0, s>>>(n, p, r, one, st);
-          timing_end(ctx, s);
-          ctx->launches += 2;
-        }));
+          const gdt_status ps = pcg_persistent(ctx, m, x, r, p, q, z, one, st, s);
+          if (ps == GDT_EUNSUPPORTED) persistent = false;  // x untouched: the graph form starts afresh
+          else if (ps != GDT_OK) return ps;
+          else ctx->last_solver_launch = GDT_SOLVER_LAUNCH_PERSISTENT;
+        }
+        if (!persistent) {
+          ctx->last_solver_launch = GDT_SOLVER_LAUNCH_GRAPH;
+          GDT_CHECK(ctx, tune_cg(ctx, m, L, s));
+          L.sched = m->cg_sched;
+          residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
+          // pairs of rows per thread when every vector is 16-byte aligned (the solver's own are; x is
+          // the caller's)
+          const bool pairs = (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
+          const int pair_blocks = std::max(1, std::min(grid_blocks((n + 1) / 2, TH), ctx->num_sms * 8));
+          GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
+            spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
+            timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);
+            if (pairs)
+              k_cg_update_jacobi2<<<pair_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);
+            else
+              k_cg_update_jacobi<double, double><<<L.vec_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials,
+                                                                             L.ticket);
+            timing_end(ctx, s);
+            timing_begin(ctx, s, GDT_TIMING_CG_DIRECTION);
+            if (pairs)
+              k_cg_p_jacobi2<<<pair_blocks, TH, 0, s>>>(n, p, r, one, st);
+            else
+              k_cg_p_jacobi<double><<<L.vec_blocks, TH, 0, s>>>(n, p, r, one, st);
+            timing_end(ctx, s);
+            ctx->launches += 2;
+          }));
         }
       } else {
         double* z = (double*)alloc(vb);
