@@ -7,7 +7,9 @@
 // flag) live in device memory; every reduction finishes in the last block of its kernel (ticketed,
 // fixed summation order: deterministic), so an iteration issues no host synchronisation. Iterations
 // are captured into a CUDA graph in chunks of `check_every`; the host reads the converged flag once
-// per chunk, and kernels of iterations past convergence return immediately.
+// per chunk, and kernels of iterations past convergence return immediately. FP64 CG with Jacobi or
+// no preconditioner on a system that fits in L2 instead runs all its iterations in one persistent
+// cooperative launch (k_pcg_persistent below).
 // Mixed precision: FP32 inner CG (FP32 CSR values, FP32 vectors, FP32 Jacobi) inside FP64
 // iterative refinement with an FP64 residual r = b - A x from the FP64 matrix.
 #include <cfloat>
