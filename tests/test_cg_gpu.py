@@ -192,6 +192,9 @@ def test_persistent_cg_matches_graph_and_direct(gdt, oracle, case, precond):
 
 def test_persistent_cg_reports_non_convergence_and_skips_long_rows(gdt, oracle):
     op, rhs, A, b = _heat_problem(gdt, oracle, 2, [30, 30], False)
+    lib = gdt._capi.load()
+    assert lib.gdt_context_set_solver_launch(op.ctx.handle, 3) == gdt._capi.EINVAL
+    assert lib.gdt_context_set_solver_launch(None, 0) == gdt._capi.EINVAL
     op.ctx.set_solver_launch("persistent")
     try:
         with pytest.raises(gdt.GdtError) as e:
