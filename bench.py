@@ -303,8 +303,11 @@ def run_gdt(args):
         "error_vs_fp64_reference": err_mixed,
         "solve": {"mixed": info_mixed, "fp64": info_fp64},
         "fp64_plain": {"ms_per_step": ms_fp64, "value": world * ndof / (ms_fp64 / 1e3), "error": err_fp64,
+                       "launch": info_fp64.get("launch"),
                        "spmv_gbs": bytes64 / (spmv64_ms / 1e3) / 1e9 if n64b else None,
-                       "spmv_frac_of_hbm": (bytes64 / (spmv64_ms / 1e3) / 1e9) / hbm if n64b else None},
+                       "spmv_frac_of_hbm": (bytes64 / (spmv64_ms / 1e3) / 1e9) / hbm if n64b else None,
+                       "spmv_note": "spmv_gbs: the graph form's k_spmv, one CUDA-event pair per launch (timing mode "
+                                    "runs the graph kernels); the timed FP64 solves run in the form named by launch"},
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "spmv_autotuner": {"chosen_schedule": sched.value,
                            "ms_per_launch": {name: round(sched_ms[k], 4) for k, name in enumerate(

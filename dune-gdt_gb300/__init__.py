@@ -76,7 +76,7 @@ class Context:
         return int(self.lib.gdt_context_kernel_launches(self.handle))
 
     def set_solver_launch(self, mode):
-        """Launch form of FP64 CG solves: 'auto' (persistent where the system fits in L2), 'graph'
+        """Launch form of FP64 CG solves: 'auto' (persistent wherever it applies), 'graph'
         (one kernel per step, CUDA graphs) or 'persistent' (one cooperative launch for all iterations)."""
         self.call("gdt_context_set_solver_launch", {"auto": capi.SOLVER_LAUNCH_AUTO, "graph": capi.SOLVER_LAUNCH_GRAPH,
                                                     "persistent": capi.SOLVER_LAUNCH_PERSISTENT}[mode])

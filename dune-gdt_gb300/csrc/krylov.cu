@@ -8,7 +8,7 @@
 // fixed summation order: deterministic), so an iteration issues no host synchronisation. Iterations
 // are captured into a CUDA graph in chunks of `check_every`; the host reads the converged flag once
 // per chunk, and kernels of iterations past convergence return immediately. FP64 CG with Jacobi or
-// no preconditioner on a system that fits in L2 instead runs all its iterations in one persistent
+// no preconditioner on rows of at most 32 entries instead runs all its iterations in one persistent
 // cooperative launch (k_pcg_persistent below).
 // Mixed precision: FP32 inner CG (FP32 CSR values, FP32 vectors, FP32 Jacobi) inside FP64
 // iterative refinement with an FP64 residual r = b - A x from the FP64 matrix.
@@ -603,13 +603,14 @@ void ilu_apply(gdt_context ctx, gdt_matrix m, const Ilu& f, const double* r, dou
 }
 
 
-// ------------------------------------------------- persistent CG for systems that fit in L2 ---
+// ------------------------------------------------------------------------- persistent CG ---
 // One cooperative launch runs every iteration of Jacobi-preconditioned (or plain) CG. The kernel
 // boundaries of the graph form become grid barriers, three per iteration: after q = A p, after the
 // x/r update, after the direction update. Every block reduces the per-block partial sums itself, in
 // block order, so all blocks hold bit-identical alpha, beta and convergence decisions without a
-// broadcast step. This pays where an iteration is bound by launch, ramp-up and tail latency rather
-// than bandwidth: matrices and vectors that stay in the 129 MB L2. The Chronopoulos-Gear form (one
+// broadcast step. This pays most where an iteration is bound by launch, ramp-up and tail latency
+// rather than bandwidth (matrices and vectors that stay in the 129 MB L2), and also where the SpMV
+// streams the matrix from HBM (no kernel boundaries, no row-pointer indirection). The Chronopoulos-Gear form (one
 // reduction and two barriers per iteration) measured slower here (277 against 250 ms for the SWIPDG
 // system of 256^2 squares) and needed up to 65 % more iterations on badly conditioned 1D and 2D
 // systems, so the iteration stays the standard one of the graph form. The SpMV reads a SELL-32 copy
@@ -897,7 +898,10 @@ gdt_status sell_prepare(gdt_context ctx, gdt_matrix m, cudaStream_t s) {
   const int blocks = (nslices * 32 + 255) / 256;
   if (!m->sell_meta) {
     int* width = nullptr;
-    GDT_TRY_CUDA(ctx, cudaMalloc(&width, sizeof(int) * nslices));
+    if (cudaMalloc(&width, sizeof(int) * nslices) != cudaSuccess) {
+      cudaGetLastError();
+      return GDT_EUNSUPPORTED;
+    }
     k_sell_width<<<blocks, 256, 0, s>>>(n, nslices, m->rp, width);
     ctx->launches++;
     std::vector<int> w(nslices);
@@ -912,7 +916,7 @@ gdt_status sell_prepare(gdt_context ctx, gdt_matrix m, cudaStream_t s) {
       meta[2 * i + 1] = w[i];
       off += 32LL * w[i];
     }
-    if (off >= (1LL << 31)) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: matrix too large");
+    if (off >= (1LL << 31)) return GDT_EUNSUPPORTED;  // offsets are 32-bit: the graph form runs
     int* dmeta = nullptr;
     int* dcol = nullptr;
     double* dval = nullptr;
@@ -925,7 +929,8 @@ gdt_status sell_prepare(gdt_context ctx, gdt_matrix m, cudaStream_t s) {
       cudaFree(dmeta);
       cudaFree(dcol);
       cudaFree(dval);
-      return fail(ctx, GDT_ENOMEM, std::string("sell copy: ") + cudaGetErrorString(e));
+      cudaGetLastError();
+      return GDT_EUNSUPPORTED;  // no room for the copy: the caller runs the graph form
     }
     m->sell_meta = dmeta;
     m->sell_col = dcol;
@@ -938,15 +943,13 @@ gdt_status sell_prepare(gdt_context ctx, gdt_matrix m, cudaStream_t s) {
   return check_launch(ctx, "sell fill");
 }
 
-// the matrix and the solver's vectors (x, b, r, p, q, dinv) within this many bytes stay in L2
-constexpr double kPersistentL2Bytes = 96.0e6;
-
+// Rows of at most 32 entries (the SELL-32 SpMV's limit). Measured against the graph form: 40.6 against
+// 51.7 us per iteration for the L2-resident SWIPDG system of 256^2 squares, and 209 against 264 us
+// for the 128^3 Q1 system (727.7 MB streamed from HBM per SpMV), same iteration counts: AUTO takes it
+// wherever it applies.
 bool persistent_applies(gdt_context ctx, gdt_matrix m) {
   if (ctx->timing || ctx->solver_launch == GDT_SOLVER_LAUNCH_GRAPH) return false;
-  if (m->max_row < 1 || m->max_row > 32 || m->rows < 1) return false;
-  if (ctx->solver_launch == GDT_SOLVER_LAUNCH_PERSISTENT) return true;
-  const double bytes = 12.0 * double(m->nnz) + 4.0 * double(m->rows + 1) + 48.0 * double(m->rows);
-  return bytes <= kPersistentL2Bytes;
+  return m->max_row >= 1 && m->max_row <= 32 && m->rows >= 1;
 }
 
 // Runs the iterations after residual_init; the caller reads the final state from st. Returns
@@ -967,7 +970,10 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   const int nslices = int((m->rows + 31) / 32);
   const int needed = (nslices + PT / 32 - 1) / (PT / 32);
   if (needed < blocks) blocks = std::max(1, needed);
-  GDT_CHECK(ctx, sell_prepare(ctx, m, s));
+  {
+    const gdt_status ss = sell_prepare(ctx, m, s);
+    if (ss != GDT_OK) return ss;
+  }
   PcgArgs a;
   a.n = int(m->rows);
   a.nslices = nslices;

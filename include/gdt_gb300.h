@@ -100,10 +100,10 @@ gdt_status gdt_context_kernel_timing(gdt_context ctx, int kind, double* ms, int6
 /* How gdt_solve runs FP64 CG with Jacobi or no preconditioner (no reference counterpart: the launch
  * form of the device solver). GRAPH: one kernel per step (SpMV, update, direction), iterations
  * captured in CUDA graphs. PERSISTENT: one cooperative launch runs every iteration, with grid
- * barriers between the steps; it takes matrices whose rows hold at most 32 entries. AUTO (default):
- * PERSISTENT where the matrix and the solver vectors fit in L2 (there an iteration is bound by
- * launch and synchronisation latency, not by bandwidth), GRAPH otherwise. Timing mode always runs
- * GRAPH's kernels launched one by one. */
+ * barriers between the steps and a SELL-32 copy of the matrix; it takes matrices whose rows hold at
+ * most 32 entries. AUTO (default): PERSISTENT wherever it applies (it was faster both for systems
+ * that stay in L2 and for ones streamed from HBM), GRAPH otherwise or where no cooperative launch or
+ * no room for the copy is available. Timing mode always runs GRAPH's kernels launched one by one. */
 #define GDT_SOLVER_LAUNCH_AUTO 0
 #define GDT_SOLVER_LAUNCH_GRAPH 1
 #define GDT_SOLVER_LAUNCH_PERSISTENT 2
