@@ -964,8 +964,7 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   if (!coop) return GDT_EUNSUPPORTED;  // the caller runs the graph form
   GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, 0));
   if (per_sm < 1) return GDT_EUNSUPPORTED;
-  per_sm = 1;
-  int blocks = per_sm * ctx->num_sms;
+  int blocks = ctx->num_sms;  // one block per SM
   // no more blocks than warps have slices
   const int nslices = int((m->rows + 31) / 32);
   const int needed = (nslices + PT / 32 - 1) / (PT / 32);
