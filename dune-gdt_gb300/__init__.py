@@ -81,6 +81,11 @@ class Context:
         self.call("gdt_context_set_solver_launch", {"auto": capi.SOLVER_LAUNCH_AUTO, "graph": capi.SOLVER_LAUNCH_GRAPH,
                                                     "persistent": capi.SOLVER_LAUNCH_PERSISTENT}[mode])
 
+    def set_persistent_limits(self, blocks=0, wait_limit_ns=0):
+        """Grid size cap (0: one block per SM) and grid-barrier wait limit in ns (0: one second) of the
+        persistent solver launches."""
+        self.call("gdt_context_set_persistent_limits", int(blocks), int(wait_limit_ns))
+
 
 _default = {}
 

@@ -91,6 +91,7 @@ _SIGNATURES = {
     "gdt_context_set_timing": (C.c_int, [P, C.c_int]),
     "gdt_context_set_solver_launch": (C.c_int, [P, C.c_int]),
     "gdt_context_last_solver_launch": (C.c_int, [P]),
+    "gdt_context_set_persistent_limits": (C.c_int, [P, C.c_int, C.c_int64]),
     "gdt_context_spmv_timing": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                           C.POINTER(C.c_int64), C.c_int]),
     "gdt_context_kernel_timing": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int]),

@@ -109,6 +109,13 @@ gdt_status gdt_context_set_solver_launch(gdt_context ctx, int mode) {
 
 int gdt_context_last_solver_launch(gdt_context ctx) { return ctx ? ctx->last_solver_launch : 0; }
 
+gdt_status gdt_context_set_persistent_limits(gdt_context ctx, int blocks, int64_t wait_limit_ns) {
+  if (!ctx || blocks < 0 || wait_limit_ns < 0) return GDT_EINVAL;
+  ctx->persistent_blocks = blocks;
+  ctx->persistent_wait_ns = wait_limit_ns;
+  return GDT_OK;
+}
+
 gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp64_launches, double* fp32_ms,
                                    int64_t* fp32_launches, int reset) {
   if (!ctx) return GDT_EINVAL;

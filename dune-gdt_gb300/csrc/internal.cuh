@@ -45,6 +45,8 @@ struct gdt_context_s {
   // accumulate per class
   int timing = 0;
   int solver_launch = 0;       // GDT_SOLVER_LAUNCH_* requested for FP64 CG
+  int persistent_blocks = 0;   // grid size cap of the persistent solver launches (0: one block per SM)
+  long long persistent_wait_ns = 0;  // longest grid-barrier wait of the persistent solvers (0: 1 s)
   int last_solver_launch = 0;  // the form the last FP64 CG solve ran in
   std::vector<cudaEvent_t> events;  // pairs (start, stop)
   std::vector<int> event_kind;      // GDT_TIMING_* class of each pair

@@ -639,6 +639,7 @@ struct PcgArgs {
   KState* st;
   double* part;       // 3 * gridDim.x doubles: p.q | r.z, r.r per block
   unsigned int* bar;  // 64-bit arrival count at bar[0], generation at bar[kBarGen], fault at bar[kBarFault]
+  unsigned long long wait_ns;  // longest wait at a grid barrier
 };
 // the arrival counter, the generation the waiting blocks poll and the fault flag sit 4 KB apart, so
 // the polls and the arrivals do not queue at the same L2 slice
@@ -653,9 +654,10 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Grid barrier (all blocks are co-resident: cooperative launch). Barrier number `epoch` (counted by
 // thread 0 of every block) is complete when the 64-bit arrival count reaches epoch * blocks; the last
 // block to arrive publishes the epoch as the generation the others poll (no reset of the count, so
-// the release is one store after the arrival). The waits are bounded by time and by count, after
-// which the fault flag is set and every block returns false from then on.
-__device__ bool pcg_sync(unsigned int* bar, unsigned int& epoch) {
+// the release is one store after the arrival). The waits are bounded by time (wait_ns, checked at the
+// first poll and every 256 polls) and by count, after which the fault flag is set and every block
+// returns false from then on.
+__device__ bool pcg_sync(unsigned int* bar, unsigned int& epoch, unsigned long long wait_ns) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -674,12 +676,12 @@ __device__ bool pcg_sync(unsigned int* bar, unsigned int& epoch) {
         unsigned int spins = 0;
         while (*vgen != epoch) {
           ++spins;
-          if ((spins & 255u) == 0) {
+          if ((spins & 255u) == 1u) {
             if (*vfault) {
               good = 0;
               break;
             }
-            if (spins > (1u << 26) || global_ns() - t0 > kBarrierNs) {
+            if (spins > (1u << 26) || global_ns() - t0 > wait_ns) {
               atomicExch(bar + kBarFault, 1u);
               good = 0;
               break;
@@ -785,7 +787,7 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
     double v1[1] = {pcg_spmv(a, mymeta)};
     block_reduce<1>(v1, red);
     if (threadIdx.x == 0) a.part[blockIdx.x] = v1[0];
-    if (!pcg_sync(a.bar, epoch)) break;
+    if (!pcg_sync(a.bar, epoch, a.wait_ns)) break;
     pcg_allreduce<1>(a.part, v1, red, bc);
     alpha = rho / v1[0];
     if (!(v1[0] > 0.0) || !isfinite(v1[0])) {
@@ -826,7 +828,7 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
       a.part[nb + blockIdx.x] = v2[0];
       a.part[2 * nb + blockIdx.x] = v2[1];
     }
-    if (!pcg_sync(a.bar, epoch)) break;
+    if (!pcg_sync(a.bar, epoch, a.wait_ns)) break;
     pcg_allreduce<2>(a.part + nb, v2, red, bc);
     beta = v2[0] / rho;
     rho = v2[0];
@@ -851,7 +853,7 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
         if (i < a.n) a.p[i] = fma(beta, pv[u], zv[u]);
       }
     }
-    if (!pcg_sync(a.bar, epoch)) break;
+    if (!pcg_sync(a.bar, epoch, a.wait_ns)) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->rho = rho;
@@ -965,6 +967,7 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, 0));
   if (per_sm < 1) return GDT_EUNSUPPORTED;
   int blocks = ctx->num_sms;  // one block per SM
+  if (ctx->persistent_blocks > 0) blocks = std::min(blocks, ctx->persistent_blocks);
   // no more blocks than warps have slices
   const int nslices = int((m->rows + 31) / 32);
   const int needed = (nslices + PT / 32 - 1) / (PT / 32);
@@ -989,6 +992,7 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   a.part = ctx->scratch;
   // the barrier words live in the upper half of the scratch (the partials use its start)
   a.bar = reinterpret_cast<unsigned int*>(ctx->scratch + kScratchDoubles / 2);
+  a.wait_ns = ctx->persistent_wait_ns > 0 ? (unsigned long long)ctx->persistent_wait_ns : kBarrierNs;
   if (3 * blocks > kScratchDoubles / 2) return fail(ctx, GDT_EUNSUPPORTED, "persistent solver: grid too large");
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar, 0, sizeof(unsigned long long), s));
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarGen, 0, sizeof(unsigned int), s));

@@ -8,12 +8,18 @@
 //
 // Its work vectors (r, p, q, the Jacobi diagonal), reduction partials, the last-block ticket and the
 // solver scalars live in one file-scope __device__ array of fixed size (GDT_NOALLOC_MAX_ROWS rows,
-// about 8 MB), which every GPU that loads the library keeps until the process exits. Host code does
-// not use the array's name as an address: the first call on a device (with that device current)
-// looks the address up once with cudaGetSymbolAddress and all kernels receive that pointer. Make that
-// first call on a device before any stream capture. All calls share the array and it keeps the last
+// about 8 MB), which every GPU keeps until the process exits once this module is loaded there. With
+// CUDA's lazy module loading (the default) that happens at the first call on a device, not when the
+// library is loaded: that call loads the module (which places the array and may synchronise the
+// device), so make it at set-up time, before any stream capture. Host code does not use the array's
+// name as an address: that first call (with the device current) looks the address up with
+// cudaGetSymbolAddress and all kernels receive that pointer; the lookup is repeated only when the
+// device's context changed (after cudaDeviceReset). All calls share the array and it keeps the last
 // call's contents, so the ticket is cleared at the start of every call; calls whose work overlaps on
 // the GPU (two streams, two host threads) race on it and must be serialised by the caller.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cmath>
 #include <mutex>
 
@@ -133,21 +139,45 @@ __global__ void __launch_bounds__(kTH) k_na_p(int n, NaScratch* s) {
     s->p[i] = fma(beta, s->p[i], s->dinv[i] * s->r[i]);
 }
 
-// per-device address of the scratch array, looked up once per device
+// Address of the scratch array in the current context of each device. The lookup is cached per
+// device together with the context it was made in: after cudaDeviceReset (or any new primary context)
+// the module is loaded again, the array may move, and the next call looks it up again.
 std::mutex g_noalloc_mutex;
-NaScratch* g_noalloc_ptr[64] = {};
+struct NaCached {
+  CUcontext ctx;
+  NaScratch* ptr;
+};
+NaCached g_noalloc_ptr[64] = {};
+
+CUcontext current_cu_context() {
+  static PFN_cuCtxGetCurrent_v4000 get = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(fn);
+  });
+  CUcontext c = nullptr;
+  if (get) get(&c);
+  return c;
+}
 
 gdt_status scratch_for_current_device(NaScratch** out, int* device) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return GDT_ECUDA;
   *device = dev;
+  CUcontext cur = current_cu_context();  // NULL before the runtime made the primary context current
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  if (!cur || !g_noalloc_ptr[dev].ptr || g_noalloc_ptr[dev].ctx != cur) {
+    // the first lookup in a context loads this module (lazy loading), which places the array
     void* ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return GDT_ECUDA;
-    g_noalloc_ptr[dev] = static_cast<NaScratch*>(ptr);
+    cur = current_cu_context();  // the lookup made the device's primary context current
+    g_noalloc_ptr[dev] = NaCached{cur, static_cast<NaScratch*>(ptr)};
   }
-  *out = g_noalloc_ptr[dev];
+  *out = g_noalloc_ptr[dev].ptr;
   return GDT_OK;
 }
 

@@ -110,6 +110,12 @@ gdt_status gdt_context_kernel_timing(gdt_context ctx, int kind, double* ms, int6
 gdt_status gdt_context_set_solver_launch(gdt_context ctx, int mode);
 /* launch form (GRAPH or PERSISTENT) of the context's last FP64 CG solve; 0 before the first */
 int gdt_context_last_solver_launch(gdt_context ctx);
+/* Limits of the persistent (cooperative) solver launches (no reference counterpart; diagnostics and
+ * tests of the launch form): blocks caps the grid (0: one block per SM, the default), wait_limit_ns
+ * bounds every wait at a grid barrier (0: the default of one second). A wait that runs out sets a
+ * device flag, every block leaves at its next barrier, and the solve returns GDT_ECUDA ("a grid
+ * barrier wait ran out"); the context stays usable. */
+gdt_status gdt_context_set_persistent_limits(gdt_context ctx, int blocks, int64_t wait_limit_ns);
 
 /* --------------------------------------------------------------------- grid --- */
 /* make_cube_grid(lower_left, upper_right, num_elements): equidistant YaspGrid-like cube grid
@@ -298,9 +304,11 @@ gdt_status gdt_newton_solve(gdt_context ctx, gdt_matrix m, const double* range, 
  * callers that may not allocate device memory themselves or let a library do it: code inside a host
  * framework that owns all device memory through its own pool, or a time-critical loop that cannot
  * take cudaMalloc's implicit device synchronisation. Its work vectors live in a fixed file-scope
- * device array (about 8 MB, held by every GPU that loads the library until exit), so
- * n <= GDT_NOALLOC_MAX_ROWS; larger n returns GDT_EINVAL (use gdt_solve). The first call on a device
- * looks the array's address up (make it before any stream capture). All calls share the array:
+ * device array (about 8 MB, held by a GPU until exit once the library's module is loaded there), so
+ * n <= GDT_NOALLOC_MAX_ROWS; larger n returns GDT_EINVAL (use gdt_solve). With CUDA's lazy module
+ * loading (the default) the first call on a device loads the module, which places the array there,
+ * and looks the array's address up: make that first call at set-up time, before any stream capture.
+ * The address is looked up again only after the device's context changed (cudaDeviceReset). All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller. x holds the initial guess;
  * stop when ||b - A x|| <= tol ||b - A x0|| (recursive residual), GDT_ENOCONV after max_iter. */
 #define GDT_NOALLOC_MAX_ROWS 262144

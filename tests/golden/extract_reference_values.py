@@ -70,4 +70,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python extract_reference_values.py <root of the dune-gdt source tree>")
+    main(sys.argv[1])

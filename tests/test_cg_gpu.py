@@ -215,6 +215,60 @@ def test_persistent_cg_reports_non_convergence_and_skips_long_rows(gdt, oracle):
         op.ctx.set_solver_launch("auto")
 
 
+@pytest.mark.parametrize("dim,n,blocks", [(2, [200, 200], 1), (3, [40, 40, 40], 2)])
+def test_persistent_cg_on_few_blocks_reaches_later_slices(gdt, dim, n, blocks):
+    # A warp of the persistent kernel keeps the (offset, width) of its first 32 SELL-32 slices in
+    # registers and loads those of later slices from memory. With the grid capped at 1 or 2 blocks
+    # (32 or 64 warps) the 1,263 slices of the 200^2 Q1 system and the 2,154 of the 40^3 one give
+    # warps a 33rd and later slice, so that branch runs here (a full grid reaches it only above
+    # ~5 M rows).
+    g = gdt.make_cube_grid([0.0] * dim, [1.0] * dim, n)
+    kappa = torch.exp(torch.tensor(np.random.default_rng(12).standard_normal(g.num_elements), device="cuda"))
+    prob = gdt.DiffusionProblem(g)
+    prob.assemble(kappa)
+    op, rhs = prob.op, prob.rhs
+    nslices = (op.shape[0] + 31) // 32
+    assert nslices > 32 * 32 * blocks
+    opts = {"tol": 1e-12, "precond": "jacobi", "max_iter": 100000}
+    xg, ig = _solve_in(op, rhs, "graph", opts)
+    op.ctx.set_persistent_limits(blocks=blocks)
+    try:
+        xp, ip = _solve_in(op, rhs, "persistent", opts)
+    finally:
+        op.ctx.set_persistent_limits()
+    assert ip["launch"] == "persistent" and ip["converged"]
+    assert abs(ig["iterations"] - ip["iterations"]) <= max(2, 0.02 * ig["iterations"])
+    xd = spl.spsolve(_scipy(op).tocsc(), rhs.cpu().numpy())
+    assert rel_err(xp.cpu().numpy(), xd) < 1e-10
+    assert rel_err(xp.cpu().numpy(), xg.cpu().numpy()) < 1e-10
+
+
+def test_persistent_cg_barrier_wait_limit_reports_and_recovers(gdt):
+    # Every grid-barrier wait of the persistent solver is bounded. With the limit set to 1 ns the
+    # first wait runs out: the waiting block sets the fault flag, every block leaves at its next
+    # barrier, and the solve reports GDT_ECUDA. The same context then solves normally.
+    g = gdt.make_cube_grid([0.0] * 3, [1.0] * 3, [30, 30, 30])
+    kappa = torch.exp(torch.tensor(np.random.default_rng(13).standard_normal(g.num_elements), device="cuda"))
+    prob = gdt.DiffusionProblem(g)
+    prob.assemble(kappa)
+    op, rhs = prob.op, prob.rhs
+    opts = {"tol": 1e-12, "precond": "jacobi", "max_iter": 100000}
+    op.ctx.set_persistent_limits(wait_limit_ns=1)
+    try:
+        op.ctx.set_solver_launch("persistent")
+        with pytest.raises(gdt.GdtError) as e:
+            op.apply_inverse(rhs, opts=opts)
+    finally:
+        op.ctx.set_persistent_limits()
+        op.ctx.set_solver_launch("auto")
+    assert e.value.status == gdt._capi.ECUDA
+    assert "grid barrier wait ran out" in str(e.value)
+    x, info = _solve_in(op, rhs, "persistent", opts)
+    assert info["launch"] == "persistent" and info["converged"]
+    xd = spl.spsolve(_scipy(op).tocsc(), rhs.cpu().numpy())
+    assert rel_err(x.cpu().numpy(), xd) < 1e-10
+
+
 def test_mixed_precision_refinement_reaches_fp64_accuracy(gdt, oracle):
     op, rhs, A, b = _heat_problem(gdt, oracle, 3, [12, 10, 14], False)
     xd = spl.spsolve(A.to_scipy().tocsc(), b)
