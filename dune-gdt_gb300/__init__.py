@@ -409,12 +409,17 @@ class MatrixOperator:
         return int(capi.load().gdt_matrix_nnz(self.handle))
 
     def csr(self):
-        """(row_ptr, col, val) as zero-copy CUDA tensors over the library-owned CSR arrays."""
+        """(row_ptr, col, val) as zero-copy CUDA tensors over the library-owned CSR arrays. Values written
+        through these tensors after a later apply() need values_changed() before the next apply()."""
         rp, col, val = C.c_void_p(), C.c_void_p(), C.c_void_p()
         capi.check(capi.load().gdt_matrix_device_arrays(self.handle, C.byref(rp), C.byref(col), C.byref(val)))
         n, nnz = self.shape[0], self.nnz
         return (_wrap(rp.value, n + 1, torch.int32, self.ctx.device), _wrap(col.value, nnz, torch.int32, self.ctx.device),
                 _wrap(val.value, nnz, torch.float64, self.ctx.device))
+
+    def values_changed(self):
+        """Tell the library that the values were written through csr() tensors (gdt_matrix_values_changed)."""
+        capi.check(capi.load().gdt_matrix_values_changed(self.handle), what="gdt_matrix_values_changed")
 
     @property
     def matrix(self):

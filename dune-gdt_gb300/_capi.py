@@ -9,7 +9,8 @@ import os
 
 from . import _build
 
-SPMV_SCHEDULES = 8
+SPMV_SCHEDULES = 9
+SPMV_SCHEDULE_SELL32 = 8
 NORM_H1_SEMI, NORM_L2 = 0, 1
 TIMING_SPMV_FP64, TIMING_SPMV_FP32, TIMING_CG_UPDATE, TIMING_CG_DIRECTION, TIMING_RELIABLE_UPDATE = range(5)
 TIMING_KINDS = 8
@@ -114,6 +115,7 @@ _SIGNATURES = {
     "gdt_matrix_set_zero": (C.c_int, [P, P]),
     "gdt_matrix_tune": (C.c_int, [P, P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gdt_matrix_set_schedule": (C.c_int, [P, C.c_int]),
+    "gdt_matrix_values_changed": (C.c_int, [P]),
     "gdt_matrix_mixed_operator": (C.c_int, [P]),
     "gdt_assemble_cg_diffusion": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_assemble_cg_rhs": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),

@@ -302,9 +302,7 @@ gdt_status gdt_matrix_destroy(gdt_matrix m) {
   if (!m) return GDT_EINVAL;
   ho_matrix_free(static_cast<HoMatrix*>(m->ho));
   if (m->mf_kappa) cudaFree(m->mf_kappa);
-  if (m->sell_meta) cudaFree(m->sell_meta);
-  if (m->sell_col) cudaFree(m->sell_col);
-  if (m->sell_val) cudaFree(m->sell_val);
+  sell_free(m);
   if (m->rp) cudaFree(m->rp);
   if (m->col) cudaFree(m->col);
   if (m->val) cudaFree(m->val);
@@ -320,13 +318,17 @@ gdt_status gdt_matrix_device_arrays(gdt_matrix m, const int32_t** rp, const int3
   if (!m) return GDT_EINVAL;
   if (rp) *rp = m->rp;
   if (col) *col = m->col;
-  if (val) *val = m->val;
+  if (val) {
+    *val = m->val;
+    m->val_version++;  // the caller may write the values through this pointer
+  }
   return GDT_OK;
 }
 
 gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m) {
   if (!ctx || !m) return GDT_EINVAL;
   m->mf_valid = 0;
+  m->val_version++;
   GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * m->nnz, ctx->stream));
   return GDT_OK;
 }
@@ -335,6 +337,7 @@ gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m) {
 gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs) {
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  m->val_version++;
   if (m->test.order == 2 || d->kappa_qp) {
     m->mf_valid = 0;
     GDT_CHECK(ctx, ho_prepare(ctx, m));
@@ -353,6 +356,7 @@ gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space s, const gdt_diffusion
 gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
   if (!ctx || !m) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  m->val_version++;
   if (m->test.order == 2) return ho_dirichlet(ctx, m, rhs);
   m->mf_dirichlet = 1;
   return dirichlet_apply(ctx, m, rhs);
@@ -362,6 +366,7 @@ gdt_status gdt_assemble_cg_product(gdt_context ctx, gdt_matrix m, const gdt_prod
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
   m->mf_valid = 0;
+  m->val_version++;
   GDT_CHECK(ctx, ho_prepare(ctx, m));
   return ho_assemble(ctx, m, 1, d->weight, d->weight_const, d->weight_qp, nullptr, 0.0, nullptr, 0);
 }
@@ -391,6 +396,7 @@ gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_des
   if (m->test.kind != GDT_SPACE_DG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a DG space");
   if (m->stencil != GDT_STENCIL_ELEMENT_AND_INTERSECTION)
     return fail(ctx, GDT_ESHAPE, "SWIPDG needs the element_and_intersection stencil");
+  m->val_version++;
   return assemble_swipdg(ctx, m, d, rhs);
 }
 

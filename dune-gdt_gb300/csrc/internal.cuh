@@ -85,13 +85,16 @@ struct gdt_matrix_s {
   // 3D Q1 Laplace assemblies: the element coefficients in FP32 and the reference element stiffness
   // (corner-bit indexing), for the matrix-free inner operator of the mixed-precision solver
   float* mf_kappa = nullptr;
-  // SELL-32 copy for the persistent solver: slices of 32 rows stored column-major, padded to the
-  // slice's longest row; (offset, width) per slice (from the pattern, built once), values and
-  // columns (refreshed at every persistent solve)
+  // SELL-32 copy (linalg.cuh SellView): slices of 32 rows stored column-major, padded to the slice's
+  // longest row; (offset, width) per slice (from the pattern, built once), values and columns copied
+  // from the CSR arrays when the values changed (val_version) and at every solve
   int* sell_meta = nullptr;
   int* sell_col = nullptr;
   double* sell_val = nullptr;
   long long sell_len = 0;
+  long long val_version = 0;    // bumped by every entry point that may change the values
+  long long sell_version = -1;  // val_version the SELL copy was filled at
+  int use_sell = 0;             // plain SpMV and the graph-form CG SpMV read the SELL copy (tuned or pinned)
   float mf_K[64] = {};
   int mf_valid = 0;      // the values are exactly that assembly (cleared by any other value change)
   int mf_dirichlet = 0;  // with Dirichlet unit rows and columns
@@ -143,6 +146,12 @@ gdt_status swipdg_dlogkappa(gdt_context ctx, const gdt_space_s& s, const gdt_ipd
 // spmv.cu
 gdt_status spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y);
 gdt_status tune_spmv(gdt_context ctx, gdt_matrix m, double* times_ms = nullptr);
+// SELL-32 copy of m: slice table built once per pattern (GDT_EUNSUPPORTED when there is no room or the
+// offsets do not fit 32 bits), values and columns copied when the values changed or `refill` is set
+gdt_status sell_prepare(gdt_context ctx, gdt_matrix m, cudaStream_t s, bool refill);
+void sell_free(gdt_matrix m);
+// index of the SELL-32 schedule in gdt_matrix_tune / gdt_matrix_set_schedule
+constexpr int kSellSchedule = 8;
 // krylov.cu
 gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
                  gdt_solve_info* info);

@@ -83,6 +83,32 @@ __global__ void __launch_bounds__(TH) k_spmv(int n, const int* __restrict__ rp, 
   }
 }
 
+// q = A p on the SELL-32 copy with p.q -> alpha: the graph-form CG SpMV where the SELL schedule
+// was tuned fastest inside the iteration (or pinned)
+__global__ void __launch_bounds__(256) k_sell_spmv_cg(SellView A, const double* __restrict__ p,
+                                                      double* __restrict__ q, KState* st, double* partials,
+                                                      unsigned int* ticket) {
+  if (stopped(st)) return;
+  double a0 = 0.0;
+  for_slices<true>(
+      A, p,
+      [&](int row, bool active, double s, double pr) {
+        if (active) {
+          q[row] = s;
+          a0 = fma(pr, s, a0);
+        }
+      },
+      p);
+  double v[1] = {a0};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    if (!(v[0] > 0.0) || !isfinite(v[0])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+    st->alpha = st->rho / v[0];
+  }
+}
+
 // r = b - A x, z = M^{-1} r (Jacobi if dinv, else z = r), p = z (CG start); rho = r.z, rr0 = r.r
 template <int G, int PL, class T>
 __global__ void __launch_bounds__(TH) k_residual_init(int n, const int* __restrict__ rp, const int* __restrict__ col,
@@ -487,6 +513,15 @@ struct Launch {
   }
 };
 
+// the graph-form CG SpMV (q = A p, alpha) on the SELL-32 copy
+void spmv_cg_sell(const Launch& L, gdt_matrix m, const double* p, double* q, KState* st) {
+  const SellView A = sell_view(m);
+  timing_begin(L.ctx, L.s, GDT_TIMING_SPMV_FP64);
+  k_sell_spmv_cg<<<sell_blocks(A.nslices, L.ctx->num_sms), 256, 0, L.s>>>(A, p, q, st, L.partials, L.ticket);
+  timing_end(L.ctx, L.s);
+  L.ctx->launches++;
+}
+
 template <class T, int MODE>
 void spmv_mode(const Launch& L, const int* rp, const int* col, const T* val, const T* x, T* y, const T* w,
                KState* st) {
@@ -866,85 +901,6 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
   }
 }
 
-// SELL-32 widths: one warp per slice, the longest row of its 32
-__global__ void k_sell_width(int n, int nslices, const int* __restrict__ rp, int* __restrict__ width) {
-  const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (slice >= nslices) return;
-  const int row = slice * 32 + (threadIdx.x & 31);
-  const int len = row < n ? rp[row + 1] - rp[row] : 0;
-  const int w = __reduce_max_sync(0xffffffffu, len);
-  if ((threadIdx.x & 31) == 0) width[slice] = w;
-}
-
-// SELL-32 values and columns from the CSR arrays; padding entries are 0 * p[row] (row 0 past the end)
-__global__ void k_sell_fill(int n, int nslices, const int* __restrict__ rp, const int* __restrict__ col,
-                            const double* __restrict__ val, const int2* __restrict__ meta, int* __restrict__ scol,
-                            double* __restrict__ sval) {
-  const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (slice >= nslices) return;
-  const int lane = threadIdx.x & 31;
-  const int row = slice * 32 + lane;
-  const int2 md = meta[slice];
-  const int beg = row < n ? rp[row] : 0, len = row < n ? rp[row + 1] - beg : 0;
-  for (int t = 0; t < md.y; ++t) {
-    const long long k = md.x + (long long)t * 32 + lane;
-    scol[k] = t < len ? col[beg + t] : (row < n ? row : 0);
-    sval[k] = t < len ? val[beg + t] : 0.0;
-  }
-}
-
-// Builds the slice table once per matrix (the pattern never changes) and copies the current values.
-gdt_status sell_prepare(gdt_context ctx, gdt_matrix m, cudaStream_t s) {
-  const int n = int(m->rows);
-  const int nslices = (n + 31) / 32;
-  const int blocks = (nslices * 32 + 255) / 256;
-  if (!m->sell_meta) {
-    int* width = nullptr;
-    if (cudaMalloc(&width, sizeof(int) * nslices) != cudaSuccess) {
-      cudaGetLastError();
-      return GDT_EUNSUPPORTED;
-    }
-    k_sell_width<<<blocks, 256, 0, s>>>(n, nslices, m->rp, width);
-    ctx->launches++;
-    std::vector<int> w(nslices);
-    cudaError_t e = cudaMemcpyAsync(w.data(), width, sizeof(int) * nslices, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(width);
-    if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string("sell widths: ") + cudaGetErrorString(e));
-    std::vector<int> meta(2 * size_t(nslices));
-    long long off = 0;
-    for (int i = 0; i < nslices; ++i) {
-      meta[2 * i] = int(off);
-      meta[2 * i + 1] = w[i];
-      off += 32LL * w[i];
-    }
-    if (off >= (1LL << 31)) return GDT_EUNSUPPORTED;  // offsets are 32-bit: the graph form runs
-    int* dmeta = nullptr;
-    int* dcol = nullptr;
-    double* dval = nullptr;
-    e = cudaMalloc(&dmeta, sizeof(int) * meta.size());
-    if (e == cudaSuccess) e = cudaMalloc(&dcol, sizeof(int) * std::max(off, 1LL));
-    if (e == cudaSuccess) e = cudaMalloc(&dval, sizeof(double) * std::max(off, 1LL));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-      cudaFree(dmeta);
-      cudaFree(dcol);
-      cudaFree(dval);
-      cudaGetLastError();
-      return GDT_EUNSUPPORTED;  // no room for the copy: the caller runs the graph form
-    }
-    m->sell_meta = dmeta;
-    m->sell_col = dcol;
-    m->sell_val = dval;
-    m->sell_len = off;
-  }
-  k_sell_fill<<<blocks, 256, 0, s>>>(n, nslices, m->rp, m->col, m->val, reinterpret_cast<const int2*>(m->sell_meta),
-                                     m->sell_col, m->sell_val);
-  ctx->launches++;
-  return check_launch(ctx, "sell fill");
-}
-
 // Rows of at most 32 entries (the SELL-32 SpMV's limit). Measured against the graph form: 40.6 against
 // 51.7 us per iteration for the L2-resident SWIPDG system of 256^2 squares, and 209 against 264 us
 // for the 128^3 Q1 system (727.7 MB streamed from HBM per SpMV), same iteration counts: AUTO takes it
@@ -973,7 +929,8 @@ gdt_status pcg_persistent(gdt_context ctx, gdt_matrix m, double* x, double* r, d
   const int needed = (nslices + PT / 32 - 1) / (PT / 32);
   if (needed < blocks) blocks = std::max(1, needed);
   {
-    const gdt_status ss = sell_prepare(ctx, m, s);
+    // the values are copied at every solve: the caller may have written them through the CSR pointer
+    const gdt_status ss = sell_prepare(ctx, m, s, true);
     if (ss != GDT_OK) return ss;
   }
   PcgArgs a;
@@ -1031,7 +988,7 @@ __global__ void k_probe(int n, double* __restrict__ a, double* __restrict__ b) {
 gdt_status tune_cg(gdt_context ctx, gdt_matrix m, const Launch& L0, cudaStream_t s) {
   if (m->cg_sched >= 0) return GDT_OK;
   if (m->pinned) {
-    m->cg_sched = m->spmv_sched;
+    m->cg_sched = m->use_sell ? kSellSchedule : m->spmv_sched;
     return GDT_OK;
   }
   const int n = int(m->rows);
@@ -1052,10 +1009,11 @@ gdt_status tune_cg(gdt_context ctx, gdt_matrix m, const Launch& L0, cudaStream_t
   ctx->timing = 0;
   float best = FLT_MAX;
   int best_sched = m->spmv_sched;
-  for (int sched = 0; sched < kSchedules; ++sched) {
-    if (!schedule_valid(sched, m->max_row)) continue;
+  const bool sell = sell_prepare(ctx, m, s, true) == GDT_OK;
+  for (int sched = 0; sched <= kSellSchedule; ++sched) {
+    if (sched < kSchedules ? !schedule_valid(sched, m->max_row) : !sell) continue;
     Launch L = L0;
-    L.sched = sched;
+    L.sched = sched < kSchedules ? sched : L0.sched;
     KState init{};
     init.rho = 1.0;
     init.rr0 = 1.0;
@@ -1068,7 +1026,8 @@ gdt_status tune_cg(gdt_context ctx, gdt_matrix m, const Launch& L0, cudaStream_t
     bool ok = true;
     for (int it = 0; it < 5; ++it) {
       cudaEventRecord(e0, s);
-      spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
+      if (sched == kSellSchedule) spmv_cg_sell(L, m, p, q, st);
+      else spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
       cudaEventRecord(e1, s);
       k_cg_update_jacobi2<<<pair_blocks, TH, 0, s>>>(n, x, p, r, q, d, st, L.partials, L.ticket);
       k_cg_p_jacobi2<<<pair_blocks, TH, 0, s>>>(n, p, r, d, st);
@@ -1201,14 +1160,17 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
         if (!persistent) {
           ctx->last_solver_launch = GDT_SOLVER_LAUNCH_GRAPH;
           GDT_CHECK(ctx, tune_cg(ctx, m, L, s));
-          L.sched = m->cg_sched;
+          // the SELL copy is refreshed at every solve (the caller may have written the CSR values)
+          const bool cg_sell = m->cg_sched == kSellSchedule && sell_prepare(ctx, m, s, true) == GDT_OK;
+          L.sched = m->cg_sched == kSellSchedule ? m->spmv_sched : m->cg_sched;
           residual_init<double>(L, m->rp, m->col, m->val, x, b, r, one, p, st);
           // pairs of rows per thread when every vector is 16-byte aligned (the solver's own are; x is
           // the caller's)
           const bool pairs = (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
           const int pair_blocks = std::max(1, std::min(grid_blocks((n + 1) / 2, TH), ctx->num_sms * 8));
           GDT_CHECK(ctx, iterate_chunks(ctx, s, &st->converged, chunk_used, max_chunks, [&] {
-            spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
+            if (cg_sell) spmv_cg_sell(L, m, p, q, st);
+            else spmv_mode<double, 1>(L, m->rp, m->col, m->val, p, q, nullptr, st);
             timing_begin(ctx, s, GDT_TIMING_CG_UPDATE);
             if (pairs)
               k_cg_update_jacobi2<<<pair_blocks, TH, 0, s>>>(n, x, p, r, q, one, st, L.partials, L.ticket);

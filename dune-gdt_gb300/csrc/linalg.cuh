@@ -204,6 +204,63 @@ __device__ __forceinline__ void for_rows_async(int n, const int* __restrict__ rp
   }
 }
 
+// SELL-32 copy of a CSR matrix: slices of 32 consecutive rows, each stored column-major and padded
+// to the slice's longest row: entry t of row 32 s + l sits at meta[s].x + 32 t + l (meta[s].y = the
+// slice's width); padding entries hold 0 and the row's own index as column. One warp owns a slice
+// and a lane owns a row, so every load instruction of the warp reads 32 consecutive values
+// (256 bytes) or columns (128 bytes), and the FP64 instructions of a row are its FMAs only (no
+// shuffle reductions as in vector CSR).
+struct SellView {
+  int n, nslices;
+  const int2* meta;
+  const int* col;
+  const double* val;
+};
+
+// Warp-uniform loop over the slices, one warp per slice (grid-stride): body(row, active, s, wr) runs
+// in every lane with s = (A x)[row]; with HASW, wr = w[row] is loaded before the row's gathers (the
+// dot partner of a fused reduction), else 0. Entries are consumed 9 at a time (the 27 of a 3D Q1
+// row are three full groups), all 9 value/column loads issued before the first FMA, then one at a
+// time for the rest of the slice's width.
+template <bool HASW = false, class Body>
+__device__ __forceinline__ void for_slices(const SellView& A, const double* __restrict__ x, Body body,
+                                           const double* __restrict__ w = nullptr) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int slice = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); slice < A.nslices; slice += warps) {
+    const int2 md = __ldg(A.meta + slice);
+    const int row = slice * 32 + lane;
+    const bool active = row < A.n;
+    const double wr = (HASW && active) ? w[row] : 0.0;
+    const double* v = A.val + md.x + lane;
+    const int* c = A.col + md.x + lane;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    int t = 0;
+    for (; t + 9 <= md.y; t += 9) {
+      double vv[9];
+      int cc[9];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        vv[j] = ld_stream(v + (t + j) * 32);
+        cc[j] = ld_stream(c + (t + j) * 32);
+      }
+#pragma unroll
+      for (int j = 0; j < 9; j += 3) {
+        s0 = fma(vv[j], __ldg(x + cc[j]), s0);
+        s1 = fma(vv[j + 1], __ldg(x + cc[j + 1]), s1);
+        s2 = fma(vv[j + 2], __ldg(x + cc[j + 2]), s2);
+      }
+    }
+    for (; t < md.y; ++t) s0 = fma(ld_stream(v + t * 32), __ldg(x + ld_stream(c + t * 32)), s0);
+    body(row, active, (s0 + s1) + s2, wr);
+  }
+}
+
+// the SELL-32 copy of m (spmv.cu; sell_prepare must have succeeded) and the grid of its SpMV kernels
+// (blocks of 256 threads, one resident wave)
+SellView sell_view(gdt_matrix m);
+int sell_blocks(long long nslices, int num_sms);
+
 // SpMV schedules: PL == 0 -> vector-CSR with G lanes per row; PL > 0 -> pipelined warp staging with
 // PL entries per lane; PL < 0 -> asynchronous double-buffered staging for rows of at most -PL
 // entries. Chosen per matrix by the autotuner.

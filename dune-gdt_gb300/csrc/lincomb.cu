@@ -119,6 +119,7 @@ gdt_status gdt_matrix_lincomb(gdt_context ctx, gdt_matrix out, int nterms, const
     t.theta[q] = theta[q];
   }
   out->mf_valid = 0;
+  out->val_version++;
   return lincomb(ctx, out->nnz, t, out->val);
 }
 

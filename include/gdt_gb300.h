@@ -152,15 +152,26 @@ gdt_status gdt_matrix_device_arrays(gdt_matrix m, const int32_t** row_ptr, const
 gdt_status gdt_matrix_set_zero(gdt_context ctx, gdt_matrix m);
 /* SpMV schedule autotuner (no reference counterpart; the reference's ISTL BCRS has one schedule):
  * times every valid SpMV schedule on this matrix with CUDA events and keeps the fastest for all
- * SpMV-type kernels of the matrix. Runs automatically on the first SpMV-type call; schedule (may be
- * NULL) receives the chosen index, times_ms (may be NULL, GDT_SPMV_SCHEDULES entries) the measured ms
- * per launch of each schedule (-1 where a schedule does not apply). */
+ * SpMV-type kernels of the matrix. Schedules 0-7 read the CSR arrays (vector CSR with 4/8/16/32
+ * lanes per row; warp staging of up to 8/16/32 entries per row; cp.async staging of up to 28);
+ * schedule 8 (GDT_SPMV_SCHEDULE_SELL32) reads a SELL-32 copy of the matrix (slices of 32 rows stored
+ * column-major, one lane per row; 12 bytes per padded entry held besides the CSR arrays). When it is
+ * the fastest, the plain SpMV and the graph-form CG SpMV read the copy and the other kernels keep
+ * the fastest CSR schedule. Runs automatically on the first SpMV-type call; schedule (may be NULL)
+ * receives the chosen index, times_ms (may be NULL, GDT_SPMV_SCHEDULES entries) the measured ms per
+ * launch of each schedule (-1 where a schedule does not apply). */
 gdt_status gdt_matrix_tune(gdt_context ctx, gdt_matrix m, int* schedule, double* times_ms);
 /* Pins the SpMV schedule of m (0 .. GDT_SPMV_SCHEDULES-1; no reference counterpart) instead of
  * tuning it. GDT_EINVAL when the index is out of range or the schedule cannot hold the matrix's
  * longest row (the staged schedules take rows of at most 8, 16, 32 and 28 entries). */
-#define GDT_SPMV_SCHEDULES 8
+#define GDT_SPMV_SCHEDULES 9
+#define GDT_SPMV_SCHEDULE_SELL32 8
 gdt_status gdt_matrix_set_schedule(gdt_matrix m, int schedule);
+/* The copy of the values kept for the SELL-32 schedule follows every change the library makes
+ * (assembly, constraints, lincomb, set_zero) and every gdt_matrix_device_arrays call that returns the
+ * value pointer. A caller that writes values through a pointer obtained earlier calls this before
+ * the next gdt_spmv (no reference counterpart; solves copy the values afresh in any case). */
+gdt_status gdt_matrix_values_changed(gdt_matrix m);
 
 /* ----------------------------------------------------------------- assembly --- */
 typedef struct gdt_diffusion_desc {

@@ -3,7 +3,7 @@
 mixed-precision CG solvers (apply_inverse, operators/matrix-based.hh:131-159).
 
 The autotuner keeps whichever schedule is fastest on the GPU at hand, so each one has to be right on
-its own. Cases cover row lengths 7 (P1 2D), 12 (SWIPDG P1 2D), 15 (P1 3D) and 27 (Q1 3D), row counts
+its own. Schedule 8 reads a SELL-32 copy of the matrix, which has to follow every change of the values. Cases cover row lengths 7 (P1 2D), 12 (SWIPDG P1 2D), 15 (P1 3D) and 27 (Q1 3D), row counts
 that are not multiples of a warp, and sizes large enough that every warp of the staged schedules
 walks several row slices (the double-buffered path).
 """
@@ -98,3 +98,52 @@ def test_set_schedule_rejects_bad_indices(gdt):
     assert L.gdt_matrix_set_schedule(prob.op.handle, 5) == gdt._capi.EINVAL
     with pytest.raises(gdt._capi.GdtError):
         prob.op.set_spmv_schedule(4)
+
+
+def test_sell_copy_follows_value_changes(gdt):
+    prob, A = _problem(gdt, "q1_3d_ragged")
+    op = prob.op
+    op.set_spmv_schedule(gdt._capi.SPMV_SCHEDULE_SELL32)
+    x = np.random.default_rng(5).standard_normal(A.shape[1])
+    xd = torch.tensor(x, device="cuda")
+
+    def check(ref):
+        y = op.apply(xd).cpu().numpy()
+        y_ref = ref @ x
+        assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max()
+
+    check(A)
+    # a new assembly
+    kappa2 = torch.tensor(np.exp(np.random.default_rng(9).standard_normal(prob.grid.num_elements)), device="cuda")
+    prob.assemble(kappa2)
+    rp, col, val = op.csr()
+    A2 = sp.csr_matrix((val.cpu().numpy(), col.cpu().numpy(), rp.cpu().numpy()), shape=A.shape)
+    assert abs(A2 - A).max() > 0
+    check(A2)
+    # values written through a fresh view (csr() marks the values as changed)
+    op.csr()[2].mul_(2.0)
+    check(2.0 * A2)
+    # values written through a view taken before an apply: values_changed() tells the library
+    view = op.csr()[2]
+    check(2.0 * A2)
+    view.mul_(0.5)
+    op.values_changed()
+    check(A2)
+
+
+@pytest.mark.parametrize("case", ["q1_3d_large", "swipdg_p1_2d"])
+def test_graph_form_cg_on_the_sell_copy(gdt, case):
+    import scipy.sparse.linalg as spl
+
+    prob, A = _problem(gdt, case)
+    op = prob.op
+    op.set_spmv_schedule(gdt._capi.SPMV_SCHEDULE_SELL32)
+    op.ctx.set_solver_launch("graph")
+    try:
+        u = op.apply_inverse(prob.rhs, opts={"tol": 1e-12, "precond": "jacobi"})
+        info = dict(op.last_solve_info)
+    finally:
+        op.ctx.set_solver_launch("auto")
+    assert info["launch"] == "graph" and info["converged"]
+    xd = spl.spsolve(A.tocsc(), prob.rhs.cpu().numpy())
+    assert np.abs(u.cpu().numpy() - xd).max() <= 1e-10 * np.abs(xd).max()
