@@ -4,12 +4,18 @@
 piecewise constant and lognormal exp(N(0,1)) per cell (seeded), homogeneous Dirichlet boundary.
 
 One step = assemble (stiffness + load + Dirichlet, one fused pass) + solve to 1e-8 relative error
-(CG + Jacobi). `value` is the mixed-precision form (FP32 inner CG, FP64 iterative refinement),
-inputs resident in HBM; the plain FP64 GPU path runs on the same inputs for comparison; `e2e` runs
-the same step through the public API with kappa copied in from pinned host memory and the solution
-copied back every step. Data: synthetic (seeded); the reference publishes no dataset for this path.
+(CG + Jacobi to a relative residual of 1e-11). `value` is the mixed-precision form (FP32 inner CG,
+FP64 reliable updates), inputs resident in HBM; the plain FP64 GPU path runs on the same inputs;
+`e2e` runs the same step through the public API with kappa copied in from pinned host memory and the
+solution copied back every step. Data: synthetic (seeded); the reference publishes no dataset.
 
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+The same line carries the rest of the metric: the FP64 SpMV (standalone ConstMatrixOperator::apply
+and inside the CG iteration) against the HBM roofline, the batched parametric solve (512 uneven P1
+problems in one persistent launch), the 2D Burgers FV step (4096^2, and 64 x 512^2 batched), each with
+its roofline, a CPU baseline and a parity check against the oracle, and `parity` for the headline
+workload itself (pattern, matrix, right-hand side and solutions against the oracle's at 128^3).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--config ...]
 Under torchrun (N > 1) every rank solves its own instance (weak scaling, no collective on the path).
 """
 from __future__ import annotations
@@ -32,7 +38,12 @@ sys.path.insert(0, ROOT)
 METRIC = "DoF/s assembled+solved at 1e-8 rel err: mixed/batched vs FP64 GPU; SpMV GB/s"
 # kernel classes timed by gdt_context_kernel_timing, in GDT_TIMING_* order
 KERNEL_CLASSES = ["spmv_fp64", "spmv_fp32", "cg_update", "cg_direction", "reliable_update"]
+SCHEDULE_NAMES = ["csr_vector_g4", "csr_vector_g8", "csr_vector_g16", "csr_vector_g32", "warp_staged_pl8",
+                  "warp_staged_pl16", "warp_staged_pl32", "async_staged_28", "sell32"]
 SEED = 20261205
+L2_NOTE = ("not needed: every step assembles and streams the 685 MB FP64 CSR matrix (again in each FP64 "
+           "residual replacement), far more than the 129 MB L2; within a step the inner FP32 iteration's "
+           "working set stays L2-resident by design")
 
 
 def parse():
@@ -43,13 +54,13 @@ def parse():
     p.add_argument("--impl", default="gdt", choices=["gdt", "reference"])
     p.add_argument("--n", type=int, default=128, help="cells per axis")
     p.add_argument("--tol", type=float, default=1e-11, help="relative residual stop of both solvers")
-    p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-iters", type=int, default=60, help="CG iterations timed in the CPU sample")
-    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg", "q2"],
-                   help="heat3d: the headline 128^3 workload; batched: 512 parametric P1 problems of uneven "
-                        "size in one persistent launch; fv: 2D Burgers FV, SSP-RK2; swipdg: SWIPDG P1 "
-                        "forward solve + adjoint log-kappa gradient on 256^2 squares; q2: 3D Q2 assembly "
-                        "(tensor-core local matrices, diffusion at quadrature points) + solve")
+    p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU legs (baseline and parity)")
+    p.add_argument("--headline-only", action="store_true", help="default config without the extra metric keys")
+    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg", "q2", "peaks"],
+                   help="heat3d: the headline 128^3 workload (with the other metric keys); batched: 512 "
+                        "parametric P1 problems of uneven size in one persistent launch; fv: 2D Burgers FV, "
+                        "SSP-RK2; swipdg: SWIPDG P1 forward solve + adjoint log-kappa gradient on 256^2 "
+                        "squares; q2: 3D Q2 assembly + solve; peaks: FP64 FMA / tensor-core throughput")
     p.add_argument("--problems", type=int, default=512, help="batched: number of problems")
     p.add_argument("--fv-n", type=int, default=4096, help="fv: cells per axis")
     p.add_argument("--fv-steps", type=int, default=500, help="fv: SSP-RK2 steps per bench step")
@@ -63,6 +74,29 @@ def parse():
 def kappa_field(n):
     rng = np.random.default_rng(SEED)
     return np.exp(rng.standard_normal(n ** 3))
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def hbm_peak():
+    p = measured_peaks()
+    if "hbm_gbs" in p:
+        return float(p["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    return 6800.0, "fallback 6.8 TB/s (of fallback)"
+
+
+def heat3d_config(n, ndof, nnz, tol, world, precision):
+    """The workload of both arms (identical apart from the precision of the GPU arm's `value`)."""
+    return {"workload": f"3D heat equation, {n}^3 Q1 hexes, lognormal kappa, f=1, Dirichlet 0; "
+                        "assemble + CG-Jacobi solve to 1e-8 rel error",
+            "dofs": ndof, "nnz": nnz, "tol_rel_residual": tol, "precision": precision, "l2_flush": L2_NOTE,
+            "parallelism": f"replicas x{world}"}
 
 
 # ------------------------------------------------------------------------------- clocks ---
@@ -85,6 +119,7 @@ class Clocks:
                                       stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        return self
 
     def stop(self):
         if self.p is None:
@@ -113,27 +148,77 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-# ------------------------------------------------------------------------------- CPU legs ---
-def cpu_sample(n, tol, iters, threads):
-    """The oracle (CPU restatement of the reference path) on the same workload: full assembly +
-    `iters` CG+Jacobi iterations, scaled to the iteration count the full solve needs."""
+def event_ms(fn, stream=None):
+    """fn() bracketed by CUDA events on `stream` (the current stream by default), milliseconds."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+# ------------------------------------------------------------------------ oracle (CPU) legs ---
+def oracle_heat3d(n, tol, threads, kappa):
+    """The oracle (CPU restatement of the reference path) on the headline workload: assembly and a full
+    CG-Jacobi solve to `tol`, timed, with `threads` host threads."""
     import oracle
 
     oracle.build()
     oracle.set_threads(threads)
     og = oracle.grid(3, [n, n, n], 0.0, 1.0)
-    kappa = kappa_field(n)
     t0 = time.perf_counter()
     A, b = oracle.assemble_cg(og, 1, kappa=kappa, force_const=1.0)
     t_asm = time.perf_counter() - t0
     t0 = time.perf_counter()
-    _, it, rr, _ = oracle.solve(A, b, tol=1e-300, max_iter=iters)
-    t_it = (time.perf_counter() - t0) / max(it, 1)
-    return A.n, t_asm, t_it
+    x, it, _, _ = oracle.solve(A, b, tol=tol, max_iter=200000)
+    t_solve = time.perf_counter() - t0
+    return A, b, x, it, t_asm, t_solve
+
+
+def heat3d_cpu_legs(args, n, kappa_host, gpu, threads):
+    """cpu_baseline (one full oracle step, all host threads) and parity at the full size: the GPU's
+    pattern, matrix and right-hand side against the oracle's, and the GPU solutions against an oracle
+    FP64 solve at 1e-14."""
+    import oracle
+
+    A, b, x_tol, it_tol, t_asm, t_solve = oracle_heat3d(n, args.tol, threads, kappa_host)
+    rp, col, val = gpu["csr"]
+    pattern = bool(np.array_equal(rp.astype(np.int64), A.row_ptr) and np.array_equal(col, A.col))
+    mat_rel = float(np.abs(val - A.val).max() / np.abs(A.val).max()) if pattern else None
+    rhs_rel = float(np.abs(gpu["rhs"] - b).max() / np.abs(b).max())
+    x_tight, it_tight, _, _ = oracle.solve(A, b, tol=1e-14, max_iter=400000)
+    scale = np.abs(x_tight).max()
+
+    def rel(u):
+        return float(np.abs(u - x_tight).max() / scale)
+
+    parity = {
+        "reference": "oracle (CPU restatement of the reference path) on the same seeded inputs",
+        "pattern_bit_exact": pattern,
+        "matrix_rel": mat_rel, "rhs_rel": rhs_rel,
+        "solution_fp64_tol1e-14_rel": rel(gpu["u_tight"]),
+        "solution_mixed_rel": rel(gpu["u_mixed"]), "solution_fp64_rel": rel(gpu["u_fp64"]),
+        "oracle_solution_tol_rel": rel(x_tol),
+        "oracle_iterations": {"tol": it_tol, "tol1e-14": it_tight},
+        "bars": {"pattern": "bit-exact", "matrix_rhs": 1e-12, "solution_tight": 1e-12, "solution_timed": 1e-8},
+    }
+    parity["pass"] = bool(pattern and mat_rel <= 1e-12 and rhs_rel <= 1e-12
+                          and parity["solution_fp64_tol1e-14_rel"] <= 1e-12
+                          and parity["solution_mixed_rel"] <= 1e-8 and parity["solution_fp64_rel"] <= 1e-8)
+    ndof = A.n
+    cpu = {"value": ndof / (t_asm + t_solve), "unit": "DoF/s", "cores": threads, "kind": "port",
+           "sample": f"one full step of the same workload: oracle assembly ({t_asm:.2f} s) + CG-Jacobi solve to "
+                     f"{args.tol:g} ({it_tol} iterations, {t_solve:.2f} s), {threads} host threads"}
+    return cpu, parity
 
 
 # --------------------------------------------------------------------------------- GPU arm ---
 def run_gdt(args):
+    import ctypes as C
+
     import torch
     import torch.distributed as dist
 
@@ -145,7 +230,7 @@ def run_gdt(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     gdt = importlib.import_module("dune-gdt_gb300")
     gdt._build.build()
-    gdt._capi.load()
+    lib = gdt._capi.load()
 
     def barrier():
         if world > 1:
@@ -163,14 +248,12 @@ def run_gdt(args):
     op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kappa))
     rhs = torch.zeros(ndof, dtype=torch.float64, device="cuda")
     u = torch.zeros(ndof, dtype=torch.float64, device="cuda")
-    # FP64 reference solution at a tight tolerance (untimed) for the error statement
     op.assemble(rhs=rhs, force=1.0, dirichlet=True)
-    import ctypes as C
-
     sched = C.c_int()
-    sched_ms = (C.c_double * 8)()
+    sched_ms = (C.c_double * len(SCHEDULE_NAMES))()
     ctx.call("gdt_matrix_tune", op.handle, C.byref(sched), sched_ms)
-    u_ref = op.apply_inverse(rhs, opts={"tol": 1e-14, "max_iter": 200000}).clone()
+    # FP64 reference solution at a tight tolerance (untimed) for the error statement
+    u_tight = op.apply_inverse(rhs, opts={"tol": 1e-14, "max_iter": 200000}).clone()
 
     def step(precision):
         op.assemble(rhs=rhs, force=1.0, dirichlet=True)
@@ -180,7 +263,6 @@ def run_gdt(args):
     def timed(precision, steps, warmup, timing=False):
         for _ in range(warmup):
             step(precision)
-        lib = gdt._capi.load()
         lib.gdt_context_set_timing(ctx.handle, int(timing))
         lib.gdt_context_spmv_timing(ctx.handle, None, None, None, None, 1)
         launches0 = ctx.kernel_launches
@@ -194,8 +276,6 @@ def run_gdt(args):
         barrier()
         ms = e0.elapsed_time(e1) / steps
         launches = ctx.kernel_launches - launches0
-        import ctypes as C
-
         kinds = {}
         for k, name in enumerate(KERNEL_CLASSES):
             t, c = C.c_double(), C.c_int64()
@@ -204,23 +284,32 @@ def run_gdt(args):
                 kinds[name] = (t.value, c.value)
         lib.gdt_context_set_timing(ctx.handle, 0)
         info = dict(op.last_solve_info)
-        err = ((u - u_ref).abs().max() / u_ref.abs().max()).item()
+        err = ((u - u_tight).abs().max() / u_tight.abs().max()).item()
         return ms, launches, info, err, kinds
 
     # inputs are larger than L2 (FP64 CSR 728 MB per SpMV), so no L2 flush is needed between steps.
-    # The timed steps run the solvers as launched in production (iterations captured in CUDA graphs);
-    # one further step per precision, outside the timed region, brackets every kernel class with
-    # CUDA events (no graph capture) for the roofline and the per-kernel breakdown.
-    clocks = Clocks(local)
-    clocks.start()
+    # The timed steps run the solvers as launched in production; one further step per precision,
+    # outside the timed region, brackets every kernel class with CUDA events (no graph capture, the
+    # FP64 CG in its graph form) for the roofline and the per-kernel breakdown.
+    clocks = Clocks(local).start()
     ms_mixed, launches, info_mixed, err_mixed, _ = timed("mixed", args.steps, args.warmup)
     clk = clocks.stop()
+    u_mixed = u.cpu().numpy() if rank == 0 else None
     ms_fp64, _, info_fp64, err_fp64, _ = timed("fp64", max(1, args.steps // 2), 1)
+    u_fp64 = u.cpu().numpy() if rank == 0 else None
     _, _, _, _, kinds32 = timed("mixed", 1, 0, timing=True)
-    _, _, _, _, kinds64 = timed("fp64", 1, 0, timing=True)
-    # replicas: units of all ranks over the slowest rank's time (no collective on the data path)
+    _, _, info_fp64_graph, _, kinds64 = timed("fp64", 1, 0, timing=True)
     ms_mixed = gdt.replicas.max_over_ranks(ms_mixed, device="cuda")
     ms_fp64 = gdt.replicas.max_over_ranks(ms_fp64, device="cuda")
+
+    # standalone FP64 SpMV (ConstMatrixOperator::apply) on the tuned schedule: back-to-back launches,
+    # each streaming the 728 MB matrix from HBM (5.6x the L2)
+    xs = torch.rand(ndof, dtype=torch.float64, device="cuda")
+    ys = torch.empty_like(xs)
+    for _ in range(3):
+        op.apply(xs, ys)
+    reps = 20
+    spmv_ms = event_ms(lambda: [op.apply(xs, ys) for _ in range(reps)], ctx.stream) / reps
 
     # end to end through the public API: host kappa (pinned) -> device, assemble + solve, solution -> host
     kappa_pinned = torch.tensor(kappa_host).pin_memory()
@@ -248,9 +337,7 @@ def run_gdt(args):
 
     value = world * ndof / (ms_mixed / 1e3)
     inner = info_mixed.get("inner_operator")
-    # algorithmic bytes per launch of each kernel class of the mixed iteration (stencil path: 14 slot
-    # arrays = diagonal + 13 upper neighbours of the 27-point stencil, p read, q written; update x32,
-    # p, r32, q, 1/diag read, x32, r32 written; direction p, r32, 1/diag read, p written)
+    # algorithmic bytes per launch of each kernel class of the mixed iteration
     if inner == "matrix_free":
         # Chronopoulos-Gear iteration: operator w = A z with r.z, z.w, r.r (coefficients, z, own r read,
         # w written); one vector update p, s, x, r, z (z, p, w, s, x, r, 1/diag read; p, s, x, r, z written)
@@ -261,13 +348,7 @@ def run_gdt(args):
         classes = {"spmv_fp32": ("k_mx_spmv3d / k_mx_spmv: FP32 symmetric-stencil SpMV", (14 + 2) * 4 * ndof),
                    "cg_update": ("k_mx_update: x, r, r.z, r.r", 28 * ndof),
                    "cg_direction": ("k_mx_p: p = z + beta p", 16 * ndof)}
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
+    hbm, hbm_src = hbm_peak()
     by_kernel = {}
     for cls, (kname, nbytes) in classes.items():
         t, c = kinds32.get(cls, (0.0, 0))
@@ -277,9 +358,26 @@ def run_gdt(args):
                               "total_ms": t, "achieved_gbs": nbytes / (ms_l / 1e3) / 1e9,
                               "frac": nbytes / (ms_l / 1e3) / 1e9 / hbm}
     dom = max(by_kernel, key=lambda k: by_kernel[k]["total_ms"])
-    t64b, n64b = kinds64.get("spmv_fp64", (0.0, 0))
-    spmv64_ms = t64b / max(n64b, 1)
+    # FP64 CSR SpMV: values + columns + row pointers + x + y = 727.7 MB at 128^3
     bytes64 = 12 * nnz + 4 * (ndof + 1) + 16 * ndof
+    t64b, n64b = kinds64.get("spmv_fp64", (0.0, 0))
+    spmv_iter_ms = t64b / max(n64b, 1)
+    chosen = SCHEDULE_NAMES[sched.value] if 0 <= sched.value < len(SCHEDULE_NAMES) else str(sched.value)
+    spmv = {
+        "bytes_per_spmv": bytes64,
+        "standalone": {"ms": spmv_ms, "gbs": bytes64 / (spmv_ms / 1e3) / 1e9,
+                       "frac": bytes64 / (spmv_ms / 1e3) / 1e9 / hbm, "schedule": chosen,
+                       "how": f"{reps} back-to-back gdt_spmv calls, CUDA events on the context stream"},
+        "in_iteration": {"ms": spmv_iter_ms if n64b else None,
+                         "gbs": bytes64 / (spmv_iter_ms / 1e3) / 1e9 if n64b else None,
+                         "frac": bytes64 / (spmv_iter_ms / 1e3) / 1e9 / hbm if n64b else None,
+                         "launches": n64b,
+                         "how": "the FP64 CG's SpMV launches of one graph-form solve in timing mode (CUDA events "
+                                "around each launch; the update and direction kernels run between them)"},
+        "peak": hbm, "peak_source": hbm_src, "target_frac": 0.7,
+        "autotuner_ms_per_launch": {name: round(sched_ms[k], 4) for k, name in enumerate(SCHEDULE_NAMES)
+                                    if sched_ms[k] > 0},
+    }
     line = {
         "metric": METRIC,
         "value": value,
@@ -293,54 +391,43 @@ def run_gdt(args):
         "vs_baseline": None,
         "dtype": "f64 (FP32 inner CG values/vectors, FP64 assembly, residual and refinement)",
         "data": "synthetic (seeded lognormal kappa per cell)",
-        "config": {"workload": f"3D heat equation, {n}^3 Q1 hexes, lognormal kappa, f=1, Dirichlet 0; "
-                               "assemble + CG-Jacobi solve to 1e-8 rel error",
-                   "dofs": ndof, "nnz": nnz, "precision": "mixed", "tol_rel_residual": args.tol,
-                   "l2_flush": "not needed: every step assembles and streams the 685 MB FP64 CSR matrix (again "
-                               "in each FP64 residual replacement), far more than the 129 MB L2; within a step "
-                               "the inner FP32 iteration's ~52 MB working set stays L2-resident by design",
-                   "parallelism": f"replicas x{world}"},
+        "config": heat3d_config(n, ndof, nnz, args.tol, world, "mixed"),
         "error_vs_fp64_reference": err_mixed,
         "solve": {"mixed": info_mixed, "fp64": info_fp64},
         "fp64_plain": {"ms_per_step": ms_fp64, "value": world * ndof / (ms_fp64 / 1e3), "error": err_fp64,
-                       "launch": info_fp64.get("launch"),
-                       "spmv_gbs": bytes64 / (spmv64_ms / 1e3) / 1e9 if n64b else None,
-                       "spmv_frac_of_hbm": (bytes64 / (spmv64_ms / 1e3) / 1e9) / hbm if n64b else None,
-                       "spmv_note": "spmv_gbs: the graph form's k_spmv, one CUDA-event pair per launch (timing mode "
-                                    "runs the graph kernels); the timed FP64 solves run in the form named by launch"},
+                       "launch": info_fp64.get("launch"), "iterations": info_fp64.get("iterations")},
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
-        "spmv_autotuner": {"chosen_schedule": sched.value,
-                           "ms_per_launch": {name: round(sched_ms[k], 4) for k, name in enumerate(
-                               ["csr_vector_g4", "csr_vector_g8", "csr_vector_g16", "csr_vector_g32",
-                                "warp_staged_pl8", "warp_staged_pl16", "warp_staged_pl32", "async_staged_28"]) if sched_ms[k] > 0}},
+        "spmv_fp64": spmv,
         "e2e": {"value": world * ndof / (ms_e2e / 1e3), "unit": "DoF/s", "h2d_bytes_per_step": 8 * grid.num_elements,
                 "d2h_bytes_per_step": 8 * ndof},
         "gpu_launches": launches,
         "kernel_ms_per_launch": {
             "mixed": {k: round(t / c, 5) for k, (t, c) in kinds32.items()},
-            "fp64": {k: round(t / c, 5) for k, (t, c) in kinds64.items()},
+            "fp64_graph_form": {k: round(t / c, 5) for k, (t, c) in kinds64.items()},
             "note": "CUDA events around each kernel class in one extra solve without graph capture"},
         "roofline": {"bound": "hbm", "kernel": by_kernel[dom]["kernel"],
                      "achieved": by_kernel[dom]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": by_kernel[dom]["frac"], "bytes_per_launch": by_kernel[dom]["bytes_per_launch"],
                      "avg_launch_ms": by_kernel[dom]["avg_launch_ms"], "launches": by_kernel[dom]["launches"],
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)", "traffic": None,
+                     "peak_source": hbm_src, "traffic": None,
                      "note": ("the inner iteration's working set stays L2-resident; the matrix-free operator is "
-                              "bound by instruction issue and load latency, not HBM "
-                              "(profiles/k_mf_column_128cube_ncu_full.md)") if inner == "matrix_free" else None},
+                              "bound by instruction issue and load latency, not HBM") if inner == "matrix_free"
+                     else None},
         "roofline_by_kernel": by_kernel,
         "inner_operator": inner,
         "clocks": clk,
     }
+    csr = [t.cpu().numpy() for t in op.csr()] if rank == 0 and not args.no_cpu_baseline else None
+    rhs_host = rhs.cpu().numpy() if rank == 0 else None
+    u_tight_host = u_tight.cpu().numpy() if rank == 0 else None
+    if not args.headline_only:
+        line["batched"] = batched_metrics(args, gdt, cpu=rank == 0 and not args.no_cpu_baseline, world=world)
+        line["fv"] = fv_metrics(args, gdt, args.fv_n, 1, cpu=rank == 0 and not args.no_cpu_baseline, world=world)
+        line["fv_batched"] = fv_metrics(args, gdt, 512, 64, cpu=rank == 0 and not args.no_cpu_baseline, world=world)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        nd, t_asm, t_it = cpu_sample(n, args.tol, args.cpu_iters, threads)
-        iters = info_fp64["iterations"]
-        t_total = t_asm + t_it * iters
-        line["cpu_baseline"] = {"value": nd / t_total, "unit": "DoF/s", "cores": threads, "kind": "port",
-                                "sample": f"oracle assembly of the full {n}^3 system + {args.cpu_iters} CG-Jacobi "
-                                          f"iterations, scaled to the {iters} iterations the FP64 solve needs "
-                                          f"(assembly {t_asm:.2f} s, {t_it * 1e3:.1f} ms/iteration)"}
+        gpu = {"csr": csr, "rhs": rhs_host, "u_tight": u_tight_host, "u_mixed": u_mixed, "u_fp64": u_fp64}
+        line["cpu_baseline"], line["parity"] = heat3d_cpu_legs(args, n, kappa_host, gpu, threads)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -355,14 +442,15 @@ def quadrant_kappa(n, mu):
     return np.repeat(mu[q], 2)
 
 
-def run_batched(args):
-    """512 parametric diffusion problems on P1 triangle meshes of side n in {64,128,256,512}
-    (uneven, seeded), kappa = mu_q per quadrant, mu ~ U[0.1, 10]: assemble + solve all in one
-    persistent launch (FP64 and mixed), against the plain FP64 GPU path problem by problem."""
+def batched_metrics(args, gdt, cpu=True, world=1, steps=None, warmup=None):
+    """512 parametric diffusion problems on P1 triangle meshes of side n in {64,128,256,512} (uneven,
+    seeded), kappa = mu_q per quadrant, mu ~ U[0.1, 10]: assemble + solve all in one persistent launch
+    (FP64 and mixed), against the plain FP64 GPU path problem by problem; CPU baseline and parity on
+    one problem per size class."""
     import torch
 
-    gdt = importlib.import_module("dune-gdt_gb300")
-    gdt._build.build()
+    steps = steps or min(args.steps, 3)
+    warmup = warmup or max(3, min(args.warmup, 3))
     rng = np.random.default_rng(SEED + 3)
     sides = rng.choice([64, 128, 256, 512], size=args.problems)
     mu = rng.uniform(0.1, 10.0, (args.problems, 4))
@@ -380,24 +468,22 @@ def run_batched(args):
         return e
 
     def timed(precision):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(args.steps):
-            b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000, wait=False)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
+        ms = event_ms(lambda: [b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000, wait=False)
+                               for _ in range(steps)]) / steps
         b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000)  # waits, fills last_info
-        return ms, dict(b.last_info), err(x)
+        its, _ = b.iterations()
+        return ms, dict(b.last_info), err(x), its
 
-    clocks = Clocks(0)
-    clocks.start()
-    ms_mixed, info_mixed, err_mixed = timed("mixed")
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0"))).start()
+    ms_mixed, info_mixed, err_mixed, its_mixed = timed("mixed")
     clk = clocks.stop()
-    ms_fp64, info_fp64, err_fp64 = timed("fp64")
+    ms_fp64, info_fp64, err_fp64, its_fp64 = timed("fp64")
+    x_fp64 = x.clone()
+    ms_mixed = gdt.replicas.max_over_ranks(ms_mixed, device="cuda")
+    ms_fp64 = gdt.replicas.max_over_ranks(ms_fp64, device="cuda")
     # plain FP64 GPU path, one problem after another (operators built beforehand, as a user would):
     # a stratified sample of `per_class` problems of every size, scaled by the class counts
     per_class = 4
@@ -405,43 +491,237 @@ def run_batched(args):
     sample = []
     for side in (64, 128, 256, 512):
         idx = np.nonzero(sides == side)[0]
-        pick = idx[:per_class]
         probs = []
-        for i in pick:
+        for i in idx[:per_class]:
             g = gdt.make_cube_grid([0, 0], [1, 1], [side, side], simplex=True)
             pr = gdt.DiffusionProblem(g, solver_opts={"tol": args.tol, "max_iter": 200000})
             k = torch.tensor(quadrant_kappa(side, mu[i]), device="cuda")
             pr.solve(k)  # warm-up (pattern tuning, first use)
             probs.append((pr, k))
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for pr, k in probs:
-            pr.solve(k)
-        e1.record()
-        torch.cuda.synchronize()
-        t_class = e0.elapsed_time(e1) / len(probs) * len(idx)
+        t_class = event_ms(lambda: [pr.solve(k) for pr, k in probs]) / len(probs) * len(idx)
         t_plain += t_class
         sample.append(f"{len(probs)} of {len(idx)} problems of side {side}")
-    line = {
+    # algorithmic bytes of the batched FP64 iteration: the 7-point stencil (7 values) and 6 vector
+    # words per DoF and iteration, all in FP64 (the kernel keeps a problem's data in its cluster's
+    # shared memory and L2 where it fits, so HBM is not its bound: it waits on cluster barriers)
+    offs = np.array(b.offsets)
+    sizes = np.diff(offs)
+    bytes_fp64 = float(np.sum(sizes * np.abs(its_fp64))) * 8 * (7 + 6)
+    hbm, hbm_src = hbm_peak()
+    out = {
         "metric": "batched DoF/s assembled+solved (512 uneven P1 problems, one persistent launch)",
-        "value": ndof / (ms_mixed / 1e3), "unit": "DoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 assembly + FP32 inner CG / FP64 refinement", "data": "synthetic (seeded sizes and mu)",
-        "config": {"workload": f"{args.problems} problems, side n uniform in {{64,128,256,512}}, P1 Kuhn triangles, "
-                               "kappa = mu_q per quadrant, mu ~ U[0.1,10], f=1, Dirichlet 0",
-                   "dofs": ndof, "tol_rel_residual": args.tol},
+        "value": world * ndof / (ms_mixed / 1e3), "unit": "DoF/s", "ms_per_step": ms_mixed, "steps": steps,
+        "warmup": warmup,
+        "config": {"workload": f"{args.problems} problems, side n uniform in {{64,128,256,512}}, P1 Kuhn "
+                               "triangles, kappa = mu_q per quadrant, mu ~ U[0.1,10], f=1, Dirichlet 0",
+                   "dofs": ndof, "tol_rel_residual": args.tol,
+                   "l2_flush": "not needed: each launch solves all 512 problems from their assembly (44.8 M DoF "
+                               "of FP64 vectors, ~2.5 GB of solver state) well past the 129 MB L2"},
         "batched_mixed": {"ms": ms_mixed, "error_vs_fp64_reference": err_mixed, **info_mixed},
-        "batched_fp64": {"ms": ms_fp64, "value": ndof / (ms_fp64 / 1e3), "error_vs_fp64_reference": err_fp64,
+        "batched_fp64": {"ms": ms_fp64, "value": world * ndof / (ms_fp64 / 1e3), "error_vs_fp64_reference": err_fp64,
                          **info_fp64},
         "plain_fp64_sequential": {"ms": t_plain, "value": ndof / (t_plain / 1e3),
                                   "sample": "; ".join(sample) + " (assemble + solve per problem, timed with CUDA "
                                                                 "events, scaled by the class counts)"},
         "speedup_batched_mixed_vs_plain_fp64": t_plain / ms_mixed,
         "speedup_batched_fp64_vs_plain_fp64": t_plain / ms_fp64,
+        "roofline": {"bound": "latency (cluster barriers)", "kernel": "batch_kernel (FP64)",
+                     "achieved": bytes_fp64 / (ms_fp64 / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": bytes_fp64 / (ms_fp64 / 1e3) / 1e9 / hbm, "peak_source": hbm_src,
+                     "bytes": "13 FP64 words per DoF and CG iteration (7 stencil values, 6 vector accesses), "
+                              "summed over every problem's iterations", "traffic": None},
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    if cpu:
+        out["cpu_baseline"], out["parity"] = batched_cpu_legs(args, b, sides, mu, x_fp64)
+    return out
+
+
+def batched_cpu_legs(args, b, sides, mu, x_gpu):
+    """The oracle on one problem of every size class (assembly + CG-Jacobi to the same tolerance, all
+    host threads), scaled by the class counts; the same problems' GPU solutions against the oracle's."""
+    import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    t_total, errs, parts = 0.0, {}, []
+    for side in (64, 128, 256, 512):
+        idx = np.nonzero(sides == side)[0]
+        if len(idx) == 0:
+            continue
+        i = int(idx[0])
+        og = oracle.grid(2, [side, side], 0.0, 1.0, simplex=True)
+        t0 = time.perf_counter()
+        A, rhs = oracle.assemble_cg(og, 1, kappa=quadrant_kappa(side, mu[i]), force_const=1.0)
+        xo, it, _, _ = oracle.solve(A, rhs, tol=args.tol, max_iter=400000)
+        dt = time.perf_counter() - t0
+        t_total += dt * len(idx)
+        xt, _, _, _ = oracle.solve(A, rhs, x0=xo, tol=1e-6, max_iter=400000)  # polish past the stop test
+        xg = b.unpack(x_gpu, i).cpu().numpy()
+        errs[f"side_{side}"] = float(np.abs(xg - xt).max() / np.abs(xt).max())
+        parts.append(f"side {side}: {dt:.2f} s ({it} iterations) x {len(idx)}")
+    cpu = {"value": b.total_dofs / t_total, "unit": "DoF/s", "cores": threads, "kind": "port",
+           "sample": "oracle assembly + CG-Jacobi solve of one problem per size class, scaled by the class counts: "
+                     + "; ".join(parts)}
+    parity = {"reference": "oracle solution of the same problem (CG to the bench tolerance, then polished)",
+              "solution_fp64_rel": errs, "bar": 1e-8, "pass": bool(max(errs.values()) <= 1e-8)}
+    return cpu, parity
+
+
+def run_batched(args):
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    out = batched_metrics(args, gdt, cpu=not args.no_cpu_baseline, steps=args.steps, warmup=args.warmup)
+    out.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64 assembly + FP32 inner CG / FP64 refinement", "data": "synthetic (seeded sizes and mu)"})
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------- FV (config 5) ---
+def bumps(n, seed, count=32):
+    rng = np.random.default_rng(seed)
+    xc = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(xc, xc, indexing="xy")  # X varies along axis 1 (x fastest in the flat index)
+    u = np.zeros((n, n))
+    for _ in range(count):
+        a = rng.uniform(-1, 1)
+        w = rng.uniform(0.01, 0.1)
+        cx, cy = rng.uniform(0, 1, 2)
+        dx = np.minimum(np.abs(X - cx), 1 - np.abs(X - cx))
+        dy = np.minimum(np.abs(Y - cy), 1 - np.abs(Y - cy))
+        u += a * np.exp(-(dx * dx + dy * dy) / (2 * w * w))
+    return u.reshape(-1)
+
+
+# FP64 operations of one cell and SSP-RK2 stage of the LF Burgers flux, counted on the formula: per
+# face (two faces computed per cell) u^2 + v^2 (2), the LF term max(|u|,|v|) (u - v) (2) and their
+# sum (1); per cell the divergence of the two directions' face differences (3) and the stage update
+# (2 for stage 1, 3 for stage 2)
+FV_OPS_PER_CELL_STEP = 2 * (5 + 3) + 2 + 3
+
+
+def fv_metrics(args, gdt, n, nb, cpu=True, world=1, steps=None, warmup=None):
+    """2D inviscid Burgers on periodic n^2 cubes (nb initial conditions), FV P0, local LF flux, SSP-RK2
+    at CFL 0.5, fv_steps time steps per bench step."""
+    import torch
+
+    steps = steps or min(args.steps, 5)
+    warmup = warmup or max(3, min(args.warmup, 3))
+    g = gdt.make_cube_grid([0, 0], [1, 1], [n, n], periodic=True)
+    space = gdt.FiniteVolumeSpace(g)
+    op = gdt.AdvectionFvOperator(g, gdt.NumericalLaxFriedrichsFlux(gdt.BurgersFlux()), space)
+    u0 = np.concatenate([bumps(n, SEED + 5 + b) for b in range(nb)])
+    u0_t = torch.tensor(u0, device="cuda")
+    dt = 0.5 * min(gdt.estimate_dt_for_hyperbolic_system(g, u0_t[b * n * n:(b + 1) * n * n].contiguous(), op)
+                   for b in range(nb))
+    u = u0_t.clone()
+    stepper = gdt.ExplicitRungeKuttaTimeStepper(op, u, method="ssp2")
+    for _ in range(warmup):
+        u.copy_(u0_t)
+        stepper.step(dt, args.fv_steps)
+    torch.cuda.synchronize()
+    ms = []
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0"))).start()
+    for _ in range(steps):
+        u.copy_(u0_t)
+        torch.cuda.synchronize()
+        ms.append(event_ms(lambda: stepper.step(dt, args.fv_steps)))
+    clk = clocks.stop()
+    t = gdt.replicas.max_over_ranks(sum(ms) / len(ms), device="cuda")
+    cells = n * n * nb
+    mass0 = u0_t.view(nb, -1).sum(1)
+    mass_err = ((u.view(nb, -1).sum(1) - mass0).abs() / mass0.abs()).max().item()
+    per_step_s = t / 1e3 / args.fv_steps
+    hbm, hbm_src = hbm_peak()
+    fma_tf, dmma_tf = fp64_peak(gdt)
+    bytes_step = 40 * cells  # fused SSP-RK2: read u twice and k0, write k0 and the next state
+    fp64_ops = FV_OPS_PER_CELL_STEP * cells / per_step_s
+    out = {
+        "metric": "FV cell-updates/s (2D Burgers, LF flux, SSP-RK2)", "value": world * cells / per_step_s,
+        "unit": "cell-updates/s", "ms_per_step": t, "steps": steps, "warmup": warmup,
+        "config": {"workload": f"{nb} x {n}^2 periodic cells, {args.fv_steps} SSP-RK2 steps per bench step, "
+                               "dt = 0.5 estimate_dt_for_hyperbolic_system", "dt": dt,
+                   "l2_flush": f"not needed: the states ({16 * cells / 1e6:.0f} MB with the stage vector) exceed "
+                               "the 129 MB L2"},
+        "rel_mass_conservation_error": mass_err,
+        "roofline": {"bound": "fp64 pipe", "kernel": "fv2d_tile (fused SSP-RK2 stages)",
+                     "achieved": bytes_step / per_step_s / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": bytes_step / per_step_s / 1e9 / hbm, "peak_source": hbm_src,
+                     "bytes_per_step": bytes_step, "traffic": None,
+                     "fp64": {"ops_per_cell_and_step": FV_OPS_PER_CELL_STEP, "achieved_tflops": fp64_ops / 1e12,
+                              "peak_tflops": fma_tf, "frac": fp64_ops / 1e12 / fma_tf if fma_tf else None,
+                              "peak_source": "gdt_measure_fp64_peak (FMA chains, this GPU, this run)"}},
+        "clocks": clk,
+    }
+    if cpu:
+        out["cpu_baseline"], out["parity"] = fv_cpu_legs(args, gdt, g, n, nb, u0, dt)
+    return out
+
+
+def fv_cpu_legs(args, gdt, g, n, nb, u0, dt, psteps=5):
+    """The oracle's SSP-RK2 (all host threads) on the first initial condition: a bounded number of steps
+    timed for the baseline, and `psteps` steps compared cell by cell with the GPU's."""
+    import torch
+
+    import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    og = oracle.grid(2, [n, n], 0.0, 1.0, periodic=True)
+    first = u0[: n * n]
+    t0 = time.perf_counter()
+    uo = oracle.fv_ssprk2(og, oracle.FLUX_BURGERS, oracle.NUMFLUX_LAX_FRIEDRICHS, first, dt, psteps)
+    t_cpu = time.perf_counter() - t0
+    space = gdt.FiniteVolumeSpace(g)
+    op = gdt.AdvectionFvOperator(g, gdt.NumericalLaxFriedrichsFlux(gdt.BurgersFlux()), space)
+    ug = torch.tensor(first, device="cuda")
+    gdt.ExplicitRungeKuttaTimeStepper(op, ug, method="ssp2").step(dt, psteps)
+    rel = float(np.abs(ug.cpu().numpy() - uo).max() / np.abs(uo).max())
+    cpu = {"value": n * n * psteps / t_cpu, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+           "sample": f"oracle SSP-RK2, {psteps} steps on one {n}^2 state ({t_cpu:.2f} s)"}
+    parity = {"reference": f"oracle SSP-RK2, {psteps} steps from the same initial state", "state_rel": rel,
+              "bar": 1e-12, "pass": bool(rel <= 1e-12)}
+    return cpu, parity
+
+
+def run_fv(args):
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    out = fv_metrics(args, gdt, args.fv_n, args.fv_batch, cpu=not args.no_cpu_baseline, steps=args.steps,
+                     warmup=args.warmup)
+    out.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (32 seeded Gaussian bumps per state)"})
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------------- FP64 peak probe ---
+_PEAK = {}
+
+
+def fp64_peak(gdt):
+    """Measured FP64 FMA and DMMA throughput (TFLOP/s) of this GPU, once per process."""
+    import ctypes as C
+
+    if "fp64" not in _PEAK:
+        ctx = gdt.default_context()
+        f, d = C.c_double(), C.c_double()
+        ctx.call("gdt_measure_fp64_peak", C.byref(f), C.byref(d))
+        _PEAK["fp64"] = (f.value, d.value)
+    return _PEAK["fp64"]
+
+
+def run_peaks(args):
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    clocks = Clocks(0).start()
+    fma_tf, dmma_tf = fp64_peak(gdt)
+    clk = clocks.stop()
+    print(json.dumps({"metric": "FP64 throughput (TFLOP/s)", "fma_tflops": fma_tf, "dmma_tflops": dmma_tf,
+                      "how": "gdt_measure_fp64_peak: independent FMA chains / m8n8k4 FP64 MMA chains, one resident "
+                             "wave on every SM, best of 3 after a warm-up, CUDA events", "clocks": clk}), flush=True)
 
 
 # ---------------------------------------------------------------------------- Q2 (next-1 row) ---
@@ -449,8 +729,6 @@ def run_q2(args):
     """-div(kappa grad u) = 1 on the unit cube, n^3 hexahedra, continuous Q2, Dirichlet 0; kappa at the
     quadrature points = exp(N(0,1)) per element x (1 + 0.5 sin(2 pi x) sin(2 pi y) sin(2 pi z)); one step =
     element-batched assembly (FP64 tensor cores) + load vector + Dirichlet + CG-Jacobi solve (FP64)."""
-    import ctypes as C
-
     import torch
 
     gdt = importlib.import_module("dune-gdt_gb300")
@@ -485,27 +763,16 @@ def run_q2(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    clocks = Clocks(0)
-    clocks.start()
-    ev[0].record()
-    for _ in range(args.steps):
-        step()
-    ev[1].record()
-    torch.cuda.synchronize()
+    clocks = Clocks(0).start()
+    ms = event_ms(lambda: [step() for _ in range(args.steps)]) / args.steps
     clk = clocks.stop()
-    ms = ev[0].elapsed_time(ev[1]) / args.steps
     info = dict(op.last_solve_info)
-    ev[2].record()
-    for _ in range(args.steps):
-        assemble()
-    ev[3].record()
-    torch.cuda.synchronize()
-    ms_asm = ev[2].elapsed_time(ev[3]) / args.steps
+    ms_asm = event_ms(lambda: [assemble() for _ in range(args.steps)]) / args.steps
     # the contraction's arithmetic: 2 flops per (pair, quadrature point, element), pairs i <= j
     L = space.max_local_size
     flops = 2.0 * (L * (L + 1) // 2) * nq * ne
     r = (op.apply(u) - rhs).norm().item() / rhs.norm().item()
+    fma_tf, dmma_tf = fp64_peak(gdt)
     line = {
         "metric": "Q2 DoF/s assembled+solved (3D, diffusion at quadrature points)",
         "value": ndof / (ms / 1e3), "unit": "DoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -517,6 +784,7 @@ def run_q2(args):
         "assembly_ms": ms_asm,
         "assembly_contraction_flops": flops,
         "assembly_tflops_upper_bound": flops / (ms_asm / 1e3) / 1e12,
+        "fp64_peak_tflops": {"fma": fma_tf, "dmma": dmma_tf},
         "solve": info, "final_rel_residual": r,
         "clocks": clk,
     }
@@ -547,8 +815,8 @@ def run_swipdg(args):
     logk = torch.tensor(logk_host, device="cuda")
 
     def J(lk):
-        u = gdt.DiffusionSolve.apply(lk, prob)
-        return 0.5 * torch.sum((u - u_d) ** 2)
+        uu = gdt.DiffusionSolve.apply(lk, prob)
+        return 0.5 * torch.sum((uu - u_d) ** 2)
 
     def step():
         lk = logk.clone().requires_grad_(True)
@@ -559,16 +827,11 @@ def run_swipdg(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    clocks = Clocks(0)
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        j, grad = step()
-    e1.record()
-    torch.cuda.synchronize()
+    clocks = Clocks(0).start()
+    res = {}
+    ms = event_ms(lambda: res.update(out=[step() for _ in range(args.steps)][-1])) / args.steps
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
+    j, grad = res["out"]
     iters = prob.op.last_solve_info["iterations"]
     launch = prob.op.last_solve_info.get("launch")
     # The system (64 MB) stays in L2, so the solves run as one cooperative launch each (all CG
@@ -584,12 +847,8 @@ def run_swipdg(args):
         try:
             x = torch.zeros_like(prob.rhs)
             torch.cuda.synchronize()
-            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a0.record(ctx.stream)
-            op.apply_inverse(prob.rhs, x, opts=prob.solver_opts)
-            a1.record(ctx.stream)
-            torch.cuda.synchronize()
-            return a0.elapsed_time(a1) / max(op.last_solve_info["iterations"], 1), op.last_solve_info["iterations"]
+            t = event_ms(lambda: op.apply_inverse(prob.rhs, x, opts=prob.solver_opts), ctx.stream)
+            return t / max(op.last_solve_info["iterations"], 1), op.last_solve_info["iterations"]
         finally:
             ctx.set_solver_launch("auto")
 
@@ -599,13 +858,7 @@ def run_swipdg(args):
     # algorithmic bytes of one CG iteration: SpMV (values, columns, row pointers, p gathered once, q)
     # + x/r update (p, q, x, r, dinv read; x, r written) + direction (p, r, dinv read; p written)
     bytes_it = 12 * nnz + 4 * (ndof + 1) + 16 * ndof + 8 * ndof * (7 + 4)
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
+    hbm, hbm_src = hbm_peak()
     # central differences on seeded elements, untimed: h = 1e-6 (the stated check) and h = 1e-4 (less
     # sensitive to the 1e-12 solver tolerance at this contrast); errors relative to max |gradient|
     grad_h = grad.detach().cpu().numpy()
@@ -638,90 +891,10 @@ def run_swipdg(args):
         "roofline": {"bound": "hbm", "kernel": "k_pcg_persistent: all CG iterations in one cooperative launch",
                      "achieved": bytes_it / (it_ms_persistent / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
                      "frac": bytes_it / (it_ms_persistent / 1e3) / 1e9 / hbm, "bytes_per_iteration": bytes_it,
-                     "ms_per_iteration": it_ms_persistent, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                     "traffic": None,
+                     "ms_per_iteration": it_ms_persistent, "peak_source": hbm_src, "traffic": None,
                      "note": "the 64 MB system stays in the 129 MB L2 across iterations, so HBM is not the bound: "
-                             "ncu shows the FP64 pipe active 64 % of cycles (about 21 FP64 operations per row and "
-                             "iteration: 12 in the SpMV) and the rest in the three grid barriers and reductions of "
-                             "an iteration (profiles/k_pcg_persistent_swipdg256_ncu_full.md)"},
-        "clocks": clk,
-    }
-    print(json.dumps(line), flush=True)
-
-
-# ---------------------------------------------------------------------------- FV (config 5) ---
-def bumps(n, seed, count=32):
-    rng = np.random.default_rng(seed)
-    xc = (np.arange(n) + 0.5) / n
-    X, Y = np.meshgrid(xc, xc, indexing="xy")  # X varies along axis 1 (x fastest in the flat index)
-    u = np.zeros((n, n))
-    for _ in range(count):
-        a = rng.uniform(-1, 1)
-        w = rng.uniform(0.01, 0.1)
-        cx, cy = rng.uniform(0, 1, 2)
-        dx = np.minimum(np.abs(X - cx), 1 - np.abs(X - cx))
-        dy = np.minimum(np.abs(Y - cy), 1 - np.abs(Y - cy))
-        u += a * np.exp(-(dx * dx + dy * dy) / (2 * w * w))
-    return u.reshape(-1)
-
-
-def run_fv(args):
-    """2D inviscid Burgers on periodic n^2 cubes, FV P0, local LF flux, SSP-RK2 at CFL 0.5."""
-    import torch
-
-    gdt = importlib.import_module("dune-gdt_gb300")
-    gdt._build.build()
-    n, nb = args.fv_n, args.fv_batch
-    g = gdt.make_cube_grid([0, 0], [1, 1], [n, n], periodic=True)
-    space = gdt.FiniteVolumeSpace(g)
-    op = gdt.AdvectionFvOperator(g, gdt.NumericalLaxFriedrichsFlux(gdt.BurgersFlux()), space)
-    u0 = np.concatenate([bumps(n, SEED + 5 + b) for b in range(nb)])
-    u0_t = torch.tensor(u0, device="cuda")
-    dt = 0.5 * min(gdt.estimate_dt_for_hyperbolic_system(g, u0_t[b * n * n:(b + 1) * n * n].contiguous(), op)
-                   for b in range(nb))
-    u = u0_t.clone()
-    stepper = gdt.ExplicitRungeKuttaTimeStepper(op, u, method="ssp2")
-    for _ in range(args.warmup):
-        u.copy_(u0_t)
-        stepper.step(dt, args.fv_steps)
-    torch.cuda.synchronize()
-    ms = []
-    clocks = Clocks(0)
-    clocks.start()
-    for _ in range(args.steps):
-        u.copy_(u0_t)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        stepper.step(dt, args.fv_steps)
-        e1.record()
-        torch.cuda.synchronize()
-        ms.append(e0.elapsed_time(e1))
-    clk = clocks.stop()
-    t = sum(ms) / len(ms)
-    cells = n * n * nb
-    mass0 = u0_t.view(nb, -1).sum(1)
-    mass_err = ((u.view(nb, -1).sum(1) - mass0).abs() / mass0.abs()).max().item()
-    per_step_s = t / 1e3 / args.fv_steps
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    bytes_step = 40 * cells  # fused SSP-RK2: read u twice and k0, write k0 and the next state
-    line = {
-        "metric": "FV cell-updates/s (2D Burgers, LF flux, SSP-RK2)", "value": cells * args.fv_steps / (t / 1e3),
-        "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (32 seeded Gaussian bumps per state)",
-        "config": {"workload": f"{nb} x {n}^2 periodic cells, {args.fv_steps} SSP-RK2 steps per bench step, "
-                               "dt = 0.5 estimate_dt_for_hyperbolic_system", "dt": dt},
-        "rel_mass_conservation_error": mass_err,
-        "roofline": {"bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s); HBM fraction shown",
-                     "achieved": bytes_step / per_step_s / 1e9, "peak": hbm, "unit": "GB/s",
-                     "frac": bytes_step / per_step_s / 1e9 / hbm, "bytes_per_step": bytes_step},
+                             "the FP64 pipe (about 21 FP64 operations per row and iteration, 12 in the SpMV) and "
+                             "the three grid barriers and reductions of an iteration are"},
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -729,54 +902,45 @@ def run_fv(args):
 
 # ----------------------------------------------------------------------------- reference arm ---
 def run_reference(args):
+    """The reference's CPU path (its restatement in the oracle: the reference needs DUNE modules absent
+    here) on the headline workload with all host threads: every step is the full assembly plus the full
+    CG-Jacobi solve to the same tolerance, timed as a whole, nothing extrapolated. One more step with
+    a single thread follows the timed ones."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     n = args.n
-    times = []
-    nd = 0
-    iters_needed = None
+    kappa = kappa_field(n)
+    times, its = [], []
+    nd = nnz = 0
     for s in range(args.warmup + args.steps):
-        nd, t_asm, t_it = cpu_sample(n, args.tol, args.cpu_iters, threads)
-        if iters_needed is None:
-            iters_needed = cg_iterations_needed(n, args.tol)
+        A, b, x, it, t_asm, t_solve = oracle_heat3d(n, args.tol, threads, kappa)
+        nd, nnz = A.n, A.nnz
+        del A, b, x
         if s >= args.warmup:
-            times.append(t_asm + t_it * iters_needed)
+            times.append(t_asm + t_solve)
+            its.append(it)
     ms = 1e3 * sum(times) / len(times)
     value = nd / (ms / 1e3)
+    _, _, _, it1, t_asm1, t_solve1 = oracle_heat3d(n, args.tol, 1, kappa)
     line = {
         "metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lognormal kappa per cell)",
-        "config": {"workload": f"3D heat equation, {n}^3 Q1 hexes, lognormal kappa, f=1, Dirichlet 0; "
-                               "assemble + CG-Jacobi solve to 1e-8 rel error", "dofs": nd, "precision": "fp64",
-                   "tol_rel_residual": args.tol, "parallelism": "host threads"},
+        "config": heat3d_config(n, nd, nnz, args.tol, 1, "fp64"),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "DoF/s", "cores": threads, "kind": "port",
-                         "sample": f"per step: full assembly + {args.cpu_iters} CG-Jacobi iterations, scaled to "
-                                   f"the {iters_needed} iterations of the full solve (the reference itself "
-                                   "needs DUNE modules absent here; the oracle restates its CPU path)"},
+                         "sample": f"every step: full oracle assembly + full CG-Jacobi solve to {args.tol:g} "
+                                   f"({its[-1]} iterations), {threads} host threads, timed as a whole (the "
+                                   "reference itself needs DUNE modules absent here; the oracle restates its "
+                                   "CPU path)"},
+        "best_ms_per_step": 1e3 * min(times),
+        "single_thread": {"ms_per_step": 1e3 * (t_asm1 + t_solve1), "value": nd / (t_asm1 + t_solve1),
+                          "assembly_s": t_asm1, "solve_s": t_solve1, "iterations": it1, "cores": 1},
         "e2e": {"value": value, "unit": "DoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
-
-
-_ITER_CACHE = {}
-
-
-def cg_iterations_needed(n, tol):
-    """CG+Jacobi iterations of the full solve, from a one-off oracle solve on a coarse proxy would be
-    inexact; instead run the full oracle solve once (untimed) and reuse its count."""
-    key = (n, tol)
-    if key not in _ITER_CACHE:
-        import oracle
-
-        og = oracle.grid(3, [n, n, n], 0.0, 1.0)
-        A, b = oracle.assemble_cg(og, 1, kappa=kappa_field(n), force_const=1.0)
-        _, it, _, _ = oracle.solve(A, b, tol=tol, max_iter=100000)
-        _ITER_CACHE[key] = it
-    return _ITER_CACHE[key]
 
 
 if __name__ == "__main__":
@@ -791,5 +955,7 @@ if __name__ == "__main__":
         run_swipdg(a)
     elif a.config == "q2":
         run_q2(a)
+    elif a.config == "peaks":
+        run_peaks(a)
     else:
         run_gdt(a)

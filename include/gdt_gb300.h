@@ -96,6 +96,10 @@ gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp
 /* accumulated time (ms) and launch count of one kernel class since its last reset (all classes are
  * reset by gdt_context_spmv_timing with reset = 1) */
 gdt_status gdt_context_kernel_timing(gdt_context ctx, int kind, double* ms, int64_t* launches, int reset);
+/* FP64 throughput of the context's GPU in TFLOP/s, measured with CUDA events on the context stream
+ * (no reference counterpart; the denominator of FP64-bound rooflines): independent FMA chains on
+ * every SM (fma_tflops) and m8n8k4 FP64 tensor-core products (dmma_tflops). Either may be NULL. */
+gdt_status gdt_measure_fp64_peak(gdt_context ctx, double* fma_tflops, double* dmma_tflops);
 
 /* How gdt_solve runs FP64 CG with Jacobi or no preconditioner (no reference counterpart: the launch
  * form of the device solver). GRAPH: one kernel per step (SpMV, update, direction), iterations
