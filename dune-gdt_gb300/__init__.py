@@ -26,7 +26,7 @@ __all__ = [
     "Walker", "DiscreteFunction", "BurgersFlux", "LinearTransportFlux", "NumericalLaxFriedrichsFlux",
     "NumericalUpwindFlux", "NumericalEngquistOsherFlux", "AdvectionFvOperator", "BoundaryTreatmentByCustomExtrapolation",
     "BoundaryTreatmentByCustomNumericalFlux", "ExplicitRungeKuttaTimeStepper",
-    "estimate_dt_for_hyperbolic_system", "GdtError", "element_error", "LincombOperator", "lincomb",
+    "estimate_dt_for_hyperbolic_system", "GdtError", "element_error", "LincombOperator", "lincomb", "GridFunction",
 ]
 
 
@@ -286,6 +286,42 @@ def _coef_qp(c):
     return t, k, None
 
 
+class GridFunction:
+    """A function of the global point x with its polynomial order, as dune-xt's
+    GenericFunction(order, lambda) (examples/stationary-heat-equation.cc:68-70): `fn` maps a float64
+    tensor of points [..., dim] to the values [...]. As the source of a load vector it is evaluated at
+    the points of the Gauss rule of order `order` + the space's order (the reference's product
+    integrand at its own quadrature points), not sampled per element."""
+
+    def __init__(self, fn, order=3):
+        self.fn = fn
+        self.order = int(order)
+
+    def at_quadrature_points(self, space):
+        quad_order = self.order + space.order
+        pts = space.quadrature_points(order=quad_order)
+        vals = self.fn(pts)
+        vals = torch.as_tensor(vals, dtype=torch.float64, device=pts.device)
+        if tuple(vals.shape) != tuple(pts.shape[:2]):
+            raise ValueError(f"GridFunction returned shape {tuple(vals.shape)}, expected {tuple(pts.shape[:2])}")
+        return vals.contiguous(), quad_order
+
+
+def _force_fields(d, force, space):
+    """Sets force / force_const / force_qp / force_quad_order of a DiffusionDesc; returns the tensors
+    that must stay alive while the descriptor is used."""
+    if isinstance(force, GridFunction):
+        vals, quad_order = force.at_quadrature_points(space)
+        d.force, d.force_const = None, 0.0
+        d.force_qp, d.force_quad_order = vals.data_ptr(), quad_order
+        return [vals]
+    ft, fc = _coef(force)
+    d.force = ft.data_ptr() if ft is not None else None
+    d.force_const = fc
+    d.force_qp, d.force_quad_order = None, 0
+    return [ft]
+
+
 class LocalLaplaceIntegrand:
     def __init__(self, diffusion=1.0):
         self.diffusion = diffusion
@@ -450,10 +486,7 @@ class MatrixOperator:
         d.kappa = kt.data_ptr() if kt is not None else None
         d.kappa_const = kc
         d.kappa_qp = kq.data_ptr() if kq is not None else None
-        self._keep = [kt, kq]
-        ft, fc = _coef(1.0 if rhs_force is None else rhs_force)
-        d.force = ft.data_ptr() if ft is not None else None
-        d.force_const = fc
+        self._keep = [kt, kq] + _force_fields(d, 1.0 if rhs_force is None else rhs_force, self.source_space)
         d.dirichlet = int(dirichlet)
         return d
 
@@ -659,13 +692,12 @@ class VectorFunctional:
         return f
 
     def assemble(self, parallel=True):
-        ft, fc = _coef(self.force())
         d = capi.DiffusionDesc()
         d.kappa, d.kappa_const = None, 1.0
-        d.force = ft.data_ptr() if ft is not None else None
-        d.force_const = fc
+        keep = _force_fields(d, self.force(), self.space)
         d.dirichlet = 0
         self.ctx.call("gdt_assemble_cg_rhs", self.space.handle, C.byref(d), _ptr(self.vector))
+        del keep
         return self
 
 

@@ -12,7 +12,8 @@ from . import _build
 SPMV_SCHEDULES = 9
 SPMV_SCHEDULE_SELL32 = 8
 NORM_H1_SEMI, NORM_L2 = 0, 1
-TIMING_SPMV_FP64, TIMING_SPMV_FP32, TIMING_CG_UPDATE, TIMING_CG_DIRECTION, TIMING_RELIABLE_UPDATE = range(5)
+(TIMING_SPMV_FP64, TIMING_SPMV_FP32, TIMING_CG_UPDATE, TIMING_CG_DIRECTION, TIMING_RELIABLE_UPDATE,
+ TIMING_MIXED_PERSISTENT) = range(6)
 TIMING_KINDS = 8
 OK, EINVAL, ESHAPE, ENOCONV, ETIMEOUT, ENAN, EUNSUPPORTED, ECUDA, ENOMEM = range(9)
 SPACE_CG, SPACE_DG, SPACE_FV = 0, 1, 2
@@ -30,7 +31,8 @@ SOLVER_LAUNCH_AUTO, SOLVER_LAUNCH_GRAPH, SOLVER_LAUNCH_PERSISTENT = 0, 1, 2
 
 class DiffusionDesc(C.Structure):
     _fields_ = [("kappa", C.c_void_p), ("kappa_const", C.c_double), ("force", C.c_void_p),
-                ("force_const", C.c_double), ("dirichlet", C.c_int), ("kappa_qp", C.c_void_p)]
+                ("force_const", C.c_double), ("dirichlet", C.c_int), ("kappa_qp", C.c_void_p),
+                ("force_qp", C.c_void_p), ("force_quad_order", C.c_int)]
 
 
 class ProductDesc(C.Structure):

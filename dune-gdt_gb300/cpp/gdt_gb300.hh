@@ -6,12 +6,15 @@
 // namespace. Everything below calls the C ABI (include/gdt_gb300.h); device memory is plain
 // cudaMalloc memory owned by DeviceVector.
 //
-// Lowering rules (documented limits of the GPU library): diffusion and source data are element-wise
-// constant; a function-valued source or diffusion (std::function of the global point) is sampled at
-// element barycentres on the host when the form is appended.
+// Lowering rules (documented limits of the GPU library): the diffusion is a constant or element-wise
+// constant; a function-valued source (std::function of the global point, with its polynomial order as
+// dune-xt's GenericFunction(order, lambda)) is evaluated on the host at the quadrature points the
+// reference's product integrand uses (a Gauss rule of order f + space order) and the load vector is
+// assembled from those values.
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <functional>
@@ -127,6 +130,31 @@ class CubeGrid {
     }
     return x;
   }
+  // the physical point of reference coordinates xref in element e: its first vertex plus J_e xref,
+  // J_e the cube's scaling (times the Kuhn simplex's corner matrix: column m is the sum of the unit
+  // vectors of the first m + 1 axes of its permutation, permutations in std::next_permutation order)
+  FieldVector<d> global(int64_t e, const double* xref) const {
+    const int nsub = simplex_ ? (d == 2 ? 2 : d == 3 ? 6 : 1) : 1;
+    int64_t c = e / nsub;
+    std::array<double, d> loc{};
+    if (simplex_ && d >= 2) {
+      std::array<int, d> perm;
+      for (int a = 0; a < d; ++a) perm[a] = a;
+      for (int64_t t = 0; t < e % nsub; ++t) std::next_permutation(perm.begin(), perm.end());
+      for (int m = 0; m < d; ++m)
+        for (int k = 0; k <= m; ++k) loc[perm[k]] += xref[m];
+    } else {
+      for (int a = 0; a < d; ++a) loc[a] = xref[a];
+    }
+    FieldVector<d> x;
+    for (int a = 0; a < d; ++a) {
+      const double h = (upper_[a] - lower_[a]) / double(cells_[a]);
+      const int64_t i = c % cells_[a];
+      c /= cells_[a];
+      x[a] = lower_[a] + (double(i) + loc[a]) * h;
+    }
+    return x;
+  }
 
  private:
   FieldVector<d> lower_, upper_;
@@ -150,17 +178,19 @@ CubeGrid<d> make_cube_grid(double lower, double upper, int64_t cells, bool simpl
 template <int d>
 class Space {
  public:
-  Space(const CubeGrid<d>& grid, int kind, int order) : grid_(grid) {
+  Space(const CubeGrid<d>& grid, int kind, int order) : grid_(grid), order_(order) {
     gdt_space s = nullptr;
     check(gdt_space_create(grid.handle(), kind, order, &s), nullptr, "space");
     handle_.reset(s, [](gdt_space x) { gdt_space_destroy(x); });
   }
   gdt_space handle() const { return handle_.get(); }
   int64_t size() const { return gdt_space_size(handle()); }
+  int order() const { return order_; }
   const CubeGrid<d>& grid_view() const { return grid_; }
 
  private:
   CubeGrid<d> grid_;
+  int order_;
   std::shared_ptr<gdt_space_s> handle_;
 };
 
@@ -196,14 +226,15 @@ struct ProductWithAnsatz {
   GridFunction<d> f;
   double constant = 1.0;
   bool is_constant = true;
+  int order = 3;  // polynomial order of f (GenericFunction(order, lambda))
 };
 
 struct LocalElementProductIntegrand {
   template <int d>
-  ProductWithAnsatz<d> with_ansatz(const GridFunction<d>& f) const {
-    return ProductWithAnsatz<d>{f, 0.0, false};
+  ProductWithAnsatz<d> with_ansatz(const GridFunction<d>& f, int order = 3) const {
+    return ProductWithAnsatz<d>{f, 0.0, false, order};
   }
-  ProductWithAnsatz<2> with_ansatz(double c) const { return ProductWithAnsatz<2>{{}, c, true}; }
+  ProductWithAnsatz<2> with_ansatz(double c) const { return ProductWithAnsatz<2>{{}, c, true, 0}; }
 };
 
 struct LocalElementIntegralBilinearForm {
@@ -277,15 +308,23 @@ class VectorFunctional {
   void append(const LocalElementIntegralFunctional<d>& f) {
     if (f.integrand.is_constant) {
       force_.reset();
+      force_qp_.reset();
       constant_ = f.integrand.constant;
       return;
     }
-    // element-wise constant lowering: the source at each element barycentre
+    // the source at the quadrature points of the product integrand (order of f + order of the space)
     const auto& grid = space_.grid_view();
-    std::vector<double> h(size_t(grid.num_elements()));
-    for (int64_t e = 0; e < grid.num_elements(); ++e) h[size_t(e)] = f.integrand.f(grid.barycentre(e));
-    force_ = std::make_shared<DeviceVector>(h.size());
-    force_->upload(h);
+    quad_order_ = f.integrand.order + space_.order();
+    const int nq = gdt_space_quadrature_order(space_.handle(), quad_order_, nullptr, nullptr);
+    if (nq <= 0) throw Exception(GDT_EUNSUPPORTED, "no quadrature rule for this space");
+    std::vector<double> xq(3 * size_t(nq)), wq(static_cast<size_t>(nq));
+    gdt_space_quadrature_order(space_.handle(), quad_order_, xq.data(), wq.data());
+    std::vector<double> h(size_t(grid.num_elements()) * nq);
+    for (int64_t e = 0; e < grid.num_elements(); ++e)
+      for (int q = 0; q < nq; ++q) h[size_t(e) * nq + q] = f.integrand.f(grid.global(e, &xq[3 * size_t(q)]));
+    force_qp_ = std::make_shared<DeviceVector>(h.size());
+    force_qp_->upload(h);
+    force_.reset();
   }
   DeviceVector& vector() { return vector_; }
   gdt_diffusion_desc desc(double kappa_const = 1.0, const DeviceVector* kappa = nullptr) const {
@@ -294,6 +333,8 @@ class VectorFunctional {
     ds.kappa_const = kappa_const;
     ds.force = force_ ? force_->data() : nullptr;
     ds.force_const = constant_;
+    ds.force_qp = force_qp_ ? force_qp_->data() : nullptr;
+    ds.force_quad_order = quad_order_;
     return ds;
   }
   void assemble(bool /*use_tbb*/ = true) {
@@ -306,6 +347,8 @@ class VectorFunctional {
   Space<d> space_;
   DeviceVector vector_;
   std::shared_ptr<DeviceVector> force_;
+  std::shared_ptr<DeviceVector> force_qp_;
+  int quad_order_ = 0;
   double constant_ = 0.0;
 };
 
@@ -353,6 +396,8 @@ class Walker {
       const gdt_diffusion_desc fd = f_->desc();
       ds.force = fd.force;
       ds.force_const = fd.force_const;
+      ds.force_qp = fd.force_qp;
+      ds.force_quad_order = fd.force_quad_order;
     }
     ds.dirichlet = dc_ ? 1 : 0;
     check(gdt_assemble_cg_diffusion(default_context(), op_->handle(), &ds, f_ ? f_->vector().data() : nullptr),

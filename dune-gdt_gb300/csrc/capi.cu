@@ -338,17 +338,28 @@ gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_di
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
   m->val_version++;
+  if (d->force_qp && d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
+  // a source at quadrature points: the matrix first, then the load vector from its own pass
+  double* rhs_fused = d->force_qp ? nullptr : rhs;
   if (m->test.order == 2 || d->kappa_qp) {
     m->mf_valid = 0;
     GDT_CHECK(ctx, ho_prepare(ctx, m));
-    return ho_assemble(ctx, m, 0, d->kappa, d->kappa_const, d->kappa_qp, d->force, d->force_const, rhs, d->dirichlet);
+    GDT_CHECK(ctx, ho_assemble(ctx, m, 0, d->kappa, d->kappa_const, d->kappa_qp, d->force, d->force_const, rhs_fused,
+                               d->dirichlet));
+  } else {
+    GDT_CHECK(ctx, assemble_cg(ctx, m, d, rhs_fused));
   }
-  return assemble_cg(ctx, m, d, rhs);
+  if (d->force_qp && rhs) return ho_rhs_qp(ctx, m->test, d->force_qp, d->force_quad_order, d->dirichlet, rhs);
+  return GDT_OK;
 }
 
 gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space s, const gdt_diffusion_desc* d, double* rhs) {
   if (!ctx || !s || !d || !rhs) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
+  if (d->force_qp) {
+    if (d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
+    return ho_rhs_qp(ctx, *s, d->force_qp, d->force_quad_order, d->dirichlet, rhs);
+  }
   if (s->order == 2) return ho_assemble_rhs(ctx, *s, d->force, d->force_const, d->dirichlet, rhs);
   return assemble_cg_rhs(ctx, *s, d, rhs);
 }

@@ -13,7 +13,10 @@
 // halo staged from global memory), and the second SSP stage fuses u1 = u - dt k0, k1 = L(u1) and
 // u_new = u + (k0 + k1)(-dt/2) into one pass: per step it reads u (twice) and k0 and writes k0 and
 // u_new (40 bytes per cell). LF uses the local speed max(|f'(u)|, |f'(v)|) multiplied in directly
-// (the reference forms 0.5 / (1 / lambda); both agree to rounding).
+// (the reference forms 0.5 / (1 / lambda); both agree to rounding). FP64 instructions per cell and
+// stage (Burgers LF): the squares once per staged cell, three per face (u - v, u^2 + v^2 and one FMA,
+// with 2 max(|u|, |v|) on the integer pipe), three for the update K and at most two for the stage's
+// output: about 10 (first stage) and 13.5 (second) where the per-face form took 25.
 #include <cmath>
 #include <limits>
 
@@ -194,63 +197,94 @@ __global__ void fv_apply_kernel(GridDesc g, FvParams p, long long nbatch, const 
 // ------------------------------------------------------------------------------- 2D tiled ---
 constexpr int TX = 32, TY = 32, BY = 8;  // tile TX x TY cells, block TX x BY threads
 
-// STAGE 0: k = L(u) ; STAGE 1 (Euler): u_next = u - dt L(u) ;
-// STAGE 2: u1 = u - dt k0 on the tile + halo, u_next = u + (-dt/2) (k0 + L(u1))
-// BND: some side has a boundary treatment; the faces on those sides are then replaced by it. FORM:
-// the numerical flux (FORM4_*), a template parameter so that each flux is straight-line code
+// 2 max(|u|, |v|) for the local LF speed, on the integer pipe: the larger magnitude's bit pattern with
+// the exponent raised by one (exact for normal numbers; for zero and subnormal speeds the product with
+// u - v, at most twice their size, underflows to zero either way)
+__device__ __forceinline__ double twice_abs_max(double u, double v) {
+  const long long a = __double_as_longlong(u) & 0x7fffffffffffffffLL, b = __double_as_longlong(v) & 0x7fffffffffffffffLL;
+  return __longlong_as_double((a > b ? a : b) + (1LL << 52));
+}
+// the Burgers LF forms use the squares of the states, computed once per cell when the tile is staged
+__host__ __device__ constexpr bool uses_squares(int form) {
+  return form == FORM4_BURGERS_LF || form == FORM4_BURGERS_LF_FIXED;
+}
+// 4 g(u, v, +e_k) with the squares qu = u^2, qv = v^2 at hand: three FP64 instructions for Burgers LF
+template <int FORM>
+__device__ __forceinline__ double face4s(const FvParams& p, int k, double u, double v, double qu, double qv) {
+  if constexpr (FORM == FORM4_BURGERS_LF) return fma(twice_abs_max(u, v), u - v, qu + qv);
+  else if constexpr (FORM == FORM4_BURGERS_LF_FIXED) return fma(p.lam2, u - v, qu + qv);
+  else return face_flux4<FORM>(p, k, u, v);
+}
+
+// One stage over a tile of TX x TY cells of state b (blockIdx.z). The fluxes are kept as 4 g, and the
+// update as K = (gx_right - gx_left) + rho (gy_top - gy_bottom), rho = h_x / h_y, so that
+// L(u) = (1 / (4 h_x)) K:
+//   STAGE 0: out = c_out K (fv_apply: c_out = 1 / (4 h_x), giving L(u); the SSP-RK2 stepper keeps K
+//            itself, c_out = 1)
+//   STAGE 1 (Euler): out = u + c_out K, c_out = -dt / (4 h_x)
+//   STAGE 2 (SSP-RK2): u1 = u + c1 k0 on the tile + halo (k0 = K(u), c1 = -dt / (4 h_x)),
+//            out = u + c_out (k0 + K(u1)), c_out = -dt / (8 h_x)
+// Every FP64 pass runs whole warps over 32 values: the tile interior column by column, the two halo
+// columns and the 33rd x face of every row in passes of their own (a pass with one active lane costs
+// the FP64 pipe as much as a full one). BND: some side has a boundary treatment; the faces on those
+// sides are then replaced by it. FORM: the numerical flux (FORM4_*), compiled as straight-line code.
 template <int STAGE, bool BND, int FORM>
 __global__ void __launch_bounds__(TX* BY) fv2d_tile(GridDesc g, FvParams p, const double* __restrict__ u,
                                                     const double* __restrict__ k0, double* __restrict__ out,
-                                                    double dt, double cx, double cy) {
-  __shared__ double s[TY + 2][TX + 3];
-  __shared__ double gx[TY][TX + 1];
-  __shared__ double gy[TY + 1][TX + 1];
+                                                    double c1, double c_out, double rho) {
+  constexpr bool SQ = uses_squares(FORM);
+  __shared__ double s[TY + 2][TX + 2];             // staged state: s[j + 1][i + 1] = cell (x0 + i, y0 + j)
+  __shared__ double q[SQ ? TY + 2 : 1][TX + 2];    // its squares
+  __shared__ double gx[TY][TX + 1];                // gx[j][i]: x face between tile columns i - 1 and i
+  __shared__ double gy[TY + 1][TX];                // gy[j][i]: y face between tile rows j - 1 and j
   const long long nx = g.n[0], ny = g.n[1];
   const long long off = (long long)blockIdx.z * nx * ny;
   const long long x0 = (long long)blockIdx.x * TX, y0 = (long long)blockIdx.y * TY;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  // stage tile + halo (periodic wrap by compare and select: a 64-bit modulo would cost more FP64-pipe
-  // time than the flux arithmetic)
-  for (int j = ty; j < TY + 2; j += BY)
-    for (int i = tx; i < TX + 2; i += TX) {
-      long long gxi = x0 + i - 1, gyj = y0 + j - 1;
-      gxi = gxi < 0 ? nx - 1 : (gxi == nx ? 0 : (gxi > nx ? nx - 1 : gxi));  // beyond a partial tile: unused
-      gyj = gyj < 0 ? ny - 1 : (gyj == ny ? 0 : (gyj > ny ? ny - 1 : gyj));
-      const long long cidx = off + gyj * nx + gxi;
-      double v = u[cidx];
-      if (STAGE == 2) v = fma(k0[cidx], -dt, v);
-      s[j][i] = v;
-    }
+  // periodic wrap by compare and select (a 64-bit modulo would cost more than the flux arithmetic);
+  // beyond a partial tile: clamped, unused
+  auto wrap = [](long long c, long long n) { return c < 0 ? n - 1 : (c == n ? 0 : (c > n ? n - 1 : c)); };
+  auto stage = [&](int j, int i) {
+    const long long cidx = off + wrap(y0 + j - 1, ny) * nx + wrap(x0 + i - 1, nx);
+    double v = u[cidx];
+    if (STAGE == 2) v = fma(k0[cidx], c1, v);
+    s[j][i] = v;
+    if constexpr (SQ) q[j][i] = v * v;
+  };
+  for (int j = ty; j < TY + 2; j += BY) stage(j, tx + 1);  // interior columns
+  {
+    // the two halo columns, 2 (TY + 2) values, in the block's first warps
+    const int e = ty * TX + tx;
+    if (e < 2 * (TY + 2)) stage(e % (TY + 2), e < TY + 2 ? 0 : TX + 1);
+  }
   __syncthreads();
-  // x faces: between tile columns i-1 and i (i = 0..TX), rows 0..TY-1; fluxes kept as 4 g
-  for (int j = ty; j < TY; j += BY)
-    for (int i = tx; i <= TX; i += TX) {
-      double f;
-      if (BND && p.bkind[0] >= 0 && x0 + i == 0) f = 4.0 * boundary_face_flux(p, 2, 0, false, s[j + 1][i + 1]);
-      else if (BND && p.bkind[0] >= 0 && x0 + i == nx) f = 4.0 * boundary_face_flux(p, 2, 0, true, s[j + 1][i]);
-      else f = face_flux4<FORM>(p, 0, s[j + 1][i], s[j + 1][i + 1]);
-      gx[j][i] = f;
-    }
-  // y faces: between tile rows j-1 and j (j = 0..TY)
+  auto xface = [&](int j, int i) {  // 4 g through the x face between tile columns i - 1 and i of row j
+    if (BND && p.bkind[0] >= 0 && x0 + i == 0) return 4.0 * boundary_face_flux(p, 2, 0, false, s[j + 1][i + 1]);
+    if (BND && p.bkind[0] >= 0 && x0 + i == nx) return 4.0 * boundary_face_flux(p, 2, 0, true, s[j + 1][i]);
+    if constexpr (SQ) return face4s<FORM>(p, 0, s[j + 1][i], s[j + 1][i + 1], q[j + 1][i], q[j + 1][i + 1]);
+    else return face4s<FORM>(p, 0, s[j + 1][i], s[j + 1][i + 1], 0.0, 0.0);
+  };
+  for (int j = ty; j < TY; j += BY) gx[j][tx] = xface(j, tx);
+  if (ty == 0) gx[tx][TX] = xface(tx, TX);  // the right face of every row: one pass of the first warp
   for (int j = ty; j <= TY; j += BY) {
     double f;
     if (BND && p.bkind[2] >= 0 && y0 + j == 0) f = 4.0 * boundary_face_flux(p, 2, 1, false, s[j + 1][tx + 1]);
     else if (BND && p.bkind[2] >= 0 && y0 + j == ny) f = 4.0 * boundary_face_flux(p, 2, 1, true, s[j][tx + 1]);
-    else f = face_flux4<FORM>(p, 1, s[j][tx + 1], s[j + 1][tx + 1]);
+    else if constexpr (SQ) f = face4s<FORM>(p, 1, s[j][tx + 1], s[j + 1][tx + 1], q[j][tx + 1], q[j + 1][tx + 1]);
+    else f = face4s<FORM>(p, 1, s[j][tx + 1], s[j + 1][tx + 1], 0.0, 0.0);
     gy[j][tx] = f;
   }
   __syncthreads();
   const long long gxi = x0 + tx;
   if (gxi >= nx) return;
-  const double cx4 = 0.25 * cx, cy4 = 0.25 * cy;
   for (int j = ty; j < TY; j += BY) {
     const long long gyj = y0 + j;
     if (gyj >= ny) break;
-    const double L = fma(cx4, gx[j][tx + 1] - gx[j][tx], cy4 * (gy[j + 1][tx] - gy[j][tx]));
+    const double K = fma(rho, gy[j + 1][tx] - gy[j][tx], gx[j][tx + 1] - gx[j][tx]);
     const long long cidx = off + gyj * nx + gxi;
-    if (STAGE == 0) out[cidx] = L;
-    else if (STAGE == 1) out[cidx] = fma(-dt, L, u[cidx]);
-    else out[cidx] = fma(-0.5 * dt, k0[cidx] + L, u[cidx]);
+    if (STAGE == 0) out[cidx] = c_out * K;
+    else if (STAGE == 1) out[cidx] = fma(c_out, K, u[cidx]);
+    else out[cidx] = fma(c_out, k0[cidx] + K, u[cidx]);
   }
 }
 
@@ -308,33 +342,33 @@ bool has_boundary(const FvParams& p, int dim) {
 
 template <int STAGE, bool BND>
 void launch_tile_b(dim3 grid, cudaStream_t s, const GridDesc& g, const FvParams& p, const double* u, const double* k0,
-                   double* out, double dt, double cx, double cy) {
+                   double* out, double c1, double c_out, double rho) {
   const dim3 block(TX, BY);
   switch (p.form4) {
-    case FORM4_BURGERS_LF: fv2d_tile<STAGE, BND, FORM4_BURGERS_LF><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy); break;
+    case FORM4_BURGERS_LF: fv2d_tile<STAGE, BND, FORM4_BURGERS_LF><<<grid, block, 0, s>>>(g, p, u, k0, out, c1, c_out, rho); break;
     case FORM4_BURGERS_LF_FIXED:
-      fv2d_tile<STAGE, BND, FORM4_BURGERS_LF_FIXED><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      fv2d_tile<STAGE, BND, FORM4_BURGERS_LF_FIXED><<<grid, block, 0, s>>>(g, p, u, k0, out, c1, c_out, rho);
       break;
     case FORM4_TRANSPORT_LINEAR:
-      fv2d_tile<STAGE, BND, FORM4_TRANSPORT_LINEAR><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      fv2d_tile<STAGE, BND, FORM4_TRANSPORT_LINEAR><<<grid, block, 0, s>>>(g, p, u, k0, out, c1, c_out, rho);
       break;
-    case FORM4_BURGERS_EO: fv2d_tile<STAGE, BND, FORM4_BURGERS_EO><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy); break;
+    case FORM4_BURGERS_EO: fv2d_tile<STAGE, BND, FORM4_BURGERS_EO><<<grid, block, 0, s>>>(g, p, u, k0, out, c1, c_out, rho); break;
     case FORM4_TRANSPORT_EO:
-      fv2d_tile<STAGE, BND, FORM4_TRANSPORT_EO><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      fv2d_tile<STAGE, BND, FORM4_TRANSPORT_EO><<<grid, block, 0, s>>>(g, p, u, k0, out, c1, c_out, rho);
       break;
     case FORM4_BURGERS_UPWIND:
-      fv2d_tile<STAGE, BND, FORM4_BURGERS_UPWIND><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy);
+      fv2d_tile<STAGE, BND, FORM4_BURGERS_UPWIND><<<grid, block, 0, s>>>(g, p, u, k0, out, c1, c_out, rho);
       break;
-    default: fv2d_tile<STAGE, BND, FORM4_GENERIC><<<grid, block, 0, s>>>(g, p, u, k0, out, dt, cx, cy); break;
+    default: fv2d_tile<STAGE, BND, FORM4_GENERIC><<<grid, block, 0, s>>>(g, p, u, k0, out, c1, c_out, rho); break;
   }
 }
 
 // one stage of the tiled 2D kernel, instantiated for the flux form and the boundary case
 template <int STAGE>
 void launch_tile(bool bnd, dim3 grid, cudaStream_t s, const GridDesc& g, const FvParams& p, const double* u,
-                 const double* k0, double* out, double dt, double cx, double cy) {
-  if (bnd) launch_tile_b<STAGE, true>(grid, s, g, p, u, k0, out, dt, cx, cy);
-  else launch_tile_b<STAGE, false>(grid, s, g, p, u, k0, out, dt, cx, cy);
+                 const double* k0, double* out, double c1, double c_out, double rho) {
+  if (bnd) launch_tile_b<STAGE, true>(grid, s, g, p, u, k0, out, c1, c_out, rho);
+  else launch_tile_b<STAGE, false>(grid, s, g, p, u, k0, out, c1, c_out, rho);
 }
 
 bool tiled_ok(const GridDesc& g) { return g.dim == 2 && g.n[0] >= 2 && g.n[1] >= 2; }
@@ -346,7 +380,8 @@ gdt_status fv_apply(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc* d
   FvParams p = make_params(g, d);
   if (tiled_ok(g)) {
     dim3 grid((unsigned)((g.n[0] + TX - 1) / TX), (unsigned)((g.n[1] + TY - 1) / TY), 1);
-    launch_tile<0>(has_boundary(p, 2), grid, ctx->stream, g, p, u, nullptr, out, 0.0, 1.0 / g.h[0], 1.0 / g.h[1]);
+    // L(u) = K / (4 h_x), K = dx + (h_x / h_y) dy
+    launch_tile<0>(has_boundary(p, 2), grid, ctx->stream, g, p, u, nullptr, out, 0.0, 0.25 / g.h[0], g.h[0] / g.h[1]);
   } else {
     fv_apply_kernel<<<grid_blocks(g.nelem, 256), 256, 0, ctx->stream>>>(g, p, 1, u, out, nullptr, 0.0, 0, nullptr,
                                                                         0.0);
@@ -419,18 +454,20 @@ gdt_status fv_timestep(gdt_context ctx, const gdt_space_s& sp, const gdt_fv_desc
   const bool tiled = tiled_ok(g);
   const bool bnd = has_boundary(p, g.dim);
   dim3 grid((unsigned)((g.n[0] + TX - 1) / TX), (unsigned)((g.n[1] + TY - 1) / TY), (unsigned)nbatch);
-  const double cx = 1.0 / g.h[0], cy = g.dim >= 2 ? 1.0 / g.h[1] : 0.0;
+  // the tiled kernels' update K = dx + rho dy with L(u) = K / (4 h_x): the stepper keeps K0 = K(u) itself
+  // (k0 = L(u) = K0 / (4 h_x)) and folds the factor into its coefficients
+  const double rho = tiled ? g.h[0] / g.h[1] : 0.0, ck = 0.25 / g.h[0];
   for (long long st = 0; st < steps; ++st) {
     if (stepper == GDT_TIMESTEPPER_EXPLICIT_EULER) {
       if (tiled)
-        launch_tile<1>(bnd, grid, s, g, p, cur, nullptr, nxt, dt, cx, cy);
+        launch_tile<1>(bnd, grid, s, g, p, cur, nullptr, nxt, 0.0, -dt * ck, rho);
       else
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, nullptr, nullptr, 0.0, 1, nxt, dt);
       ctx->launches++;
     } else {
       if (tiled) {
-        launch_tile<0>(bnd, grid, s, g, p, cur, nullptr, k0, dt, cx, cy);
-        launch_tile<2>(bnd, grid, s, g, p, cur, k0, nxt, dt, cx, cy);
+        launch_tile<0>(bnd, grid, s, g, p, cur, nullptr, k0, 0.0, 1.0, rho);
+        launch_tile<2>(bnd, grid, s, g, p, cur, k0, nxt, -dt * ck, -0.5 * dt * ck, rho);
       } else {
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, cur, k0, nullptr, 0.0, 0, nullptr, 0.0);
         fv_apply_kernel<<<grid_blocks(N, 256), 256, 0, s>>>(g, p, nbatch, nullptr, k0, cur, -dt, 2, nxt, -0.5 * dt);

@@ -774,6 +774,21 @@ __global__ void k_ho_rhs(GridDesc g, Colour c, const double* __restrict__ load, 
   }
 }
 
+// rhs[gi] += sum_q w_q |J| phi_i(x_q) f_e(x_q), f given at the points of a rule ([element][q]), colour by colour
+__global__ void k_ho_rhs_qp(GridDesc g, Colour c, const double* __restrict__ phi, const double* __restrict__ wdet,
+                            int L, int nq, const double* __restrict__ fqp, const int* __restrict__ gi,
+                            double* __restrict__ rhs) {
+  const long long n = c.total * L;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < n; w += (long long)gridDim.x * blockDim.x) {
+    const long long e = colour_element(g, c, w / L);
+    const int i = int(w % L);
+    const double* fe = fqp + e * nq;
+    double acc = 0.0;
+    for (int q = 0; q < nq; ++q) acc = fma(wdet[q] * phi[q * L + i], fe[q], acc);
+    rhs[gi[e * L + i]] += acc;
+  }
+}
+
 __global__ void k_ho_boundary(GridDesc g, HoNodes nd, const int* __restrict__ gi, unsigned char* __restrict__ flag) {
   const long long n = g.nelem * nd.lsize;
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < n; w += (long long)gridDim.x * blockDim.x) {
@@ -1020,6 +1035,54 @@ gdt_status ho_assemble_rhs(gdt_context ctx, const gdt_space_s& sp, const double*
   }
   GDT_TRY_CUDA(ctx, cudaStreamSynchronize(st));  // the host tables outlive the copies
   return check_launch(ctx, "order-2 load vector");
+}
+
+gdt_status ho_rhs_qp(gdt_context ctx, const gdt_space_s& sp, const double* fqp, int quad_order, int dirichlet,
+                     double* rhs) {
+  const GridDesc& g = sp.g;
+  cudaStream_t st = ctx->stream;
+  const ho::HoSpaceInfo info = ho::space_info(g, sp.order);
+  const ho::BasisTables B = ho::basis_tables(g, sp.order, quad_order);
+  const int L = info.lsize, nq = B.nq;
+  int* gi = nullptr;
+  double* phi = nullptr;
+  double* wdet = nullptr;
+  unsigned char* flag = nullptr;
+  struct Freer {
+    void* p[4];
+    cudaStream_t s;
+    ~Freer() {
+      for (void* q : p)
+        if (q) cudaFreeAsync(q, s);
+    }
+  } freer{{nullptr, nullptr, nullptr, nullptr}, st};
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&gi, sizeof(int) * g.nelem * L, st));
+  freer.p[0] = gi;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&phi, sizeof(double) * B.phi.size(), st));
+  freer.p[1] = phi;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&wdet, sizeof(double) * B.wdet.size(), st));
+  freer.p[2] = wdet;
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(phi, B.phi.data(), sizeof(double) * B.phi.size(), cudaMemcpyHostToDevice, st));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(wdet, B.wdet.data(), sizeof(double) * B.wdet.size(), cudaMemcpyHostToDevice, st));
+  GDT_CHECK(ctx, ho_global_indices(ctx, sp, nullptr, gi));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(rhs, 0, sizeof(double) * info.size, st));
+  for (int k = 0; k < (1 << g.dim) * g.nsub; ++k) {
+    const Colour c = colour_of(g, k);
+    if (c.total == 0) continue;
+    k_ho_rhs_qp<<<vec_grid(c.total * L, ctx->num_sms), 256, 0, st>>>(
+        g, c, phi + size_t(c.t) * nq * L, wdet + size_t(c.t) * nq, L, nq, fqp, gi, rhs);
+    ctx->launches++;
+  }
+  if (dirichlet) {
+    GDT_TRY_CUDA(ctx, cudaMallocAsync(&flag, size_t(info.size), st));
+    freer.p[3] = flag;
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(flag, 0, size_t(info.size), st));
+    k_ho_boundary<<<vec_grid(g.nelem * L, ctx->num_sms), 256, 0, st>>>(g, make_nodes(info), gi, flag);
+    k_ho_zero_flagged<<<vec_grid(info.size, ctx->num_sms), 256, 0, st>>>(info.size, flag, rhs);
+    ctx->launches += 2;
+  }
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(st));  // the host tables outlive the copies
+  return check_launch(ctx, "load vector at quadrature points");
 }
 
 int ho_quadrature(const gdt_space_s& sp, double* x_ref, double* w_ref) {

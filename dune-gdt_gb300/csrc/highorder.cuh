@@ -59,6 +59,10 @@ gdt_status ho_dirichlet(gdt_context ctx, gdt_matrix m, double* rhs);
 gdt_status ho_prepare(gdt_context ctx, gdt_matrix m);
 gdt_status ho_assemble_rhs(gdt_context ctx, const gdt_space_s& sp, const double* force, double force_const,
                            int dirichlet, double* rhs);
+// load vector of a source given at the points of the Gauss rule of quad_order
+// (gdt_space_quadrature_order), fqp [element][point]; continuous spaces of order 1 and 2
+gdt_status ho_rhs_qp(gdt_context ctx, const gdt_space_s& sp, const double* fqp, int quad_order, int dirichlet,
+                     double* rhs);
 int ho_quadrature(const gdt_space_s& sp, double* x_ref, double* w_ref);
 gdt_status element_error(gdt_context ctx, const gdt_space_s& sp, int norm, int quad_order, const double* u,
                          const double* ref, double* eta2, double* total);

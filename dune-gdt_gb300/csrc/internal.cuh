@@ -162,6 +162,11 @@ gdt_status newton_solve(gdt_context ctx, gdt_matrix m, const double* range, doub
 bool mixed_stencil_supported(gdt_matrix m);
 gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
                                gdt_solve_info* info, cudaStream_t s);
+// mixed_mf.cu: matrix-free FP32 CG (3D Q1 Laplace, element coefficients kept at assembly) in persistent
+// launches with FP64 reliable updates; GDT_EUNSUPPORTED (before touching x) where it does not apply
+bool mixed_mf_applies(gdt_matrix m);
+gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
+                          gdt_solve_info* info, cudaStream_t s);
 // fv.cu
 gdt_status fv_apply(gdt_context ctx, const gdt_space_s& s, const gdt_fv_desc* d, const double* u, double* out);
 gdt_status fv_estimate_dt(gdt_context ctx, const gdt_space_s& s, const gdt_fv_desc* d, const double* u0,

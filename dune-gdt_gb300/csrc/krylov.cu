@@ -656,8 +656,7 @@ void ilu_apply(gdt_context ctx, gdt_matrix m, const Ilu& f, const double* r, dou
 // when the lanes read their rows: 17.6 us of a 43 us iteration on that SWIPDG system.) The matrix
 // and the Jacobi diagonal are read-only in the kernel (non-coherent loads); the vectors are written
 // by other blocks between barriers and read with plain loads, which the barrier's fences order.
-constexpr int PT = 1024;                                 // threads per block (one block per SM)
-constexpr unsigned long long kBarrierNs = 1000000000ull;  // longest wait at a grid barrier (1 s)
+constexpr int PT = 1024;  // threads per block (one block per SM)
 
 struct PcgArgs {
   int n;
@@ -676,81 +675,6 @@ struct PcgArgs {
   unsigned int* bar;  // 64-bit arrival count at bar[0], generation at bar[kBarGen], fault at bar[kBarFault]
   unsigned long long wait_ns;  // longest wait at a grid barrier
 };
-// the arrival counter, the generation the waiting blocks poll and the fault flag sit 4 KB apart, so
-// the polls and the arrivals do not queue at the same L2 slice
-constexpr int kBarGen = 1024, kBarFault = 2048;
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Grid barrier (all blocks are co-resident: cooperative launch). Barrier number `epoch` (counted by
-// thread 0 of every block) is complete when the 64-bit arrival count reaches epoch * blocks; the last
-// block to arrive publishes the epoch as the generation the others poll (no reset of the count, so
-// the release is one store after the arrival). The waits are bounded by time (wait_ns, checked at the
-// first poll and every 256 polls) and by count, after which the fault flag is set and every block
-// returns false from then on.
-__device__ bool pcg_sync(unsigned int* bar, unsigned int& epoch, unsigned long long wait_ns) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ++epoch;
-    volatile unsigned int* vgen = bar + kBarGen;
-    volatile unsigned int* vfault = bar + kBarFault;
-    __threadfence();
-    int good = *vfault == 0u;
-    if (good) {
-      const unsigned long long target = (unsigned long long)epoch * gridDim.x;
-      if (atomicAdd(reinterpret_cast<unsigned long long*>(bar), 1ull) == target - 1) {
-        __threadfence();
-        atomicExch(bar + kBarGen, epoch);
-      } else {
-        const unsigned long long t0 = global_ns();
-        unsigned int spins = 0;
-        while (*vgen != epoch) {
-          ++spins;
-          if ((spins & 255u) == 1u) {
-            if (*vfault) {
-              good = 0;
-              break;
-            }
-            if (spins > (1u << 26) || global_ns() - t0 > wait_ns) {
-              atomicExch(bar + kBarFault, 1u);
-              good = 0;
-              break;
-            }
-          }
-          __nanosleep(40);
-        }
-      }
-    }
-    __threadfence();
-    ok = good;
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
-// sum of the per-block partials in block order, the same in every block; result in every thread
-template <int NV>
-__device__ __forceinline__ void pcg_allreduce(const double* part, double (&v)[NV], double* red, double* bc) {
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double s = 0.0;
-    for (int b = threadIdx.x; b < gridDim.x; b += PT) s += part[k * gridDim.x + b];
-    v[k] = s;
-  }
-  block_reduce<NV>(v, red);
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int k = 0; k < NV; ++k) bc[k] = v[k];
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = bc[k];
-}
-
 // q = A p over the warp's slices (rows of at most 32 entries); returns this thread's share of p.q.
 // The slices of a warp are the same in every iteration: lane m holds the (offset, width) of the
 // warp's m-th slice, so a pass gets them by a shuffle instead of a load.
@@ -822,8 +746,8 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
     double v1[1] = {pcg_spmv(a, mymeta)};
     block_reduce<1>(v1, red);
     if (threadIdx.x == 0) a.part[blockIdx.x] = v1[0];
-    if (!pcg_sync(a.bar, epoch, a.wait_ns)) break;
-    pcg_allreduce<1>(a.part, v1, red, bc);
+    if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
+    grid_allreduce<1>(a.part, v1, red, bc);
     alpha = rho / v1[0];
     if (!(v1[0] > 0.0) || !isfinite(v1[0])) {
       brk = conv = 1;
@@ -863,8 +787,8 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
       a.part[nb + blockIdx.x] = v2[0];
       a.part[2 * nb + blockIdx.x] = v2[1];
     }
-    if (!pcg_sync(a.bar, epoch, a.wait_ns)) break;
-    pcg_allreduce<2>(a.part + nb, v2, red, bc);
+    if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
+    grid_allreduce<2>(a.part + nb, v2, red, bc);
     beta = v2[0] / rho;
     rho = v2[0];
     rr = v2[1];
@@ -888,7 +812,7 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
         if (i < a.n) a.p[i] = fma(beta, pv[u], zv[u]);
       }
     }
-    if (!pcg_sync(a.bar, epoch, a.wait_ns)) break;
+    if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->rho = rho;
@@ -1090,7 +1014,18 @@ gdt_status solve(gdt_context ctx, gdt_matrix m, const double* b, double* x, cons
   const bool mixed = o->precision == GDT_PRECISION_MIXED;
   if (mixed && (o->solver != GDT_SOLVER_CG || o->precond == GDT_PREC_ILU0))
     return fail(ctx, GDT_EUNSUPPORTED, "mixed precision is provided for CG with Jacobi or no preconditioner");
-  if (mixed && mixed_stencil_supported(m)) return solve_mixed_stencil(ctx, m, b, x, o, info, s);
+  if (mixed && ctx->solver_launch != GDT_SOLVER_LAUNCH_GRAPH && mixed_mf_applies(m)) {
+    // 3D Q1 Laplace matrices: the matrix-free operator, all inner iterations in persistent launches
+    const gdt_status ms = solve_mixed_mf(ctx, m, b, x, o, info, s);
+    if (ms != GDT_EUNSUPPORTED) {
+      ctx->last_solver_launch = GDT_SOLVER_LAUNCH_PERSISTENT;
+      return ms;
+    }
+  }
+  if (mixed && mixed_stencil_supported(m)) {
+    ctx->last_solver_launch = GDT_SOLVER_LAUNCH_GRAPH;
+    return solve_mixed_stencil(ctx, m, b, x, o, info, s);
+  }
   KState* st = nullptr;
   GDT_TRY_CUDA(ctx, cudaMallocAsync(&st, sizeof(KState), s));
   KState init{};

@@ -522,4 +522,84 @@ inline gdt_status iterate_chunks_cond(gdt_context ctx, cudaStream_t s, const int
   return status;
 }
 
+// ------------------------------------------------------------- persistent (cooperative) kernels ---
+// Barrier words of a persistent launch (in the context scratch): the 64-bit arrival count at bar[0],
+// the generation the waiting blocks poll at bar[kBarGen] and the fault flag at bar[kBarFault], 4 KB
+// apart so the polls and the arrivals do not queue at the same L2 slice. All three start at zero.
+constexpr int kBarGen = 1024, kBarFault = 2048;
+constexpr unsigned long long kBarrierNs = 1000000000ull;  // default longest wait at a grid barrier (1 s)
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier (all blocks are co-resident: cooperative launch). Barrier number `epoch` (counted by
+// thread 0 of every block) is complete when the 64-bit arrival count reaches epoch * blocks; the last
+// block to arrive publishes the epoch as the generation the others poll (no reset of the count, so
+// the release is one store after the arrival). The waits are bounded by time (wait_ns, checked at the
+// first poll and every 256 polls) and by count, after which the fault flag is set and every block
+// returns false from then on. Data written before the barrier by any block is read after it with
+// plain (coherent) loads, not through the non-coherent read-only path.
+__device__ inline bool grid_barrier(unsigned int* bar, unsigned int& epoch, unsigned long long wait_ns) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ++epoch;
+    volatile unsigned int* vgen = bar + kBarGen;
+    volatile unsigned int* vfault = bar + kBarFault;
+    __threadfence();
+    int good = *vfault == 0u;
+    if (good) {
+      const unsigned long long target = (unsigned long long)epoch * gridDim.x;
+      if (atomicAdd(reinterpret_cast<unsigned long long*>(bar), 1ull) == target - 1) {
+        __threadfence();
+        atomicExch(bar + kBarGen, epoch);
+      } else {
+        const unsigned long long t0 = global_ns();
+        unsigned int spins = 0;
+        while (*vgen != epoch) {
+          ++spins;
+          if ((spins & 255u) == 1u) {
+            if (*vfault) {
+              good = 0;
+              break;
+            }
+            if (spins > (1u << 26) || global_ns() - t0 > wait_ns) {
+              atomicExch(bar + kBarFault, 1u);
+              good = 0;
+              break;
+            }
+          }
+          __nanosleep(40);
+        }
+      }
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// sum of the per-block partials part[k * gridDim.x + b] in block order, the same in every block;
+// result in every thread. red: NV * 32 doubles of shared memory, bc: NV.
+template <int NV>
+__device__ __forceinline__ void grid_allreduce(const double* part, double (&v)[NV], double* red, double* bc) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += part[k * gridDim.x + b];
+    v[k] = s;
+  }
+  block_reduce<NV>(v, red);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) bc[k] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = bc[k];
+}
+
 }  // namespace gdt

@@ -1,0 +1,685 @@
+// Mixed-precision CG for 3D Q1 Laplace matrices with element coefficients (the solve behind
+// ConstMatrixOperator::apply_inverse, operators/matrix-based.hh:131-159, for the matrices of
+// LocalLaplaceIntegrand on cube grids): FP32 inner iterations in the Chronopoulos-Gear form of CG,
+// all of them in one persistent cooperative launch per residual-replacement cycle, FP64 reliable
+// updates (residual replacement from the assembled FP64 CSR matrix) between the launches.
+//
+// Operator. The assembled matrix is the sum over the hexahedra c of kappa_c K_ref (the assembly keeps
+// the element coefficients, in FP32, and K_ref). On an axis-aligned box the Q1 stiffness depends only
+// on which coordinates of two corners differ: K_ref[i][j] = f[i ^ j] (corner bits x, y, z). So the
+// coupling of vertex v to v + d (d in {-1, 0, 1}^3) is f[|dx| + 2 |dy| + 4 |dz|] times the sum of
+// kappa over the cells that hold both vertices, and these sums come from the 2 x 2 coefficients of the
+// cell layers below and above v: per layer two row sums in each direction and their total, and the
+// four below + above pair sums. w_v = sum_t f[t] G_t, G_t the kappa-sum-weighted sum of z over the
+// neighbours of type t: 35 FMAs and 14 adds per row, where the element form takes 72. All FP32
+// vectors live on a zero-padded vertex layout (one layer of zero vertices around the grid), the
+// coefficients on a zero-padded cell layout, so no load is predicated. Dirichlet rows (unit rows,
+// zero columns) are the rows of boundary vertices: the operator's input is zb = D_m r with D_m = 0
+// there (their columns drop out) and the row itself is w_v = z_v = r_v.
+//
+// Iteration: p = z + beta p, s = w + beta s, x32 += alpha p, r -= alpha s, z = D r; w = A z;
+// gamma = r.z, delta = z.w, rr = r.r -> beta, alpha. In the persistent kernel the update is one
+// grid-stride pass over the padded arrays (the padding stays zero), then a grid barrier, then the
+// operator over vertex columns (a thread owns a column and a chunk of z planes and keeps three planes
+// of z and two layers of coefficients in registers), three partial sums per block, a second barrier,
+// and every block sums the partials in block order (bit-identical scalars in every block). The kernel
+// returns when a residual replacement is due (the iterated residual dropped 10x), the tolerance or
+// max_iter is reached, or on breakdown; the host then runs the FP64 reliable update (x64 += x32,
+// r = b - A x64 from the FP64 CSR matrix, stagnation guard) and launches it again, starting with the
+// operator on the replaced residual. Every grid-barrier wait is bounded (GDT_ECUDA when one runs out).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "linalg.cuh"
+
+namespace gdt {
+namespace {
+
+constexpr int TH = 256;
+constexpr int MT = 768;  // threads per block of the persistent kernel (one block per SM)
+
+struct MfState {
+  double alpha, beta, gamma, gamma_prev, alpha_prev;
+  double rr, rr0, rr_ref, tol2, drop;
+  int iter, max_iter, converged, flag, breakdown, updates, restarting, replaced_iter;
+};
+
+__device__ __forceinline__ bool mf_stopped(const MfState* st) { return entry_flag(&st->converged) != 0; }
+
+// geometry of the padded layouts: vertex (x, y, z), -1 <= x <= nx, at (x + 1) + PX (y + 1) + PXY (z + 1);
+// cell (cx, cy, cz), -1 <= cx <= nx - 1, at (cx + 1) + CPX (cy + 1) + CPXY (cz + 1)
+struct Mf3 {
+  int nx, ny, nz;
+  int PX;
+  long long PXY;
+  int CPX;
+  long long CPXY;
+  int ncol;      // nx * ny vertex columns
+  int chunks;    // z chunks per column in the operator pass
+  int zlen;      // planes per chunk
+  float f[8];    // K_ref[i][j] = f[i ^ j]
+  __host__ __device__ long long vidx(long long v) const {
+    const long long x = v % nx, y = (v / nx) % ny, z = v / ((long long)nx * ny);
+    return (x + 1) + PX * (y + 1) + PXY * (z + 1);
+  }
+};
+
+template <int V>
+using Ph = std::integral_constant<int, V>;
+
+// Weighted sums of one plane P of z (3 x 3 around the column) with one cell layer (2 x 2
+// coefficients k, their row sums and total sm): u3 over the four diagonal neighbours, u1 over the x
+// neighbours, u2 over the y neighbours, u0 the centre. A layer couples the plane below it and the
+// plane above it; a row gets f3 u3 + f1 u1 + f2 u2 + f0 u0 ("same", the layer next to the row's own
+// plane) and f7 u3 + f5 u1 + f6 u2 + f4 u0 ("cross", the layer between the row's plane and the
+// neighbouring plane) from each (plane, layer) pair it touches.
+struct U4 {
+  float u3, u1, u2, u0;
+};
+__device__ __forceinline__ U4 plane_layer(const float (&P)[9], const float (&k)[4], const float (&sm)[5]) {
+  U4 u;
+  u.u3 = k[0] * P[0];
+  u.u3 = fmaf(k[1], P[2], u.u3);
+  u.u3 = fmaf(k[2], P[6], u.u3);
+  u.u3 = fmaf(k[3], P[8], u.u3);
+  u.u1 = fmaf(sm[1], P[5], sm[0] * P[3]);
+  u.u2 = fmaf(sm[3], P[7], sm[2] * P[1]);
+  u.u0 = sm[4] * P[4];
+  return u;
+}
+__device__ __forceinline__ float same_of(const float (&f)[8], const U4& u) {
+  return fmaf(f[0], u.u0, fmaf(f[2], u.u2, fmaf(f[1], u.u1, f[3] * u.u3)));
+}
+__device__ __forceinline__ float cross_of(const float (&f)[8], const U4& u) {
+  return fmaf(f[4], u.u0, fmaf(f[6], u.u2, fmaf(f[5], u.u1, f[7] * u.u3)));
+}
+
+// w = A zb over rows z0 .. z1 - 1 of vertex column (x, y); accumulates r.z, z.w and r.r of those rows.
+// Row z is the sum over the cell layers z - 1 and z of their pairs with the planes they touch: the
+// layer z - 1 pairs (with planes z - 1 and z) are summed one step ahead into `carry`, so a step loads
+// plane z + 1 and layer z and keeps two planes in registers.
+template <bool DIR>
+__device__ __forceinline__ void mf3_column(const Mf3& g, int x, int y, int z0, int z1, const float* __restrict__ kap,
+                                           const float* zb, const float* r, float* w, float& gam, float& del,
+                                           float& rr) {
+  const long long vb = (x + 1) + (long long)g.PX * (y + 1) + g.PXY;  // vertex (x, y, 0)
+  const float* zc = zb + vb;
+  const float* rc = r + vb;
+  float* wc = w + vb;
+  const float* kc = kap + x + (long long)g.CPX * y + g.CPXY;  // cell (x - 1, y - 1, 0)
+  const long long PX = g.PX, PXY = g.PXY, CPX = g.CPX, CPXY = g.CPXY;
+  const bool colbnd = DIR && (x == 0 || y == 0 || x == g.nx - 1 || y == g.ny - 1);
+  float f[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) f[t] = g.f[t];
+  auto load_plane = [&](int z, float(&v)[9]) {
+    const float* q = zc + z * PXY;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = q[(k % 3 - 1) + (k / 3 - 1) * PX];
+  };
+  // the 2 x 2 coefficients of cell layer cz, their row sums over y (a = 0, 1), over x (b = 0, 1) and total
+  auto load_layer = [&](int cz, float(&k)[4], float(&sm)[5]) {
+    const float* q = kc + cz * CPXY;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) k[j] = __ldg(q + (j & 1) + (j >> 1) * CPX);
+    sm[0] = k[0] + k[2];
+    sm[1] = k[1] + k[3];
+    sm[2] = k[0] + k[1];
+    sm[3] = k[2] + k[3];
+    sm[4] = sm[0] + sm[1];
+  };
+  float P[2][9], kl[4], sl[5];
+  float carry;
+  {
+    float pm[9];
+    load_plane(z0 - 1, pm);
+    load_plane(z0, P[0]);
+    load_layer(z0 - 1, kl, sl);
+    carry = cross_of(f, plane_layer(pm, kl, sl)) + same_of(f, plane_layer(P[0], kl, sl));
+  }
+  auto step = [&](auto ph, int z) {
+    constexpr int PH = decltype(ph)::value;
+    float(&pc)[9] = P[PH];
+    float(&pn)[9] = P[PH ^ 1];
+    load_plane(z + 1, pn);
+    load_layer(z, kl, sl);
+    const U4 uc = plane_layer(pc, kl, sl), un = plane_layer(pn, kl, sl);
+    const float rv = rc[z * PXY];
+    float wv = carry + (same_of(f, uc) + cross_of(f, un));
+    carry = cross_of(f, uc) + same_of(f, un);
+    float zv = pc[4];
+    if (DIR && (colbnd || z == 0 || z == g.nz - 1)) {
+      zv = rv;  // unit row: z = r (the diagonal is 1), w = z
+      wv = rv;
+    }
+    wc[z * PXY] = wv;
+    gam = fmaf(rv, zv, gam);
+    del = fmaf(zv, wv, del);
+    rr = fmaf(rv, rv, rr);
+  };
+  int z = z0;
+  for (; z + 2 <= z1; z += 2) {
+    step(Ph<0>{}, z);
+    step(Ph<1>{}, z + 1);
+  }
+  if (z < z1) step(Ph<0>{}, z);
+}
+
+// the operator pass over the grid's (column, z chunk) items, grid-stride
+template <bool DIR>
+__device__ __forceinline__ void mf3_apply_items(const Mf3& g, const float* __restrict__ kap, const float* zb,
+                                                const float* r, float* w, float& gam, float& del, float& rr) {
+  const long long items = (long long)g.ncol * g.chunks;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items; it += stride) {
+    const int c = int(it % g.ncol), k = int(it / g.ncol);
+    const int z0 = k * g.zlen, z1 = min(g.nz, z0 + g.zlen);
+    mf3_column<DIR>(g, c % g.nx, c / g.nx, z0, z1, kap, zb, r, w, gam, del, rr);
+  }
+}
+
+// ---------------------------------------------------------------------------- persistent kernel ---
+enum { MF3_CONTINUE = 0, MF3_INIT = 1, MF3_REPLACE = 2 };
+
+struct MfPArgs {
+  Mf3 g;
+  long long n4;  // float4 groups of the padded vertex arrays
+  const float* kap;
+  const float* dm;  // D_m: Jacobi inverse diagonal (or 1), 0 on Dirichlet rows and in the padding
+  float* p;
+  float* s;
+  float* x32;
+  float* r;
+  float* w;
+  float* zb;
+  MfState* st;
+  double* part;  // 3 * gridDim.x doubles
+  unsigned int* bar;
+  unsigned long long wait_ns;
+  int start;  // MF3_INIT / MF3_REPLACE: the first pass is the operator alone
+};
+
+// The solver scalars live in shared memory (thread 0 updates them after each reduction), so the
+// registers go to the operator's planes.
+struct MfScalars {
+  double alpha, beta, gamma, gamma_prev, alpha_prev, rr;
+  int iter, done, flag, brk;
+};
+
+template <bool DIR>
+__global__ void __launch_bounds__(MT, 1) k_mf3_persistent(MfPArgs a) {
+  __shared__ double red[3 * 32];
+  __shared__ double bc[3];
+  __shared__ MfScalars sc;
+  MfState* st = a.st;
+  if (mf_stopped(st)) return;
+  if (threadIdx.x == 0) {
+    sc.alpha = st->alpha;
+    sc.beta = st->beta;
+    sc.gamma = st->gamma;
+    sc.gamma_prev = st->gamma_prev;
+    sc.alpha_prev = st->alpha_prev;
+    sc.rr = st->rr;
+    sc.iter = st->iter;
+    sc.done = sc.flag = sc.brk = 0;
+  }
+  __syncthreads();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int epoch = 0;
+  int pass = a.start;
+  while (true) {
+    if (pass == MF3_CONTINUE) {
+      // p = z + beta p, s = w + beta s, x32 += alpha p, r -= alpha s, zb = D_m r (z = D r: D_m, or 1 where
+      // D_m is 0 on a Dirichlet row; 0 in the padding, where r is 0)
+      const float af = float(sc.alpha), bf = float(sc.beta);
+      float4* p4 = reinterpret_cast<float4*>(a.p);
+      float4* s4 = reinterpret_cast<float4*>(a.s);
+      float4* x4 = reinterpret_cast<float4*>(a.x32);
+      float4* r4 = reinterpret_cast<float4*>(a.r);
+      const float4* w4 = reinterpret_cast<const float4*>(a.w);
+      const float4* d4 = reinterpret_cast<const float4*>(a.dm);
+      float4* z4 = reinterpret_cast<float4*>(a.zb);
+      for (long long i = t0; i < a.n4; i += stride) {
+        float4 pv = p4[i], sv = s4[i], xv = x4[i], rv = r4[i];
+        const float4 wv = w4[i], dv = __ldg(d4 + i);
+        float* pp = &pv.x;
+        float* ss = &sv.x;
+        float* xx = &xv.x;
+        float* rr4 = &rv.x;
+        const float* ww = &wv.x;
+        const float* dd = &dv.x;
+        float zn[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float zt = dd[u] != 0.f ? dd[u] * rr4[u] : rr4[u];
+          pp[u] = fmaf(bf, pp[u], zt);
+          ss[u] = fmaf(bf, ss[u], ww[u]);
+          xx[u] = fmaf(af, pp[u], xx[u]);
+          rr4[u] = fmaf(-af, ss[u], rr4[u]);
+          zn[u] = dd[u] * rr4[u];
+        }
+        p4[i] = pv;
+        s4[i] = sv;
+        x4[i] = xv;
+        r4[i] = rv;
+        z4[i] = make_float4(zn[0], zn[1], zn[2], zn[3]);
+      }
+      if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
+    }
+    // w = A zb and the three dots
+    float gs = 0.f, ds = 0.f, rs = 0.f;
+    mf3_apply_items<DIR>(a.g, a.kap, a.zb, a.r, a.w, gs, ds, rs);
+    double v[3] = {double(gs), double(ds), double(rs)};
+    block_reduce<3>(v, red);
+    if (threadIdx.x == 0) {
+      a.part[blockIdx.x] = v[0];
+      a.part[gridDim.x + blockIdx.x] = v[1];
+      a.part[2 * gridDim.x + blockIdx.x] = v[2];
+    }
+    if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
+    grid_allreduce<3>(a.part, v, red, bc);
+    if (threadIdx.x == 0) {
+      const double gam = v[0], del = v[1], rrn = v[2];
+      if (pass == MF3_INIT) {
+        sc.gamma_prev = gam;
+        sc.beta = 0.0;
+        sc.alpha = gam / del;
+        sc.alpha_prev = sc.alpha;
+      } else {
+        if (pass == MF3_CONTINUE) {
+          sc.gamma_prev = sc.gamma;
+          sc.alpha_prev = sc.alpha;
+        }
+        sc.beta = (pass == MF3_REPLACE && st->restarting) ? 0.0 : gam / sc.gamma_prev;
+        sc.alpha = gam / (del - sc.beta * gam / sc.alpha_prev);
+      }
+      sc.gamma = gam;
+      if (!(del > 0.0) || !isfinite(sc.alpha) || !isfinite(rrn)) {
+        sc.brk = 1;
+        sc.done = 1;
+      } else if (pass == MF3_CONTINUE) {
+        sc.iter += 1;
+        sc.rr = rrn;
+        if (rrn <= st->drop * st->rr_ref || rrn <= st->tol2 * st->rr0 || sc.iter >= st->max_iter) {
+          sc.flag = 1;
+          sc.done = 1;
+        }
+      }
+    }
+    __syncthreads();
+    if (sc.done) break;
+    pass = MF3_CONTINUE;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->alpha = sc.alpha;
+    st->beta = sc.beta;
+    st->gamma = sc.gamma;
+    st->gamma_prev = sc.gamma_prev;
+    st->alpha_prev = sc.alpha_prev;
+    st->rr = sc.rr;
+    st->iter = sc.iter;
+    st->flag = sc.flag;
+    if (sc.brk) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------ setup kernels ---
+// coefficients (lexicographic cells, FP32) into the padded cell layout
+__global__ void k_mf3_cells(Mf3 g, const float* __restrict__ kin, float* __restrict__ kout) {
+  const long long ncx = g.nx - 1, ncy = g.ny - 1, nc = ncx * ncy * (g.nz - 1);
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
+    const long long cx = c % ncx, cy = (c / ncx) % ncy, cz = c / (ncx * ncy);
+    kout[(cx + 1) + g.CPX * (cy + 1) + g.CPXY * (cz + 1)] = kin[c];
+  }
+}
+
+__device__ __forceinline__ bool on_boundary(const Mf3& g, long long v) {
+  const long long x = v % g.nx, y = (v / g.nx) % g.ny, z = v / ((long long)g.nx * g.ny);
+  return x == 0 || y == 0 || z == 0 || x == g.nx - 1 || y == g.ny - 1 || z == g.nz - 1;
+}
+
+// D_m: 1 / diag (Jacobi) or 1, and 0 on the Dirichlet rows
+__global__ void k_mf3_diag(int n, Mf3 g, const int* __restrict__ rp, const int* __restrict__ col,
+                           const double* __restrict__ val, int jacobi, int dir, float* __restrict__ dm) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double d = 1.0;
+    if (jacobi)
+      for (int k = rp[i]; k < rp[i + 1]; ++k)
+        if (col[k] == i) d = val[k];
+    dm[g.vidx(i)] = (dir && on_boundary(g, i)) ? 0.f : float(1.0 / d);
+  }
+}
+
+// probe of the operator against the assembled FP64 matrix: v(i) pseudo-random in [-1, 1]; r = v and
+// zb = v with the Dirichlet rows' entries zeroed (the operator's input convention)
+__device__ __forceinline__ double mf3_probe_value(long long i) {
+  unsigned long long h = (unsigned long long)i * 0x9E3779B97F4A7C15ull;
+  h ^= h >> 29;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 32;
+  return double(h & 0xFFFFFF) / double(0x800000) - 1.0;
+}
+
+__global__ void k_mf3_probe(int n, Mf3 g, int dir, double* __restrict__ v64, float* __restrict__ r32,
+                            float* __restrict__ zb) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = mf3_probe_value(i);
+    v64[i] = v;
+    const long long ip = g.vidx(i);
+    r32[ip] = float(v);
+    zb[ip] = (dir && on_boundary(g, i)) ? 0.f : float(v);
+  }
+}
+
+template <bool DIR>
+__global__ void __launch_bounds__(TH) k_mf3_apply(Mf3 g, const float* __restrict__ kap, const float* __restrict__ zb,
+                                                 const float* __restrict__ r, float* __restrict__ w) {
+  float a = 0.f, b = 0.f, c = 0.f;
+  mf3_apply_items<DIR>(g, kap, zb, r, w, a, b, c);
+}
+
+// err[0] = max |A64 v - w|, err[1] = max |A64 v| (non-negative floats compare as their bit patterns)
+template <int G, int PL>
+__global__ void __launch_bounds__(TH) k_mf3_compare(int n, Mf3 g, const int* __restrict__ rp,
+                                                   const int* __restrict__ col, const double* __restrict__ val,
+                                                   const double* __restrict__ v64, const float* __restrict__ w,
+                                                   unsigned int* err) {
+  float md = 0.f, my = 0.f;
+  for_rows_csr<G, PL, double>(n, rp, col, val, v64, [&](int row, bool leader, double y) {
+    if (leader) {
+      md = fmaxf(md, float(fabs(y - double(w[g.vidx(row)]))));
+      my = fmaxf(my, float(fabs(y)));
+    }
+  });
+  for (int o = 16; o > 0; o >>= 1) {
+    md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+    my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(err, __float_as_uint(md));
+    atomicMax(err + 1, __float_as_uint(my));
+  }
+}
+
+// start: r64 = b - A x (FP64), r32 = r64, zb = D_m r32; rr0
+template <int G, int PL>
+__global__ void __launch_bounds__(TH) k_mf3_init(int n, Mf3 g, const int* __restrict__ rp, const int* __restrict__ col,
+                                                const double* __restrict__ val, const double* __restrict__ x,
+                                                const double* __restrict__ b, float* __restrict__ r32,
+                                                const float* __restrict__ dm, float* __restrict__ zb, MfState* st,
+                                                double* partials, unsigned int* ticket) {
+  double a1 = 0.0;
+  for_rows_csr<G, PL, double>(n, rp, col, val, x, [&](int row, bool leader, double s) {
+    if (leader) {
+      const double ri = b[row] - s;
+      const float rf = float(ri);
+      const long long ip = g.vidx(row);
+      r32[ip] = rf;
+      zb[ip] = dm[ip] * rf;
+      a1 = fma(ri, ri, a1);
+    }
+  });
+  double v[1] = {a1};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    st->rr = st->rr0 = st->rr_ref = v[0];
+    st->drop = 0.01;
+    st->restarting = 0;
+    st->replaced_iter = -1;
+    st->iter = 0;
+    st->flag = 0;
+    st->updates = 0;
+    st->breakdown = 0;
+    st->converged = (v[0] == 0.0) ? 1 : 0;
+  }
+}
+
+// reliable update, part 1: x64 += x32, x32 = 0 (when a replacement is due, or always with `force`)
+__global__ void __launch_bounds__(TH) k_mf3_accumulate(int n, Mf3 g, double* __restrict__ x, float* __restrict__ x32,
+                                                      const MfState* st, int force) {
+  if (!force && (mf_stopped(st) || !entry_flag(&st->flag))) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const long long ip = g.vidx(i);
+    x[i] += double(x32[ip]);
+    x32[ip] = 0.f;
+  }
+}
+
+// reliable update, part 2: r64 = b - A64 x (FP64 CSR), r32 = r64, zb = D_m r32; convergence is decided
+// on this true residual only
+template <int G, int PL>
+__global__ void __launch_bounds__(TH) k_mf3_true_residual(int n, Mf3 g, const int* __restrict__ rp,
+                                                         const int* __restrict__ col, const double* __restrict__ val,
+                                                         const double* __restrict__ x, const double* __restrict__ b,
+                                                         float* __restrict__ r32, const float* __restrict__ dm,
+                                                         float* __restrict__ zb, MfState* st, double* partials,
+                                                         unsigned int* ticket) {
+  if (mf_stopped(st) || !entry_flag(&st->flag)) return;
+  double a1 = 0.0;
+  for_rows_csr<G, PL, double>(n, rp, col, val, x, [&](int row, bool leader, double s) {
+    if (leader) {
+      const double ri = b[row] - s;
+      const float rf = float(ri);
+      const long long ip = g.vidx(row);
+      r32[ip] = rf;
+      zb[ip] = dm[ip] * rf;
+      a1 = fma(ri, ri, a1);
+    }
+  });
+  double v[1] = {a1};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    // stagnation guard: a cycle that gained less than 2x on the true residual means the FP32 operator
+    // is too far from the FP64 one for the sequence to continue; from then on each replacement
+    // restarts the direction and waits for a 1000x drop (restarted FP64 refinement around FP32 CG)
+    if (!st->restarting && v[0] > 0.25 * st->rr_ref) {
+      st->restarting = 1;
+      st->drop = 1e-6;
+    }
+    st->rr_ref = v[0];
+    st->rr = v[0];
+    st->flag = 0;
+    st->updates += 1;
+    st->replaced_iter = st->iter;
+    if (v[0] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) st->converged = 1;
+    if (!isfinite(v[0])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
+// K_ref[i][j] = f[i ^ j] within FP32 rounding (axis-aligned boxes); false otherwise
+bool xor_structure(const float* K, float* f) {
+  float mx = 0.f;
+  for (int k = 0; k < 64; ++k) mx = std::max(mx, std::fabs(K[k]));
+  for (int t = 0; t < 8; ++t) f[t] = K[t];
+  for (int i = 0; i < 8; ++i)
+    for (int j = 0; j < 8; ++j)
+      if (std::fabs(K[i * 8 + j] - f[i ^ j]) > 1e-6f * mx) return false;
+  return mx > 0.f;
+}
+
+}  // namespace
+
+bool mixed_mf_applies(gdt_matrix m) {
+  const GridDesc& g = m->test.g;
+  float f[8];
+  return m->test.kind == GDT_SPACE_CG && m->test.order == 1 && g.dim == 3 && !g.simplex && m->mf_valid &&
+         m->mf_kappa && m->rows == g.nvert && g.vn[0] >= 2 && g.vn[1] >= 2 && g.vn[2] >= 2 &&
+         (g.vn[0] + 2) * (g.vn[1] + 2) * (g.vn[2] + 2) < (1LL << 31) && xor_structure(m->mf_K, f);
+}
+
+gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,
+                          gdt_solve_info* info, cudaStream_t s) {
+  const GridDesc& gd = m->test.g;
+  const int n = int(m->rows);
+  Mf3 g{};
+  g.nx = int(gd.vn[0]);
+  g.ny = int(gd.vn[1]);
+  g.nz = int(gd.vn[2]);
+  g.PX = g.nx + 2;
+  g.PXY = (long long)g.PX * (g.ny + 2);
+  g.CPX = g.nx + 1;
+  g.CPXY = (long long)g.CPX * (g.ny + 1);
+  g.ncol = g.nx * g.ny;
+  if (!xor_structure(m->mf_K, g.f)) return GDT_EUNSUPPORTED;
+  const long long nv = g.PXY * (g.nz + 2);
+  const long long ntot = (nv + 3) / 4 * 4;
+  const long long ctot = g.CPXY * (g.nz + 1);
+  const bool dir = m->mf_dirichlet != 0;
+  const int vec_blocks = std::max(1, std::min(grid_blocks(n, TH), ctx->num_sms * 8));
+  double* partials = ctx->scratch;
+  unsigned int* ticket = ctx->counters;
+
+  // persistent launch shape: one block of MT threads per SM (co-resident: cooperative launch)
+  const void* fn = dir ? reinterpret_cast<const void*>(&k_mf3_persistent<true>)
+                       : reinterpret_cast<const void*>(&k_mf3_persistent<false>);
+  int dev = 0, coop = 0, per_sm = 0;
+  GDT_TRY_CUDA(ctx, cudaGetDevice(&dev));
+  GDT_TRY_CUDA(ctx, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, MT, 0));
+  if (!coop || per_sm < 1) return GDT_EUNSUPPORTED;
+  int blocks = ctx->num_sms;
+  if (ctx->persistent_blocks > 0) blocks = std::min(blocks, ctx->persistent_blocks);
+  if (3 * blocks > kScratchDoubles / 2) return GDT_EUNSUPPORTED;
+  // (column, z chunk) items: about one per thread
+  const long long threads = (long long)blocks * MT;
+  g.chunks = int(std::max(1LL, std::min<long long>(g.nz, threads / g.ncol)));
+  g.zlen = (g.nz + g.chunks - 1) / g.chunks;
+  g.chunks = (g.nz + g.zlen - 1) / g.zlen;
+
+  std::vector<void*> allocs;
+  struct Freer {
+    std::vector<void*>* a;
+    cudaStream_t s;
+    ~Freer() {
+      for (void* p : *a) cudaFreeAsync(p, s);
+    }
+  } freer{&allocs, s};
+  auto alloc = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMallocAsync(&p, bytes + 256, s) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return reinterpret_cast<void*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
+  };
+  const size_t vb = sizeof(float) * ntot;
+  float* p = (float*)alloc(vb);
+  float* sv = (float*)alloc(vb);
+  float* x32 = (float*)alloc(vb);
+  float* r32 = (float*)alloc(vb);
+  float* w = (float*)alloc(vb);
+  float* zb = (float*)alloc(vb);
+  float* dm = (float*)alloc(vb);
+  float* kap = (float*)alloc(sizeof(float) * ctot);
+  double* v64 = (double*)alloc(sizeof(double) * n);
+  unsigned int* err = (unsigned int*)alloc(2 * sizeof(unsigned int));
+  MfState* st = (MfState*)alloc(sizeof(MfState));
+  if (!p || !sv || !x32 || !r32 || !w || !zb || !dm || !kap || !v64 || !err || !st)
+    return fail(ctx, GDT_ENOMEM, "mixed solver vectors");
+  for (float* v : {p, sv, x32, r32, w, zb, dm}) GDT_TRY_CUDA(ctx, cudaMemsetAsync(v, 0, vb, s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(kap, 0, sizeof(float) * ctot, s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(err, 0, 2 * sizeof(unsigned int), s));
+  MfState init{};
+  init.tol2 = o->tol * o->tol;
+  init.max_iter = o->max_iter;
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(st, &init, sizeof(MfState), cudaMemcpyHostToDevice, s));
+  k_mf3_cells<<<vec_blocks, TH, 0, s>>>(g, m->mf_kappa, kap);
+  k_mf3_diag<<<vec_blocks, TH, 0, s>>>(n, g, m->rp, m->col, m->val, o->precond == GDT_PREC_JACOBI, dir ? 1 : 0, dm);
+  ctx->launches += 2;
+
+  // the operator against the assembled FP64 matrix, one probe product (relative difference below 1e-4;
+  // FP32 rounding is ~1e-6): values changed after assembly make the caller take the stencil path
+  GDT_CHECK(ctx, tune_spmv(ctx, m));
+  const LaunchShape sh = schedule_shape<double>(m->spmv_sched, n, ctx->num_sms);
+  {
+    const int ablocks = int(std::min<long long>(((long long)g.ncol * g.chunks + TH - 1) / TH, 1LL << 30));
+    k_mf3_probe<<<vec_blocks, TH, 0, s>>>(n, g, dir ? 1 : 0, v64, r32, zb);
+    if (dir) k_mf3_apply<true><<<ablocks, TH, 0, s>>>(g, kap, zb, r32, w);
+    else k_mf3_apply<false><<<ablocks, TH, 0, s>>>(g, kap, zb, r32, w);
+#define GDT_MF3_COMPARE(GG, PP) \
+  k_mf3_compare<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, v64, w, err)
+    GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_COMPARE)
+#undef GDT_MF3_COMPARE
+    unsigned int herr[2] = {0u, 0u};
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(herr, err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->launches += 3;
+    float ed, ey;
+    std::memcpy(&ed, &herr[0], sizeof(float));
+    std::memcpy(&ey, &herr[1], sizeof(float));
+    if (!(ey > 0.f) || !std::isfinite(ed) || ed > 1e-4f * ey) return GDT_EUNSUPPORTED;
+    for (float* v : {r32, zb, w}) GDT_TRY_CUDA(ctx, cudaMemsetAsync(v, 0, vb, s));
+  }
+#define GDT_MF3_INIT(GG, PP)                                                                                     \
+  k_mf3_init<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, x, b, r32, dm, zb, st, \
+                                                            partials, ticket)
+  GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_INIT)
+#undef GDT_MF3_INIT
+  ctx->launches++;
+  m->mx_operator = GDT_MIXED_OPERATOR_MATRIX_FREE;
+
+  MfPArgs a{};
+  a.g = g;
+  a.n4 = ntot / 4;
+  a.kap = kap;
+  a.dm = dm;
+  a.p = p;
+  a.s = sv;
+  a.x32 = x32;
+  a.r = r32;
+  a.w = w;
+  a.zb = zb;
+  a.st = st;
+  a.part = ctx->scratch;
+  a.bar = reinterpret_cast<unsigned int*>(ctx->scratch + kScratchDoubles / 2);
+  a.wait_ns = ctx->persistent_wait_ns > 0 ? (unsigned long long)ctx->persistent_wait_ns : kBarrierNs;
+  MfState fin{};
+  unsigned int fault = 0;
+  int cycles = 0;
+  for (; cycles < 100000; ++cycles) {
+    a.start = cycles == 0 ? MF3_INIT : MF3_REPLACE;
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar, 0, sizeof(unsigned long long), s));
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarGen, 0, sizeof(unsigned int), s));
+    GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarFault, 0, sizeof(unsigned int), s));
+    void* args[] = {&a};
+    timing_begin(ctx, s, GDT_TIMING_MIXED_PERSISTENT);
+    const cudaError_t le = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(MT), args, 0, s);
+    timing_end(ctx, s);
+    GDT_TRY_CUDA(ctx, le);
+    ctx->launches++;
+    // the FP64 reliable update (both kernels return at once unless a replacement is due)
+    timing_begin(ctx, s, GDT_TIMING_RELIABLE_UPDATE);
+    k_mf3_accumulate<<<vec_blocks, TH, 0, s>>>(n, g, x, x32, st, 0);
+#define GDT_MF3_TRUE_RESIDUAL(GG, PP)                                                                            \
+  k_mf3_true_residual<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, x, b, r32, dm, \
+                                                                     zb, st, partials, ticket)
+    GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_TRUE_RESIDUAL)
+#undef GDT_MF3_TRUE_RESIDUAL
+    timing_end(ctx, s);
+    ctx->launches += 2;
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fin, st, sizeof(MfState), cudaMemcpyDeviceToHost, s));
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fault, a.bar + kBarFault, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+    if (ctx->timing) timing_harvest(ctx);
+    if (fault) return fail(ctx, GDT_ECUDA, "persistent mixed solver: a grid barrier wait ran out");
+    if (fin.converged) break;
+  }
+  {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, GDT_ECUDA, std::string("persistent mixed CG: ") + cudaGetErrorString(e));
+  }
+  gdt_solve_info res{};
+  res.iterations = fin.iter;
+  res.refinements = fin.updates;
+  res.rel_residual = fin.rr0 > 0 ? std::sqrt(fin.rr / fin.rr0) : 0.0;
+  res.converged = (!fin.breakdown && (fin.rr0 == 0 || fin.rr <= fin.tol2 * fin.rr0)) ? 1 : 0;
+  if (info) *info = res;
+  if (!res.converged) return fail(ctx, GDT_ENOCONV, "linear solver did not converge");
+  return GDT_OK;
+}
+
+}  // namespace gdt

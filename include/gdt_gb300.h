@@ -92,6 +92,8 @@ gdt_status gdt_context_spmv_timing(gdt_context ctx, double* fp64_ms, int64_t* fp
 #define GDT_TIMING_CG_DIRECTION 3   /* p = M^-1 r + beta p */
 #define GDT_TIMING_RELIABLE_UPDATE 4 /* FP64 accumulation and true residual (launched every inner
                                       * iteration, working only when a replacement is due) */
+#define GDT_TIMING_MIXED_PERSISTENT 5 /* persistent launches of the mixed-precision inner iterations
+                                       * (3D Q1 matrix-free path: one launch per replacement cycle) */
 #define GDT_TIMING_KINDS 8
 /* accumulated time (ms) and launch count of one kernel class since its last reset (all classes are
  * reset by gdt_context_spmv_timing with reset = 1) */
@@ -112,7 +114,9 @@ gdt_status gdt_measure_fp64_peak(gdt_context ctx, double* fma_tflops, double* dm
 #define GDT_SOLVER_LAUNCH_GRAPH 1
 #define GDT_SOLVER_LAUNCH_PERSISTENT 2
 gdt_status gdt_context_set_solver_launch(gdt_context ctx, int mode);
-/* launch form (GRAPH or PERSISTENT) of the context's last FP64 CG solve; 0 before the first */
+/* launch form (GRAPH or PERSISTENT) of the context's last CG solve (FP64, or mixed precision: the 3D
+ * Q1 matrix-free inner iterations run persistent under AUTO and PERSISTENT, the other mixed-precision
+ * paths as graphs); 0 before the first */
 int gdt_context_last_solver_launch(gdt_context ctx);
 /* Limits of the persistent (cooperative) solver launches (no reference counterpart; diagnostics and
  * tests of the launch form): blocks caps the grid (0: one block per SM, the default), wait_limit_ns
@@ -187,6 +191,13 @@ typedef struct gdt_diffusion_desc {
   const double* kappa_qp; /* device, diffusion at the quadrature points of every element
                            * ([element][gdt_space_quadrature point]), or NULL; order-2 spaces (or
                            * any order through the element-batched path) */
+  const double* force_qp; /* device, the source at the points of the rule
+                           * gdt_space_quadrature_order(space, force_quad_order) of every element
+                           * ([element][point]), or NULL: the load vector is then
+                           * sum_q w_q |det J| f(x_q) phi_i(x_q), the reference's product integrand
+                           * (local/integrands/product.hh:104-130) at its quadrature points, order
+                           * = order of f + order of the space (+ over_integrate) */
+  int force_quad_order;
 } gdt_diffusion_desc;
 
 /* continuous Lagrange: stiffness of LocalLaplaceIntegrand(kappa) into m, and (if rhs != NULL) the

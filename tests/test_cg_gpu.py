@@ -324,6 +324,56 @@ def test_mixed_precision_direct_launches_match_graphs(gdt, oracle, n):
     assert torch.equal(x1, x2)
 
 
+@pytest.mark.parametrize("n", [[9, 8, 7], [20, 18, 17], [33, 5, 12], [2, 3, 40]])
+@pytest.mark.parametrize("precond", ["jacobi", "none"])
+def test_mixed_persistent_matches_graph_form_and_direct(gdt, oracle, n, precond):
+    # 3D Q1 Laplace matrices: the matrix-free inner iterations in persistent launches (AUTO) against the
+    # graph form of the same Chronopoulos-Gear iteration (element-form operator kernel) and a direct
+    # solve; the two operators round differently in FP32, so iteration counts agree only closely
+    op, rhs, A, b = _heat_problem(gdt, oracle, 3, n, False)
+    xd = spl.spsolve(A.to_scipy().tocsc(), b)
+    opts = {"precision": "mixed", "tol": 1e-12, "precond": precond, "max_iter": 100000}
+    xp, ip = _solve_in(op, rhs, "auto", opts)
+    xg, ig = _solve_in(op, rhs, "graph", opts)
+    assert ip["launch"] == "persistent" and ip["inner_operator"] == "matrix_free" and ip["converged"]
+    assert ig["launch"] == "graph" and ig["converged"]
+    assert abs(ip["iterations"] - ig["iterations"]) <= max(3, 0.05 * ig["iterations"])
+    assert rel_err(xp.cpu().numpy(), xd) < 1e-10
+    assert rel_err(xg.cpu().numpy(), xd) < 1e-10
+    # deterministic reductions: a second solve repeats the iterates bit for bit
+    xp2, ip2 = _solve_in(op, rhs, "auto", opts)
+    assert ip2["iterations"] == ip["iterations"] and torch.equal(xp2, xp)
+
+
+@pytest.mark.parametrize("blocks", [1, 3])
+def test_mixed_persistent_on_few_blocks(gdt, oracle, blocks):
+    # a grid capped at 1 or 3 blocks: every thread walks several (column, z chunk) items and the update
+    # pass several float4 groups
+    op, rhs, A, b = _heat_problem(gdt, oracle, 3, [30, 28, 26], False)
+    op.ctx.set_persistent_limits(blocks=blocks)
+    try:
+        x, info = _solve_in(op, rhs, "auto", {"precision": "mixed", "tol": 1e-12})
+    finally:
+        op.ctx.set_persistent_limits()
+    assert info["launch"] == "persistent" and info["inner_operator"] == "matrix_free" and info["converged"]
+    assert rel_err(x.cpu().numpy(), spl.spsolve(A.to_scipy().tocsc(), b)) < 1e-10
+
+
+def test_mixed_persistent_barrier_wait_limit_reports_and_recovers(gdt, oracle):
+    op, rhs, A, b = _heat_problem(gdt, oracle, 3, [30, 30, 30], False)
+    op.ctx.set_persistent_limits(wait_limit_ns=1)
+    try:
+        with pytest.raises(gdt.GdtError) as e:
+            op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+    finally:
+        op.ctx.set_persistent_limits()
+    assert e.value.status == gdt._capi.ECUDA
+    assert "grid barrier wait ran out" in str(e.value)
+    x = op.apply_inverse(rhs, opts={"precision": "mixed", "tol": 1e-12})
+    assert op.last_solve_info["launch"] == "persistent" and op.last_solve_info["converged"]
+    assert rel_err(x.cpu().numpy(), spl.spsolve(A.to_scipy().tocsc(), b)) < 1e-10
+
+
 def test_mixed_precision_matrix_free_with_separate_dirichlet(gdt, oracle):
     # assembly without constraints, then DirichletConstraints::apply: the operator takes the unit rows
     # and zero columns from the constraint pass

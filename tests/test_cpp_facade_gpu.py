@@ -22,9 +22,28 @@ def test_stationary_heat_equation_example(gdt):
         assert fields[6] == "newton_steps" and int(fields[7]) == 1
         assert float(fields[9]) < 1e-8
         errs.append(float(fields[-1]))
-    # second-order convergence of the vertex error (element-barycentre source lowering)
+    # second-order convergence of the vertex error (the source at the product integrand's quadrature points)
     assert errs[1] < errs[0] / 3.0
     assert errs[1] < 2e-3
+
+
+@pytest.mark.parametrize("simplex,order", [(0, 1), (1, 1), (0, 2), (1, 2)])
+def test_facade_load_vector_matches_oracle(gdt, oracle, simplex, order):
+    # a function-valued source through the facade is evaluated at the quadrature points of its product
+    # integrand (order of f + order of the space), as the reference does: same load vector as the oracle
+    import numpy as np
+
+    exes = gdt._build.build_examples()
+    exe = [e for e in exes if e.endswith("load_vector")][0]
+    cells = 6
+    out = subprocess.run([exe, str(cells), str(simplex), str(order)], capture_output=True, text=True, timeout=300,
+                         check=True).stdout.split()
+    v = np.array([float(t) for t in out])
+    og = oracle.grid(2, [cells, cells], -1.0, 1.0, simplex=bool(simplex))
+    _, b = oracle.assemble_cg(og, order, kappa_const=1.0, force_fn=oracle.FORCE_ESV2007, force_order=3,
+                              dirichlet=False)
+    assert v.shape == b.shape
+    assert np.abs(v - b).max() <= 1e-12 * np.abs(b).max()
 
 
 @pytest.mark.parametrize("flux,name", [("numerical_upwind_flux", "upwind"),

@@ -147,3 +147,38 @@ def test_order2_solve_matches_direct(gdt, oracle, simplex):
         x = op.apply_inverse(rhs, opts={"tol": 1e-12, "precision": precision})
         assert op.last_solve_info["converged"]
         assert rel_err(x.cpu().numpy(), xd) < 1e-9
+
+
+def _esv2007_force(x):
+    # the ESV2007 source f = (pi^2 / 2) cos(pi x / 2) cos(pi y / 2) (examples/stationary-heat-equation.cc:68-70)
+    return (0.5 * np.pi) * np.pi * torch.cos(0.5 * np.pi * x[..., 0]) * torch.cos(0.5 * np.pi * x[..., 1])
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("simplex", [False, True])
+@pytest.mark.parametrize("fused", [True, False])
+def test_source_at_quadrature_points_matches_oracle(gdt, oracle, order, simplex, fused):
+    # LocalElementProductIntegrand().with_ansatz(f) with a function-valued f of order 3: the load vector
+    # from f at the points of the Gauss rule of order 3 + k, as the reference's product integrand
+    # evaluates it (local/integrands/product.hh:104-130), not from one value per element
+    n = [6, 5]
+    g = gdt.make_cube_grid([-1.0, -1.0], [1.0, 1.0], n, simplex=simplex)
+    og = oracle.grid(2, n, -1.0, 1.0, simplex=simplex)
+    A, b = oracle.assemble_cg(og, order, kappa_const=1.0, force_fn=oracle.FORCE_ESV2007, force_order=3,
+                              dirichlet=True)
+    space = gdt.ContinuousLagrangeSpace(g, order)
+    f = gdt.GridFunction(_esv2007_force, order=3)
+    if fused:
+        op = gdt.MatrixOperator(g, space)
+        op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(1.0))
+        rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+        op.assemble(rhs=rhs, force=f, dirichlet=True)
+        assert rel_err(op.csr()[2].cpu().numpy(), A.val) < 1e-12
+        assert rel_err(rhs.cpu().numpy(), b) < 1e-12
+    else:
+        vf = gdt.VectorFunctional(g, space)
+        vf.append(gdt.LocalElementIntegralFunctional(gdt.LocalElementProductIntegrand().with_ansatz(f)))
+        vf.assemble()
+        _, b_free = oracle.assemble_cg(og, order, kappa_const=1.0, force_fn=oracle.FORCE_ESV2007, force_order=3,
+                                       dirichlet=False)
+        assert rel_err(vf.vector.cpu().numpy(), b_free) < 1e-12
