@@ -21,6 +21,7 @@ __all__ = [
     "DiscontinuousLagrangeSpace", "FiniteVolumeSpace", "Stencil", "LocalLaplaceIntegrand",
     "LocalElementProductIntegrand", "LocalElementIntegralBilinearForm", "LocalElementIntegralFunctional",
     "LocalLaplaceIPDGInnerCoupling", "LocalLaplaceIPDGDirichletCoupling", "LocalIPDGInnerPenalty",
+    "LocalEllipticIpdgIntegrands",
     "LocalIPDGBoundaryPenalty", "LocalCouplingIntersectionIntegralBilinearForm",
     "LocalIntersectionIntegralBilinearForm", "MatrixOperator", "VectorFunctional", "DirichletConstraints",
     "Walker", "DiscreteFunction", "BurgersFlux", "LinearTransportFlux", "NumericalLaxFriedrichsFlux",
@@ -234,6 +235,16 @@ class _Space:
             local = xr[None].expand(g.num_elements, -1, -1)
         return lo + h * (ci[:, None, :] + local)
 
+    def face_points(self, device=None):
+        """Physical coordinates of the two Gauss points of every face of every element (DG spaces on 2D
+        simplex grids): float64 tensor [element, 3, 2, 2] (gdt_dg_face_points)."""
+        import numpy as np
+
+        out = np.zeros((self.grid.num_elements, 3, 2, 2))
+        capi.check(self.lib.gdt_dg_face_points(self.handle, out.ctypes.data_as(C.c_void_p)),
+                   what="gdt_dg_face_points")
+        return torch.tensor(out, device=device or torch.device("cuda", torch.cuda.current_device()))
+
     def global_indices(self, ctx: Context | None = None):
         """mapper.global_indices of every element: int64 CUDA tensor [num_elements, local_size]."""
         ctx = ctx or default_context()
@@ -376,18 +387,57 @@ class LocalLaplaceIPDGInnerCoupling(_Term):
 
 
 class LocalLaplaceIPDGDirichletCoupling(_Term):
-    def __init__(self, symmetry_prefactor, diffusion):
+    """Dirichlet boundary terms (local/integrands/laplace-ipdg.hh:231-368). dirichlet_data (a number, a
+    GridFunction, or a [element, 3, 2] tensor of values at the face points of gdt_dg_face_points) is read
+    only for the right-hand side, the unary term -theta int g (kappa grad psi_i . n)."""
+
+    def __init__(self, symmetry_prefactor, diffusion, dirichlet_data=0.0):
         self.symmetry_prefactor, self.diffusion = float(symmetry_prefactor), diffusion
+        self.dirichlet_data = dirichlet_data
 
 
 class LocalIPDGInnerPenalty(_Term):
-    def __init__(self, penalty, weight=None):
-        self.penalty, self.weight = float(penalty), weight
+    def __init__(self, penalty, weight=None, beta=None):
+        self.penalty, self.weight, self.beta = float(penalty), weight, beta
 
 
 class LocalIPDGBoundaryPenalty(_Term):
-    def __init__(self, penalty, weight=None):
-        self.penalty, self.weight = float(penalty), weight
+    """Dirichlet penalty sigma (n . w n) / h; with dirichlet_data, the right-hand side also gets its
+    counterpart int sigma (n . w n) / h g psi_i."""
+
+    def __init__(self, penalty, weight=None, beta=None, dirichlet_data=None):
+        self.penalty, self.weight, self.beta = float(penalty), weight, beta
+        self.dirichlet_data = dirichlet_data
+
+
+class LocalEllipticIpdgIntegrands:
+    """The deprecated combined SWIPDG integrands (local/integrands/elliptic-ipdg.hh): the same bilinear form
+    as InnerCoupling + InnerPenalty and DirichletCoupling + BoundaryPenalty, with the penalty sigma from
+    the polynomial order (Epshteyn, Riviere 2007; :452-501) and the length h^beta, beta = 1 / (d - 1)."""
+
+    @staticmethod
+    def default_beta(dim):
+        return float(capi.load().gdt_elliptic_ipdg_beta(int(dim)))
+
+    @staticmethod
+    def inner_sigma(pol_order):
+        return float(capi.load().gdt_elliptic_ipdg_sigma(int(pol_order), 0))
+
+    @staticmethod
+    def boundary_sigma(pol_order):
+        return float(capi.load().gdt_elliptic_ipdg_sigma(int(pol_order), 1))
+
+    @staticmethod
+    def Inner(diffusion, pol_order=1, dim=2, beta=None):
+        b = LocalEllipticIpdgIntegrands.default_beta(dim) if beta is None else float(beta)
+        return (LocalLaplaceIPDGInnerCoupling(1.0, diffusion, diffusion)
+                + LocalIPDGInnerPenalty(LocalEllipticIpdgIntegrands.inner_sigma(pol_order), diffusion, beta=b))
+
+    @staticmethod
+    def DirichletBoundary(diffusion, pol_order=1, dim=2, beta=None):
+        b = LocalEllipticIpdgIntegrands.default_beta(dim) if beta is None else float(beta)
+        return (LocalLaplaceIPDGDirichletCoupling(1.0, diffusion)
+                + LocalIPDGBoundaryPenalty(LocalEllipticIpdgIntegrands.boundary_sigma(pol_order), diffusion, beta=b))
 
 
 class LocalCouplingIntersectionIntegralBilinearForm:
@@ -480,18 +530,33 @@ class MatrixOperator:
         for f in self.forms:
             if isinstance(f, LocalElementIntegralBilinearForm) and isinstance(f.integrand, LocalLaplaceIntegrand):
                 kappa = f.integrand.diffusion
-        kt, kc, kq = _coef_qp(kappa)
-        self._check_qp(kq)
         d = capi.DiffusionDesc()
-        d.kappa = kt.data_ptr() if kt is not None else None
-        d.kappa_const = kc
-        d.kappa_qp = kq.data_ptr() if kq is not None else None
-        self._keep = [kt, kq] + _force_fields(d, 1.0 if rhs_force is None else rhs_force, self.source_space)
+        if isinstance(kappa, torch.Tensor) and kappa.dim() in (3, 4):
+            # a symmetric d x d tensor per element [element, d, d] or per quadrature point [element, q, d, d]
+            tt = _f64(kappa.contiguous(), name="diffusion tensor")
+            dim = self.grid.dimension
+            if tuple(tt.shape[-2:]) != (dim, dim) or tt.shape[0] != self.grid.num_elements:
+                raise ValueError(f"diffusion tensor has shape {tuple(tt.shape)}")
+            if tt.dim() == 4:
+                self._check_qp(tt[..., 0, 0])
+            d.kappa, d.kappa_const, d.kappa_qp = None, 0.0, None
+            d.kappa_tensor = tt.data_ptr() if tt.dim() == 3 else None
+            d.kappa_tensor_qp = tt.data_ptr() if tt.dim() == 4 else None
+            keep = [tt]
+        else:
+            kt, kc, kq = _coef_qp(kappa)
+            self._check_qp(kq)
+            d.kappa = kt.data_ptr() if kt is not None else None
+            d.kappa_const = kc
+            d.kappa_qp = kq.data_ptr() if kq is not None else None
+            keep = [kt, kq]
+        self._keep = keep + _force_fields(d, 1.0 if rhs_force is None else rhs_force, self.source_space)
         d.dirichlet = int(dirichlet)
         return d
 
     def _ipdg_desc(self, force=0.0):
-        kappa, theta, sig_in, sig_bd, wdiff = 1.0, 1.0, 8.0, 14.0, True
+        kappa, theta, sig_in, sig_bd, wdiff, beta = 1.0, 1.0, 8.0, 14.0, True, None
+        g_coupling, g_penalty = None, None
         for f in self.forms:
             if isinstance(f, LocalElementIntegralBilinearForm) and isinstance(f.integrand, LocalLaplaceIntegrand):
                 kappa = f.integrand.diffusion
@@ -499,10 +564,15 @@ class MatrixOperator:
                 if isinstance(t, LocalLaplaceIPDGInnerCoupling):
                     theta = t.symmetry_prefactor
                     wdiff = t.weight is not None
+                if isinstance(t, LocalLaplaceIPDGDirichletCoupling):
+                    g_coupling = t.dirichlet_data
                 if isinstance(t, LocalIPDGInnerPenalty):
                     sig_in = t.penalty
+                    beta = t.beta if t.beta is not None else beta
                 if isinstance(t, LocalIPDGBoundaryPenalty):
                     sig_bd = t.penalty
+                    beta = t.beta if t.beta is not None else beta
+                    g_penalty = t.dirichlet_data
         kt, kc = _coef(kappa)
         ft, fc = _coef(force)
         d = capi.IpdgDesc()
@@ -511,6 +581,24 @@ class MatrixOperator:
         d.force = ft.data_ptr() if ft is not None else None
         d.force_const = fc
         d.symmetry_prefactor, d.sigma_inner, d.sigma_boundary, d.weight_is_diffusion = theta, sig_in, sig_bd, int(wdiff)
+        d.penalty_beta = 0.0 if beta is None else float(beta)
+        # Dirichlet data on the right-hand side (the coupling's unary term, the penalty's counterpart)
+        data = [g for g in (g_coupling, g_penalty) if g is not None and not (isinstance(g, (int, float)) and g == 0)]
+        if len(data) == 2 and data[0] is not data[1]:
+            raise GdtError(capi.EUNSUPPORTED, "the coupling and the penalty take the same Dirichlet data")
+        d.dirichlet_rhs = (1 if data and g_coupling is data[0] else 0) | (2 if data and g_penalty is data[0] else 0)
+        self._keep_dg = []
+        if data:
+            g = data[0]
+            if isinstance(g, (int, float)):
+                d.dirichlet_face, d.dirichlet_const = None, float(g)
+            else:
+                if isinstance(g, GridFunction):
+                    g = g.fn(self.source_space.face_points())
+                g = _f64(torch.as_tensor(g, dtype=torch.float64, device=self.ctx.device).contiguous(),
+                         self.grid.num_elements * 6, "Dirichlet data")
+                d.dirichlet_face, d.dirichlet_const = g.data_ptr(), 0.0
+                self._keep_dg.append(g)
         return d
 
     def assemble(self, parallel=True, rhs=None, force=None, dirichlet=False):

@@ -32,7 +32,8 @@ SOLVER_LAUNCH_AUTO, SOLVER_LAUNCH_GRAPH, SOLVER_LAUNCH_PERSISTENT = 0, 1, 2
 class DiffusionDesc(C.Structure):
     _fields_ = [("kappa", C.c_void_p), ("kappa_const", C.c_double), ("force", C.c_void_p),
                 ("force_const", C.c_double), ("dirichlet", C.c_int), ("kappa_qp", C.c_void_p),
-                ("force_qp", C.c_void_p), ("force_quad_order", C.c_int)]
+                ("force_qp", C.c_void_p), ("force_quad_order", C.c_int), ("kappa_tensor", C.c_void_p),
+                ("kappa_tensor_qp", C.c_void_p)]
 
 
 class ProductDesc(C.Structure):
@@ -42,7 +43,8 @@ class ProductDesc(C.Structure):
 class IpdgDesc(C.Structure):
     _fields_ = [("kappa", C.c_void_p), ("kappa_const", C.c_double), ("force", C.c_void_p),
                 ("force_const", C.c_double), ("symmetry_prefactor", C.c_double), ("sigma_inner", C.c_double),
-                ("sigma_boundary", C.c_double), ("weight_is_diffusion", C.c_int)]
+                ("sigma_boundary", C.c_double), ("weight_is_diffusion", C.c_int), ("penalty_beta", C.c_double),
+                ("dirichlet_face", C.c_void_p), ("dirichlet_const", C.c_double), ("dirichlet_rhs", C.c_int)]
 
 
 class SolverOpts(C.Structure):
@@ -128,6 +130,9 @@ _SIGNATURES = {
     "gdt_space_quadrature_order": (C.c_int, [P, C.c_int, P, P]),
     "gdt_element_error": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P, C.POINTER(C.c_double)]),
     "gdt_assemble_swipdg": (C.c_int, [P, P, C.POINTER(IpdgDesc), P]),
+    "gdt_dg_face_points": (C.c_int, [P, P]),
+    "gdt_elliptic_ipdg_sigma": (C.c_double, [C.c_int, C.c_int]),
+    "gdt_elliptic_ipdg_beta": (C.c_double, [C.c_int]),
     "gdt_lincomb": (C.c_int, [P, C.c_int64, C.c_int, C.POINTER(P), C.POINTER(C.c_double), P]),
     "gdt_matrix_lincomb": (C.c_int, [P, P, C.c_int, C.POINTER(P), C.POINTER(C.c_double)]),
     "gdt_spmv": (C.c_int, [P, P, P, P]),

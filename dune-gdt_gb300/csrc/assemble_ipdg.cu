@@ -25,6 +25,8 @@ namespace {
 struct TriFace {
   double n[2];
   double vol;
+  double hb;          // vol^beta: the penalty's length scale
+  double xq[2][2];    // the two Gauss points, relative to the element's cell corner
   double w[2];        // quadrature weight * integration element
   double vin[2][3];   // own basis at the face points
   double vout[2][3];  // neighbour basis at the same points
@@ -76,7 +78,7 @@ void grads(const double X[3][2], double G[3][2]) {
   G[0][1] = -G[1][1] - G[2][1];
 }
 
-TriTables make_tables(const GridDesc& g) {
+TriTables make_tables(const GridDesc& g, double beta = 1.0) {
   TriTables T = {};
   const double h[2] = {g.h[0], g.h[1]};
   const double gq = 0.5 / std::sqrt(3.0);
@@ -105,6 +107,7 @@ TriTables make_tables(const GridDesc& g) {
         if (v != opp) (a < 0 ? a : b) = v;
       const double ex = X[b][0] - X[a][0], ey = X[b][1] - X[a][1];
       F.vol = std::sqrt(ex * ex + ey * ey);
+      F.hb = beta == 1.0 ? F.vol : std::pow(F.vol, beta);
       double nx = ey / F.vol, ny = -ex / F.vol;
       if ((X[opp][0] - X[a][0]) * nx + (X[opp][1] - X[a][1]) * ny > 0) {
         nx = -nx;
@@ -123,6 +126,8 @@ TriTables make_tables(const GridDesc& g) {
       }
       for (int q = 0; q < 2; ++q) {
         const double x[2] = {X[a][0] + xi[q] * ex, X[a][1] + xi[q] * ey};
+        F.xq[q][0] = x[0];
+        F.xq[q][1] = x[1];
         F.w[q] = 0.5 * F.vol;
         bary(X, x, F.vin[q]);
         bary(Y, x, F.vout[q]);
@@ -135,7 +140,37 @@ TriTables make_tables(const GridDesc& g) {
 struct IpdgParams {
   double theta, sigma_in, sigma_bd;
   int weight_is_diffusion;
+  // Dirichlet data on the boundary faces for the right-hand side: g at the two Gauss points of each
+  // face ([element][face][point]) or the constant g_const; rhs_terms bit 0: the unary DirichletCoupling
+  // term, bit 1: the boundary penalty's counterpart
+  const double* g_face;
+  double g_const;
+  int rhs_terms;
 };
+
+// right-hand side of boundary face f: sum_q w_q g_q (-theta (kappa grad psi_i . n) [bit 0]
+// + sigma (n . w n) / h^beta psi_i(x_q) [bit 1]) (local/integrands/laplace-ipdg.hh:292-320 and the
+// product of the boundary penalty's weight with g)
+__device__ __forceinline__ void boundary_rhs(const TriTables& T, int t, int f, long long e, double kin,
+                                             const IpdgParams& p, double b[3]) {
+  const TriFace& F = T.F[t][f];
+  const double w = p.weight_is_diffusion ? kin : 1.0;
+  const double penalty = (p.sigma_bd * w) / F.hb;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const double gq = p.g_face ? p.g_face[(e * 3 + f) * 2 + q] : p.g_const;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      double v = 0.0;
+      if (p.rhs_terms & 1) {
+        const double dn = (kin * T.G[t][i][0]) * F.n[0] + (kin * T.G[t][i][1]) * F.n[1];
+        v += -1.0 * p.theta * gq * dn;
+      }
+      if (p.rhs_terms & 2) v += penalty * gq * F.vin[q][i];
+      b[i] += v * F.w[q];
+    }
+  }
+}
 
 // in/in (Bii) and in/out (Bio) blocks of an inner face seen from the element of type t
 __device__ __forceinline__ void inner_blocks(const TriTables& T, int t, int f, double kin, double kout,
@@ -145,7 +180,7 @@ __device__ __forceinline__ void inner_blocks(const TriTables& T, int t, int f, d
   const double delta_plus = wout, delta_minus = win;  // n.(w n) with |n| = 1
   const double weight_minus = delta_plus / (delta_plus + delta_minus);
   const double weight_plus = delta_minus / (delta_plus + delta_minus);
-  const double penalty = (p.sigma_in * ((delta_plus * delta_minus) / (delta_plus + delta_minus))) / F.vol;
+  const double penalty = (p.sigma_in * ((delta_plus * delta_minus) / (delta_plus + delta_minus))) / F.hb;
   double dn_in[3], dn_out[3];
   const int tn = F.tnb;
 #pragma unroll
@@ -183,7 +218,7 @@ __device__ __forceinline__ void boundary_block(const TriTables& T, int t, int f,
                                                double Bb[3][3]) {
   const TriFace& F = T.F[t][f];
   const double w = p.weight_is_diffusion ? kin : 1.0;
-  const double penalty = (p.sigma_bd * w) / F.vol;
+  const double penalty = (p.sigma_bd * w) / F.hb;
   double dn[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) dn[i] = (kin * T.G[t][i][0]) * F.n[0] + (kin * T.G[t][i][1]) * F.n[1];
@@ -244,8 +279,15 @@ __global__ void __launch_bounds__(128) swipdg_rows(GridDesc g, TriTables T, Ipdg
   }
   if (rhs) {
     const double fe = force ? force[e] : force_const;
+    double b[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) rhs[3 * e + i] = fe * T.B[t][i];
+    for (int i = 0; i < 3; ++i) b[i] = fe * T.B[t][i];
+    if (p.rhs_terms)
+#pragma unroll
+      for (int f = 0; f < 3; ++f)
+        if (nb[f] < 0) boundary_rhs(T, t, f, e, kin, p, b);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) rhs[3 * e + i] = b[i];
   }
   // block order by element index: A: f0, self, f1, f2; B: f0, f1, self, f2
 #pragma unroll
@@ -326,11 +368,30 @@ bool supported(const GridDesc& g) { return g.dim == 2 && g.simplex; }
 gdt_status assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs) {
   const GridDesc& g = m->test.g;
   if (!supported(g)) return fail(ctx, GDT_EUNSUPPORTED, "SWIPDG assembly is provided for 2D simplex grids");
-  const TriTables T = make_tables(g);
-  const IpdgParams p{d->symmetry_prefactor, d->sigma_inner, d->sigma_boundary, d->weight_is_diffusion};
+  if (d->penalty_beta < 0.0 || (d->dirichlet_rhs & ~3)) return fail(ctx, GDT_EINVAL, "SWIPDG descriptor");
+  const TriTables T = make_tables(g, d->penalty_beta > 0.0 ? d->penalty_beta : 1.0);
+  const IpdgParams p{d->symmetry_prefactor, d->sigma_inner, d->sigma_boundary, d->weight_is_diffusion,
+                     d->dirichlet_face, d->dirichlet_const, d->dirichlet_rhs};
   swipdg_rows<<<grid_blocks(g.nelem, 128), 128, 0, ctx->stream>>>(g, T, p, m->rp, m->val, rhs, d->kappa,
                                                                   d->kappa_const, d->force, d->force_const);
   return check_launch(ctx, "swipdg_rows");
+}
+
+gdt_status dg_face_points(const gdt_space_s& sp, double* xy) {
+  const GridDesc& g = sp.g;
+  if (!supported(g)) return GDT_EUNSUPPORTED;
+  const TriTables T = make_tables(g);
+  for (long long e = 0; e < g.nelem; ++e) {
+    const int t = int(e & 1);
+    const long long c = e >> 1, cx = c % g.n[0], cy = c / g.n[0];
+    for (int f = 0; f < 3; ++f)
+      for (int q = 0; q < 2; ++q) {
+        double* out = xy + ((e * 3 + f) * 2 + q) * 2;
+        out[0] = g.lo[0] + double(cx) * g.h[0] + T.F[t][f].xq[q][0];
+        out[1] = g.lo[1] + double(cy) * g.h[1] + T.F[t][f].xq[q][1];
+      }
+  }
+  return GDT_OK;
 }
 
 gdt_status swipdg_dlogkappa(gdt_context ctx, const gdt_space_s& sp, const gdt_ipdg_desc* d, const double* u,
@@ -338,8 +399,8 @@ gdt_status swipdg_dlogkappa(gdt_context ctx, const gdt_space_s& sp, const gdt_ip
   const GridDesc& g = sp.g;
   if (!supported(g)) return fail(ctx, GDT_EUNSUPPORTED, "SWIPDG adjoint is provided for 2D simplex grids");
   if (!d->weight_is_diffusion) return fail(ctx, GDT_EUNSUPPORTED, "adjoint needs the SWIPDG weight (kappa)");
-  const TriTables T = make_tables(g);
-  const IpdgParams p{d->symmetry_prefactor, d->sigma_inner, d->sigma_boundary, 1};
+  const TriTables T = make_tables(g, d->penalty_beta > 0.0 ? d->penalty_beta : 1.0);
+  const IpdgParams p{d->symmetry_prefactor, d->sigma_inner, d->sigma_boundary, 1, nullptr, 0.0, 0};
   swipdg_dlogkappa_kernel<<<grid_blocks(g.nelem, 128), 128, 0, ctx->stream>>>(g, T, p, d->kappa, u, lam, out);
   return check_launch(ctx, "swipdg_dlogkappa");
 }

@@ -341,7 +341,12 @@ gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_di
   if (d->force_qp && d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
   // a source at quadrature points: the matrix first, then the load vector from its own pass
   double* rhs_fused = d->force_qp ? nullptr : rhs;
-  if (m->test.order == 2 || d->kappa_qp) {
+  if (d->kappa_tensor || d->kappa_tensor_qp) {
+    m->mf_valid = 0;
+    GDT_CHECK(ctx, ho_prepare(ctx, m));
+    GDT_CHECK(ctx, ho_assemble_tensor(ctx, m, d->kappa_tensor, d->kappa_tensor_qp, d->force, d->force_const,
+                                      rhs_fused, d->dirichlet));
+  } else if (m->test.order == 2 || d->kappa_qp) {
     m->mf_valid = 0;
     GDT_CHECK(ctx, ho_prepare(ctx, m));
     GDT_CHECK(ctx, ho_assemble(ctx, m, 0, d->kappa, d->kappa_const, d->kappa_qp, d->force, d->force_const, rhs_fused,
@@ -410,6 +415,18 @@ gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_des
   m->val_version++;
   return assemble_swipdg(ctx, m, d, rhs);
 }
+
+gdt_status gdt_dg_face_points(gdt_space dg, double* xy) {
+  if (!dg || !xy || dg->kind != GDT_SPACE_DG) return GDT_EINVAL;
+  return dg_face_points(*dg, xy);
+}
+
+// local/integrands/elliptic-ipdg.hh:452-501 (inner_sigma, boundary_sigma) and :442-445 (default_beta)
+double gdt_elliptic_ipdg_sigma(int pol_order, int boundary) {
+  if (boundary) return pol_order <= 1 ? 14.0 : pol_order <= 2 ? 38.0 : pol_order <= 3 ? 74.0 : 100.0;
+  return pol_order <= 1 ? 8.0 : pol_order <= 2 ? 20.0 : pol_order <= 3 ? 38.0 : 50.0;
+}
+double gdt_elliptic_ipdg_beta(int dim) { return dim > 1 ? 1.0 / (dim - 1.0) : 1.0; }
 
 gdt_status gdt_spmv(gdt_context ctx, gdt_matrix m, const double* x, double* y) {
   if (!ctx || !m || !x || !y) return GDT_EINVAL;

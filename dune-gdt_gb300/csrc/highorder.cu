@@ -401,6 +401,11 @@ ContractionTables contraction_tables(const GridDesc& g, int order) {
   T.stiff.assign(msize * T.ntypes, 0.0);
   T.mass.assign(msize * T.ntypes, 0.0);
   T.load.assign(size_t(T.lsize) * T.nq * T.ntypes, 0.0);
+  T.ncomp = g.dim * (g.dim + 1) / 2;
+  T.nqt = T.nq * T.ncomp;
+  T.nqt_pad = (T.nqt + 3) / 4 * 4;
+  const size_t tsize = size_t(T.npair_pad) * T.nqt_pad;
+  T.stiff_t.assign(tsize * T.ntypes, 0.0);
   std::vector<double> phi(fe.size), grbuf(3 * fe.size);
   double(*gr)[3] = reinterpret_cast<double(*)[3]>(grbuf.data());
   for (int t = 0; t < T.ntypes; ++t) {
@@ -424,6 +429,12 @@ ContractionTables contraction_tables(const GridDesc& g, int order) {
         for (int a = 0; a < g.dim; ++a) dot += pg[i][a] * pg[j][a];
         T.stiff[msize * t + size_t(p) * T.nq_pad + k] = wq * dot;
         T.mass[msize * t + size_t(p) * T.nq_pad + k] = wq * phi[i] * phi[j];
+        int c = 0;
+        for (int a = 0; a < g.dim; ++a)
+          for (int b = a; b < g.dim; ++b, ++c) {
+            const double v = a == b ? pg[i][a] * pg[j][a] : pg[i][a] * pg[j][b] + pg[i][b] * pg[j][a];
+            T.stiff_t[tsize * t + size_t(p) * T.nqt_pad + size_t(k) * T.ncomp + c] = wq * v;
+          }
       }
       for (int i = 0; i < fe.size; ++i) T.load[(size_t(t) * T.lsize + i) * T.nq + k] = wq * phi[i];
     }
@@ -614,12 +625,14 @@ struct HoMatrix {
   int* gi = nullptr;      // [nelem][lsize] DoF indices
   int* smap = nullptr;    // [nelem][lsize][lsize] CSR positions
   double* stiff = nullptr, *mass = nullptr, *load = nullptr;  // contraction tables (device)
+  double* stiff_t = nullptr;  // tensor-diffusion table, uploaded at its first use
   int* pi = nullptr, *pj = nullptr;
 };
 
 void ho_matrix_free(HoMatrix* h) {
   if (!h) return;
-  for (void* p : {(void*)h->gi, (void*)h->smap, (void*)h->stiff, (void*)h->mass, (void*)h->load, (void*)h->pi, (void*)h->pj})
+  for (void* p : {(void*)h->gi, (void*)h->smap, (void*)h->stiff, (void*)h->mass, (void*)h->load, (void*)h->pi,
+                  (void*)h->pj, (void*)h->stiff_t})
     if (p) cudaFree(p);
   delete h;
 }
@@ -989,6 +1002,69 @@ gdt_status ho_assemble(gdt_context ctx, gdt_matrix m, int form, const double* co
     ctx->launches += rhs ? 2 : 1;
   }
   GDT_CHECK(ctx, check_launch(ctx, "order-2 assembly"));
+  if (dirichlet) GDT_CHECK(ctx, ho_dirichlet(ctx, m, rhs));
+  return GDT_OK;
+}
+
+namespace {
+// the components (a <= b) of a symmetric d x d tensor per element or per quadrature point, as the
+// coefficient columns (q, c) of the tensor contraction: out[e][q * ncomp + c] = kappa(e, q)[a][b]
+__global__ void k_tensor_columns(long long ne, int dim, int nq, int ncomp, const double* __restrict__ kt,
+                                 const double* __restrict__ kt_qp, double* __restrict__ out) {
+  const long long n = ne * nq * ncomp;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < n; w += (long long)gridDim.x * blockDim.x) {
+    const long long e = w / (nq * ncomp);
+    const int r = int(w % (nq * ncomp)), q = r / ncomp, c = r % ncomp;
+    int a = 0, b = 0, k = 0;
+    for (int aa = 0; aa < dim; ++aa)
+      for (int bb = aa; bb < dim; ++bb, ++k)
+        if (k == c) {
+          a = aa;
+          b = bb;
+        }
+    const double* K = kt_qp ? kt_qp + ((size_t)e * nq + q) * dim * dim : kt + (size_t)e * dim * dim;
+    out[w] = K[a * dim + b];
+  }
+}
+}  // namespace
+
+gdt_status ho_assemble_tensor(gdt_context ctx, gdt_matrix m, const double* kt, const double* kt_qp,
+                              const double* force, double force_const, double* rhs, int dirichlet) {
+  HoMatrix* h = static_cast<HoMatrix*>(m->ho);
+  if (!h) return fail(ctx, GDT_EUNSUPPORTED, "matrix has no element-batched assembly data");
+  cudaStream_t st = ctx->stream;
+  const GridDesc& g = m->test.g;
+  const ho::ContractionTables& T = h->tab;
+  if (!h->stiff_t) {
+    gdt_status s = GDT_OK;
+    h->stiff_t = dalloc<double>(ctx, T.stiff_t.size(), s);
+    if (s != GDT_OK) return s;
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(h->stiff_t, T.stiff_t.data(), sizeof(double) * T.stiff_t.size(),
+                                      cudaMemcpyHostToDevice, st));
+  }
+  double* cols = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&cols, sizeof(double) * size_t(g.nelem) * T.nqt, st));
+  k_tensor_columns<<<vec_grid(g.nelem * T.nqt, ctx->num_sms), 256, 0, st>>>(g.nelem, g.dim, T.nq, T.ncomp, kt, kt_qp,
+                                                                         cols);
+  ctx->launches++;
+  const int ncolours = (1 << g.dim) * g.nsub;
+  const size_t tsize = size_t(T.npair_pad) * T.nqt_pad;
+  if (m->val) GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * (m->nnz + 8), st));
+  if (rhs) GDT_TRY_CUDA(ctx, cudaMemsetAsync(rhs, 0, sizeof(double) * m->rows, st));
+  for (int k = 0; k < ncolours; ++k) {
+    const Colour c = colour_of(g, k);
+    if (c.total == 0) continue;
+    const long long tasks = (c.total + 7) / 8 * ((T.npair_pad / 8 + kTileGroup - 1) / kTileGroup);
+    const int blocks = int(std::max(1LL, std::min<long long>((tasks + 7) / 8, ctx->num_sms * 8LL)));
+    k_ho_contract<<<blocks, 256, 0, st>>>(g, c, h->stiff_t + tsize * c.t, T.npair, T.npair_pad, T.nqt, T.nqt_pad,
+                                          h->pi, h->pj, nullptr, 0.0, cols, h->smap, T.lsize, m->val);
+    if (rhs)
+      k_ho_rhs<<<vec_grid(c.total * T.lsize, ctx->num_sms), 256, 0, st>>>(
+          g, c, h->load + size_t(c.t) * T.lsize * T.nq, T.lsize, T.nq, force, force_const, h->gi, rhs);
+    ctx->launches += rhs ? 2 : 1;
+  }
+  GDT_TRY_CUDA(ctx, cudaFreeAsync(cols, st));
+  GDT_CHECK(ctx, check_launch(ctx, "tensor diffusion assembly"));
   if (dirichlet) GDT_CHECK(ctx, ho_dirichlet(ctx, m, rhs));
   return GDT_OK;
 }

@@ -28,6 +28,11 @@ struct ContractionTables {
   std::vector<int> pi, pj;
   std::vector<double> stiff, mass;  // [type][npair_pad][nq_pad]
   std::vector<double> load;         // [type][lsize][nq]
+  // tensor diffusion: columns (q, c) over the components c = (a, b), a <= b, of a symmetric d x d
+  // tensor (lexicographic), nqt = nq * d (d + 1) / 2 padded to 4: w_q |J| (da phi_i db phi_j + db phi_i
+  // da phi_j) for a < b, w_q |J| da phi_i da phi_j for a = b
+  int ncomp = 1, nqt = 0, nqt_pad = 0;
+  std::vector<double> stiff_t;      // [type][npair_pad][nqt_pad]
 };
 ContractionTables contraction_tables(const GridDesc& g, int order);
 
@@ -56,6 +61,10 @@ gdt_status ho_build_pattern(gdt_context ctx, gdt_matrix m);
 gdt_status ho_assemble(gdt_context ctx, gdt_matrix m, int form, const double* coef, double coef_const,
                        const double* coef_qp, const double* force, double force_const, double* rhs, int dirichlet);
 gdt_status ho_dirichlet(gdt_context ctx, gdt_matrix m, double* rhs);
+// LocalLaplaceIntegrand with a symmetric d x d diffusion tensor, per element ([element][d][d]) or at
+// the points of gdt_space_quadrature ([element][q][d][d]); load vector and Dirichlet as ho_assemble
+gdt_status ho_assemble_tensor(gdt_context ctx, gdt_matrix m, const double* kt, const double* kt_qp,
+                              const double* force, double force_const, double* rhs, int dirichlet);
 gdt_status ho_prepare(gdt_context ctx, gdt_matrix m);
 gdt_status ho_assemble_rhs(gdt_context ctx, const gdt_space_s& sp, const double* force, double force_const,
                            int dirichlet, double* rhs);

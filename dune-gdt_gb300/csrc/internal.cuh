@@ -141,6 +141,7 @@ gdt_status cg_dlogkappa(gdt_context ctx, const gdt_space_s& s, const double* kap
                         const double* lam, double* out);
 // assemble_ipdg.cu
 gdt_status assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs);
+gdt_status dg_face_points(const gdt_space_s& sp, double* xy);
 gdt_status swipdg_dlogkappa(gdt_context ctx, const gdt_space_s& s, const gdt_ipdg_desc* d, const double* u,
                             const double* lam, double* out);
 // spmv.cu

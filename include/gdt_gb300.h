@@ -198,6 +198,12 @@ typedef struct gdt_diffusion_desc {
                            * (local/integrands/product.hh:104-130) at its quadrature points, order
                            * = order of f + order of the space (+ over_integrate) */
   int force_quad_order;
+  const double* kappa_tensor;    /* device, a symmetric d x d diffusion tensor per element
+                                  * ([element][d][d], row-major), or NULL: LocalLaplaceIntegrand's
+                                  * (kappa(x) grad phi_j) . grad psi_i (local/integrands/laplace.hh:81-102)
+                                  * with a tensor; the element-batched path, any order */
+  const double* kappa_tensor_qp; /* device, the same at the points of gdt_space_quadrature
+                                  * ([element][q][d][d]), or NULL */
 } gdt_diffusion_desc;
 
 /* continuous Lagrange: stiffness of LocalLaplaceIntegrand(kappa) into m, and (if rhs != NULL) the
@@ -250,11 +256,33 @@ typedef struct gdt_ipdg_desc {
   double sigma_inner;        /* inner penalty */
   double sigma_boundary;     /* Dirichlet penalty */
   int weight_is_diffusion;   /* 1: SWIPDG (weight = kappa), 0: weight = 1 */
+  double penalty_beta;       /* penalty sigma gamma / h^beta with h = |I|; 0: beta = 1, the h of
+                              * LocalIPDGIntegrands (local/integrands/ipdg.hh:27-38). The deprecated
+                              * LocalEllipticIpdgIntegrands use beta = 1 / (d - 1)
+                              * (local/integrands/elliptic-ipdg.hh:442-445, 677-741) */
+  const double* dirichlet_face; /* device, Dirichlet data g at the two Gauss points of every face of every
+                                 * element ([element][face][point], the points of gdt_dg_face_points;
+                                 * boundary faces are read), or NULL */
+  double dirichlet_const;       /* g where dirichlet_face is NULL */
+  int dirichlet_rhs;            /* right-hand side terms of g on the boundary faces: bit 0 the unary
+                                 * DirichletCoupling term -theta int g (kappa grad psi_i . n)
+                                 * (local/integrands/laplace-ipdg.hh:292-320), bit 1 the boundary penalty's
+                                 * counterpart int sigma (n . w n) / h^beta g psi_i (a product integrand on
+                                 * the boundary intersections with that weight); 0: homogeneous */
 } gdt_ipdg_desc;
 
 /* DG Lagrange order 1: element Laplace + InnerCoupling/InnerPenalty (inner intersections) +
- * DirichletCoupling/BoundaryPenalty (homogeneous Dirichlet boundary), penalty length h = |I|. */
+ * DirichletCoupling/BoundaryPenalty (Dirichlet boundary), penalty length h = |I|^beta; the load vector
+ * of the force plus the Dirichlet data terms selected by dirichlet_rhs. */
 gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* desc, double* rhs);
+/* physical coordinates of the two Gauss points of every face of every element of a DG space on a 2D
+ * simplex grid (host array [element][face][point][2]): where gdt_ipdg_desc.dirichlet_face is given */
+gdt_status gdt_dg_face_points(gdt_space dg, double* xy);
+/* the penalty parameters of the deprecated LocalEllipticIpdgIntegrands (Epshteyn, Riviere 2007;
+ * local/integrands/elliptic-ipdg.hh:452-501): sigma by polynomial order for inner (boundary = 0) or
+ * Dirichlet boundary (boundary = 1) faces, and beta = 1 / (d - 1) */
+double gdt_elliptic_ipdg_sigma(int pol_order, int boundary);
+double gdt_elliptic_ipdg_beta(int dim);
 
 /* Inner FP32 operator of the last mixed-precision CG solve with this matrix (-1: none yet):
  * the symmetric stencil of the assembled values (linear or plane-tiled kernel), or, for 3D Q1

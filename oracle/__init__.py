@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 CG, DG, FV = 0, 1, 2
 STENCIL_ELEMENT, STENCIL_INTERSECTION, STENCIL_ELEMENT_AND_INTERSECTION = 0, 1, 2
 FORCE_DATA, FORCE_ESV2007 = 0, 1
+DIRICHLET_CONST, DIRICHLET_TEST = 0, 1
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 PREC_NONE, PREC_JACOBI, PREC_ILU0 = 0, 1, 2
 FLUX_BURGERS, FLUX_TRANSPORT = 0, 1
@@ -91,9 +92,13 @@ def lib():
             "orc_csr_import": (C.c_void_p, [C.c_long, lp, ip, dp]),
             "orc_csr_free": (None, [C.c_void_p]),
             "orc_assemble_cg": (C.c_void_p, [g, C.c_int, dp, C.c_double, dp, C.c_double, C.c_int, C.c_int, C.c_int, dp]),
+            "orc_assemble_cg_tensor": (C.c_void_p, [g, C.c_int, dp, dp, C.c_double, C.c_int, dp]),
             "orc_assemble_mass": (C.c_void_p, [g, C.c_int, C.c_int]),
             "orc_assemble_swipdg": (C.c_void_p, [g, C.c_int, dp, C.c_double, dp, C.c_double, C.c_int, C.c_int,
                                                  C.c_double, C.c_double, C.c_double, C.c_int, dp]),
+            "orc_assemble_swipdg_data": (C.c_void_p, [g, C.c_int, dp, C.c_double, dp, C.c_double, C.c_int, C.c_int,
+                                                      C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
+                                                      C.c_int, C.c_double, C.c_int, dp]),
             "orc_swipdg_dlogkappa": (None, [g, C.c_int, dp, C.c_double, C.c_double, C.c_double, dp, dp, dp]),
             "orc_cg_dlogkappa": (None, [g, C.c_int, dp, dp, dp, dp]),
             "orc_spmv": (None, [C.c_void_p, dp, dp]),
@@ -203,19 +208,34 @@ def assemble_cg(g, order=1, kappa=None, kappa_const=1.0, force=None, force_const
     return CSR(h), rhs
 
 
+def assemble_cg_tensor(g, order, kappa_tensor, force=None, force_const=1.0, dirichlet=True):
+    """Laplace stiffness with a d x d diffusion tensor per element ([element, d, d]) + load vector."""
+    n = space_size(g, CG, order)
+    rhs = np.zeros(n)
+    kt = np.ascontiguousarray(kappa_tensor, dtype=np.float64)
+    frc = None if force is None else np.ascontiguousarray(force, dtype=np.float64)
+    h = lib().orc_assemble_cg_tensor(C.byref(g), order, _dp(kt), _dp(frc), force_const, int(dirichlet), _dp(rhs))
+    return CSR(h), rhs
+
+
 def assemble_mass(g, kind, order):
     return CSR(lib().orc_assemble_mass(C.byref(g), kind, order))
 
 
 def assemble_swipdg(g, order=1, kappa=None, kappa_const=1.0, force=None, force_const=1.0, force_fn=FORCE_DATA,
-                    force_order=0, theta=1.0, sigma_inner=8.0, sigma_boundary=14.0, weight_is_diffusion=True):
+                    force_order=0, theta=1.0, sigma_inner=8.0, sigma_boundary=14.0, weight_is_diffusion=True,
+                    beta=1.0, dirichlet_fn=DIRICHLET_CONST, dirichlet_const=0.0, dirichlet_rhs=0):
+    """SWIPDG matrix + right-hand side; beta: penalty length |I|^beta; dirichlet_rhs: bit 0 the unary
+    DirichletCoupling term, bit 1 the boundary penalty weight times g (g = dirichlet_const, or the test
+    function cos(pi x / 2) cos(pi y / 2) + 0.3 x with dirichlet_fn = DIRICHLET_TEST)."""
     n = space_size(g, DG, order)
     rhs = np.zeros(n)
     kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
     frc = None if force is None else np.ascontiguousarray(force, dtype=np.float64)
-    h = lib().orc_assemble_swipdg(C.byref(g), order, _dp(kap), kappa_const, _dp(frc), force_const, force_fn,
-                                  force_order, theta, sigma_inner, sigma_boundary, int(weight_is_diffusion),
-                                  _dp(rhs))
+    h = lib().orc_assemble_swipdg_data(C.byref(g), order, _dp(kap), kappa_const, _dp(frc), force_const, force_fn,
+                                       force_order, theta, sigma_inner, sigma_boundary, int(weight_is_diffusion),
+                                       float(beta), int(dirichlet_fn), float(dirichlet_const), int(dirichlet_rhs),
+                                       _dp(rhs))
     return CSR(h), rhs
 
 

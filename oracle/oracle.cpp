@@ -412,6 +412,35 @@ struct ElementKernel {
         }
     }
   }
+  // LocalLaplaceIntegrand::evaluate with a d x d diffusion tensor K (local/integrands/laplace.hh:81-102):
+  // (K grad phi_j) . grad psi_i, K row-major
+  void laplace_tensor(const Geometry& geo, const double* K, double* A) const {
+    int n = fe.size;
+    for (int i = 0; i < n * n; ++i) A[i] = 0.0;
+    double G[27][3];
+    for (size_t q = 0; q < qa.size(); ++q) {
+      double Jit[3][3];
+      double det = geo.jit(qa[q].x, Jit);
+      double factor = det * qa[q].w;
+      const double* dp = &dphi_a[q * n * 3];
+      for (int i = 0; i < n; ++i)
+        for (int r = 0; r < 3; ++r) {
+          double s = 0;
+          for (int k = 0; k < g.dim; ++k) s += Jit[r][k] * dp[i * 3 + k];
+          G[i][r] = s;
+        }
+      for (int ii = 0; ii < n; ++ii)
+        for (int jj = 0; jj < n; ++jj) {
+          double v = 0.0;
+          for (int rr = 0; rr < g.dim; ++rr) {
+            double kg = 0.0;  // (K grad phi_j)_rr
+            for (int ss = 0; ss < g.dim; ++ss) kg += K[rr * g.dim + ss] * G[jj][ss];
+            v += kg * G[ii][rr];
+          }
+          A[ii * n + jj] += v * factor;
+        }
+    }
+  }
   // LocalElementProductIntegrand (local/integrands/product.hh:104-130), weight 1
   void mass(const Geometry& geo, double* A) const {
     int n = fe.size;
@@ -442,6 +471,18 @@ struct ElementKernel {
 struct FaceParams {
   double theta = 1.0, sigma_in = 8.0, sigma_bd = 14.0;
   bool weight_is_diffusion = true;
+  double beta = 1.0;  // penalty length h = |I|^beta (local/integrands/elliptic-ipdg.hh:677-741; 1: ipdg.hh)
+  // Dirichlet data for the right-hand side: ORC_DIRICHLET_CONST (g = gconst) or ORC_DIRICHLET_TEST
+  // (g = cos(pi x / 2) cos(pi y / 2) + 0.3 x); rhs_terms bit 0: the unary DirichletCoupling term
+  // (local/integrands/laplace-ipdg.hh:292-320), bit 1: the boundary penalty weight times g
+  int gfn = 0;
+  double gconst = 0.0;
+  int rhs_terms = 0;
+  double h(double vol) const { return beta == 1.0 ? vol : std::pow(vol, beta); }
+  double g(const Vec3& x) const {
+    if (gfn == ORC_DIRICHLET_TEST) return std::cos(kHalfPi * x[0]) * std::cos(kHalfPi * x[1]) + 0.3 * x[0];
+    return gconst;
+  }
 };
 
 struct FaceKernel {
@@ -483,8 +524,7 @@ struct FaceKernel {
     const double weight_minus = delta_plus / (delta_plus + delta_minus);
     const double weight_plus = delta_minus / (delta_plus + delta_minus);
     const double pen_weight = (delta_plus * delta_minus) / (delta_plus + delta_minus);
-    const double h = I.volume;
-    const double penalty = (p.sigma_in * pen_weight) / h;
+    const double penalty = (p.sigma_in * pen_weight) / p.h(I.volume);
     const double th = p.theta;
     double vin[27], vout[27], Gin[27][3], Gout[27][3], dn_in[27], dn_out[27];
     for (const auto& qp : qf) {
@@ -533,7 +573,7 @@ struct FaceKernel {
     double w = p.weight_is_diffusion ? kin : 1.0;
     double nn = 0;
     for (int r = 0; r < g.dim; ++r) nn += nrm[r] * nrm[r];
-    const double penalty = (p.sigma_bd * (w * nn)) / I.volume;
+    const double penalty = (p.sigma_bd * (w * nn)) / p.h(I.volume);
     double v[27], G[27][3], dn[27];
     for (const auto& qp : qf) {
       Vec3 x = face_global(g, I, qp.x);
@@ -551,6 +591,33 @@ struct FaceKernel {
           val += penalty * v[jj] * v[ii];
           B[ii * n + jj] += val * factor;
         }
+    }
+  }
+  // right-hand side of a Dirichlet boundary face: LocalIntersectionIntegralFunctional with the unary
+  // DirichletCoupling integrand -theta g (kappa grad psi_i . n) (local/integrands/laplace-ipdg.hh:292-320)
+  // and, with bit 1, the boundary penalty's weight sigma (n . w n) / h times g psi_i
+  void boundary_rhs(const Intersection& I, const Geometry& gin, double kin, const FaceParams& p, double* b) const {
+    int n = fe.size;
+    for (int i = 0; i < n; ++i) b[i] = 0.0;
+    const Vec3& nrm = I.normal;
+    double w = p.weight_is_diffusion ? kin : 1.0;
+    double nn = 0;
+    for (int r = 0; r < g.dim; ++r) nn += nrm[r] * nrm[r];
+    const double penalty = (p.sigma_bd * (w * nn)) / p.h(I.volume);
+    double v[27], G[27][3];
+    for (const auto& qp : qf) {
+      Vec3 x = face_global(g, I, qp.x);
+      double factor = (I.volume / ref_vol) * qp.w;
+      basis_at(gin, x, v, G);
+      const double gx = p.g(x);
+      for (int ii = 0; ii < n; ++ii) {
+        double dn = 0;
+        for (int r = 0; r < g.dim; ++r) dn += (kin * G[ii][r]) * nrm[r];
+        double val = 0.0;
+        if (p.rhs_terms & 1) val += -1.0 * p.theta * gx * dn;
+        if (p.rhs_terms & 2) val += penalty * gx * v[ii];
+        b[ii] += val * factor;
+      }
     }
   }
 };
@@ -707,6 +774,40 @@ extern "C" orc_csr* orc_assemble_cg(const orc_grid* gd, int order, const double*
   return m;
 }
 
+// the same walk with a d x d diffusion tensor per element (kappa_tensor[e * d * d + r * d + s])
+extern "C" orc_csr* orc_assemble_cg_tensor(const orc_grid* gd, int order, const double* kappa_tensor,
+                                           const double* force, double force_const, int dirichlet, double* rhs) {
+  Grid g = make_grid(gd);
+  Space s;
+  build_space(g, ORC_CG, order, s);
+  orc_csr* m = build_pattern(g, s, s, ORC_STENCIL_ELEMENT, nullptr);
+  Coeffs c{nullptr, 1.0, force, force_const, ORC_FORCE_DATA, 0};
+  int k = s.fe.basis_order();
+  ElementKernel K(g, s.fe, 0 + k + k, k);
+  if (rhs) std::fill(rhs, rhs + s.size, 0.0);
+  int n = s.lsize;
+  set_threads();
+  int ncol = g_threads > 1 ? (1 << g.dim) : 1;
+  for (int colour = 0; colour < ncol; ++colour) {
+#pragma omp parallel for schedule(static) if (g_threads > 1)
+    for (long e = 0; e < g.nelem; ++e) {
+      if (ncol > 1 && colour_of(g, e) != colour) continue;
+      double A[27 * 27], b[27];
+      long gv[8];
+      Geometry geo = element_geometry(g, e, gv);
+      K.laplace_tensor(geo, kappa_tensor + e * g.dim * g.dim, A);
+      const int64_t* gi = s.indices(e);
+      scatter(m, gi, gi, n, A);
+      if (rhs) {
+        K.rhs(geo, c, e, b);
+        for (int i = 0; i < n; ++i) rhs[gi[i]] += b[i];
+      }
+    }
+  }
+  if (dirichlet) apply_dirichlet(m, rhs, dirichlet_dofs(g, s));
+  return m;
+}
+
 extern "C" orc_csr* orc_assemble_mass(const orc_grid* gd, int kind, int order) {
   Grid g = make_grid(gd);
   Space s;
@@ -723,10 +824,26 @@ extern "C" orc_csr* orc_assemble_mass(const orc_grid* gd, int kind, int order) {
   return m;
 }
 
+extern "C" orc_csr* orc_assemble_swipdg_data(const orc_grid* gd, int order, const double* kappa,
+                                             double kappa_const, const double* force, double force_const,
+                                             int force_fn, int force_order, double theta, double sigma_in,
+                                             double sigma_bd, int weight_is_diffusion, double beta, int gfn,
+                                             double gconst, int rhs_terms, double* rhs);
+
 extern "C" orc_csr* orc_assemble_swipdg(const orc_grid* gd, int order, const double* kappa, double kappa_const,
                                         const double* force, double force_const, int force_fn, int force_order,
                                         double theta, double sigma_in, double sigma_bd, int weight_is_diffusion,
                                         double* rhs) {
+  return orc_assemble_swipdg_data(gd, order, kappa, kappa_const, force, force_const, force_fn, force_order, theta,
+                                  sigma_in, sigma_bd, weight_is_diffusion, 1.0, ORC_DIRICHLET_CONST, 0.0, 0, rhs);
+}
+
+// the same with the penalty length |I|^beta and Dirichlet data on the right-hand side
+extern "C" orc_csr* orc_assemble_swipdg_data(const orc_grid* gd, int order, const double* kappa,
+                                             double kappa_const, const double* force, double force_const,
+                                             int force_fn, int force_order, double theta, double sigma_in,
+                                             double sigma_bd, int weight_is_diffusion, double beta, int gfn,
+                                             double gconst, int rhs_terms, double* rhs) {
   // test/stationary-eocstudies/diffusion-ipdg.hh:283-326: element Laplace on all elements,
   // coupling terms on InnerIntersectionsOnce, Dirichlet terms on boundary intersections.
   Grid g = make_grid(gd);
@@ -739,7 +856,7 @@ extern "C" orc_csr* orc_assemble_swipdg(const orc_grid* gd, int order, const dou
   int k = s.fe.basis_order();
   ElementKernel K(g, s.fe, k + k, force_order + k);
   FaceKernel F(g, s.fe, k + k);
-  FaceParams p{theta, sigma_in, sigma_bd, weight_is_diffusion != 0};
+  FaceParams p{theta, sigma_in, sigma_bd, weight_is_diffusion != 0, beta, gfn, gconst, rhs_terms};
   if (rhs) std::fill(rhs, rhs + s.size, 0.0);
   int n = s.lsize;
   double A[27 * 27], B1[27 * 27], B2[27 * 27], B3[27 * 27], B4[27 * 27], b[27];
@@ -764,7 +881,10 @@ extern "C" orc_csr* orc_assemble_swipdg(const orc_grid* gd, int order, const dou
       } else if (I.outside < 0) {
         F.boundary(I, geo, c.k(e), p, B1);
         scatter(m, s.indices(e), s.indices(e), n, B1);
-        // homogeneous Dirichlet data: the unary DirichletCoupling RHS term vanishes
+        if (rhs && p.rhs_terms) {
+          F.boundary_rhs(I, geo, c.k(e), p, b);
+          for (int i = 0; i < n; ++i) rhs[s.indices(e)[i]] += b[i];
+        }
       }
     }
   }

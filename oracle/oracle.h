@@ -62,6 +62,9 @@ void orc_csr_free(orc_csr* m);
 orc_csr* orc_assemble_cg(const orc_grid* g, int order, const double* kappa, double kappa_const,
                          const double* force, double force_const, int force_fn, int force_order,
                          int dirichlet, double* rhs);
+/* the same with a d x d diffusion tensor per element, row-major (local/integrands/laplace.hh:81-102) */
+orc_csr* orc_assemble_cg_tensor(const orc_grid* g, int order, const double* kappa_tensor, const double* force,
+                                double force_const, int dirichlet, double* rhs);
 /* the element mass matrix (LocalElementProductIntegrand with weight 1) of a CG/DG space */
 orc_csr* orc_assemble_mass(const orc_grid* g, int kind, int order);
 /* SWIPDG/IPDG with DG Lagrange elements (element Laplace + InnerCoupling/InnerPenalty on inner
@@ -70,6 +73,16 @@ orc_csr* orc_assemble_swipdg(const orc_grid* g, int order, const double* kappa, 
                              const double* force, double force_const, int force_fn, int force_order,
                              double symmetry_prefactor, double sigma_inner, double sigma_boundary,
                              int weight_is_diffusion, double* rhs);
+/* Dirichlet data of orc_assemble_swipdg_data: a constant, or the test function
+ * g = cos(pi x / 2) cos(pi y / 2) + 0.3 x */
+enum { ORC_DIRICHLET_CONST = 0, ORC_DIRICHLET_TEST = 1 };
+/* orc_assemble_swipdg with the penalty length |I|^beta (local/integrands/elliptic-ipdg.hh:677-741) and the
+ * right-hand side terms of Dirichlet data g (rhs_terms bit 0: the unary DirichletCoupling term,
+ * local/integrands/laplace-ipdg.hh:292-320; bit 1: the boundary penalty weight times g) */
+orc_csr* orc_assemble_swipdg_data(const orc_grid* g, int order, const double* kappa, double kappa_const,
+                                  const double* force, double force_const, int force_fn, int force_order,
+                                  double theta, double sigma_in, double sigma_bd, int weight_is_diffusion,
+                                  double beta, int gfn, double gconst, int rhs_terms, double* rhs);
 /* -d/dlog(kappa_e) [lam^T A(kappa) u] for the SWIPDG operator, by Richardson-extrapolated central
  * differences of the element's own local contributions. */
 void orc_swipdg_dlogkappa(const orc_grid* g, int order, const double* kappa, double symmetry_prefactor,

@@ -182,3 +182,33 @@ def test_source_at_quadrature_points_matches_oracle(gdt, oracle, order, simplex,
         _, b_free = oracle.assemble_cg(og, order, kappa_const=1.0, force_fn=oracle.FORCE_ESV2007, force_order=3,
                                        dirichlet=False)
         assert rel_err(vf.vector.cpu().numpy(), b_free) < 1e-12
+
+
+@pytest.mark.parametrize("dim,n,simplex", GRIDS[1:])
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("per_point", [False, True])
+def test_tensor_diffusion_matches_oracle(gdt, oracle, dim, n, simplex, order, per_point):
+    # LocalLaplaceIntegrand with a symmetric positive definite d x d diffusion tensor per element
+    # (local/integrands/laplace.hh:81-102), given per element or repeated at every quadrature point
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    ne = g.num_elements
+    rng = np.random.default_rng(40 + dim + order)
+    L = rng.standard_normal((ne, dim, dim))
+    K = np.einsum("eab,ecb->eac", L, L) + 0.5 * np.eye(dim)[None]
+    force = rng.uniform(-1, 2, ne)
+    A, b = oracle.assemble_cg_tensor(og, order, K, force=force, dirichlet=True)
+    space = gdt.ContinuousLagrangeSpace(g, order)
+    kt = torch.tensor(K, device="cuda")
+    if per_point:
+        nq = space.quadrature()[0].shape[0]
+        kt = kt[:, None].expand(ne, nq, dim, dim).contiguous()
+    op = gdt.MatrixOperator(g, space)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kt))
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    op.assemble(rhs=rhs, force=torch.tensor(force, device="cuda"), dirichlet=True)
+    rp, col, val = op.csr()
+    assert csr_equal_pattern((rp, col, val), A)
+    assert rel_err(val.cpu().numpy(), A.val) < 1e-12
+    assert rel_err(rhs.cpu().numpy(), b) < 1e-12
+    x = op.apply_inverse(rhs, opts={"tol": 1e-13})
+    assert rel_err(x.cpu().numpy(), spl.spsolve(A.to_scipy().tocsc(), b)) < 1e-10

@@ -106,3 +106,26 @@ def test_chronopoulos_gear_recurrences_match_cg(oracle):
     assert np.linalg.norm(x - xd) <= 1e-9 * np.linalg.norm(xd)
     _, it_cg, _, _ = oracle.solve(oracle.assemble_cg(og, 1, kappa=kappa, force_const=1.0)[0], b, tol=1e-12)
     assert abs(its - it_cg) <= 2
+
+
+@pytest.mark.parametrize("dim,n,simplex,order", [(2, [4, 3], False, 1), (2, [3, 3], True, 2), (3, [2, 3, 2], False, 1),
+                                                 (3, [2, 2, 2], True, 1)])
+def test_tensor_diffusion_restatement_reduces_to_scalar(oracle, dim, n, simplex, order):
+    # LocalLaplaceIntegrand with a tensor (local/integrands/laplace.hh:81-102): kappa_e * I gives the
+    # scalar assembly (pinned to the reference's known answers) to rounding, and the transpose of an
+    # anisotropic tensor's matrix is the matrix of the transposed tensor
+    og = oracle.grid(dim, n, 0.0, 1.0, simplex=simplex)
+    ne = oracle.num_elements(og)
+    rng = np.random.default_rng(31)
+    kappa = np.exp(rng.standard_normal(ne))
+    A, b = oracle.assemble_cg(og, order, kappa=kappa, force_const=1.0, dirichlet=False)
+    At, bt = oracle.assemble_cg_tensor(og, order, kappa[:, None, None] * np.eye(dim)[None], force_const=1.0,
+                                       dirichlet=False)
+    assert np.array_equal(A.col, At.col)
+    assert np.abs(A.val - At.val).max() <= 1e-14 * np.abs(A.val).max()
+    assert np.abs(b - bt).max() <= 1e-14 * np.abs(b).max()
+    K = rng.standard_normal((ne, dim, dim))
+    M1, _ = oracle.assemble_cg_tensor(og, order, K, dirichlet=False)
+    M2, _ = oracle.assemble_cg_tensor(og, order, np.transpose(K, (0, 2, 1)), dirichlet=False)
+    S1, S2 = M1.to_scipy(), M2.to_scipy()
+    assert abs(S1 - S2.T).max() <= 1e-13 * abs(S1).max()

@@ -112,3 +112,73 @@ def test_autograd_gradient_matches_central_differences(gdt, dg):
             lm[e] -= h
             fd = (J(lp).item() - J(lm).item()) / (2 * h)
         assert abs(fd - grad[e]) <= 1e-5 * max(abs(grad).max(), 1e-30)
+
+
+def _dirichlet_test_fn(x):
+    # the oracle's Dirichlet test data g = cos(pi x / 2) cos(pi y / 2) + 0.3 x
+    return torch.cos(0.5 * np.pi * x[..., 0]) * torch.cos(0.5 * np.pi * x[..., 1]) + 0.3 * x[..., 0]
+
+
+def _dg_operator(gdt, g, kt, coupling, penalty):
+    space = gdt.DiscontinuousLagrangeSpace(g, 1)
+    op = gdt.MatrixOperator(g, space, stencil=gdt.Stencil.element_and_intersection)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kt))
+    op += gdt.LocalCouplingIntersectionIntegralBilinearForm(
+        gdt.LocalLaplaceIPDGInnerCoupling(1.0, kt, kt) + gdt.LocalIPDGInnerPenalty(8.0, kt))
+    op += gdt.LocalIntersectionIntegralBilinearForm(coupling + penalty)
+    return space, op
+
+
+@pytest.mark.parametrize("terms", [1, 2, 3])
+@pytest.mark.parametrize("data", ["function", "constant"])
+def test_swipdg_dirichlet_data_matches_oracle(gdt, oracle, terms, data):
+    # non-homogeneous Dirichlet data on the right-hand side: the unary DirichletCoupling term
+    # -theta int g (kappa grad psi_i . n) (local/integrands/laplace-ipdg.hh:292-320) and/or the boundary
+    # penalty's counterpart, g a function evaluated at the face quadrature points or a constant
+    n = [12, 9]
+    g = gdt.make_cube_grid([-1, -1], [1, 1], n, simplex=True)
+    og = oracle.grid(2, n, -1.0, 1.0, simplex=True)
+    kappa = np.exp(np.random.default_rng(21).standard_normal(g.num_elements))
+    kt = torch.tensor(kappa, device="cuda")
+    gd = gdt.GridFunction(_dirichlet_test_fn, order=3) if data == "function" else 0.7
+    coupling = gdt.LocalLaplaceIPDGDirichletCoupling(1.0, kt, gd if terms & 1 else 0.0)
+    penalty = gdt.LocalIPDGBoundaryPenalty(14.0, kt, dirichlet_data=gd if terms & 2 else None)
+    space, op = _dg_operator(gdt, g, kt, coupling, penalty)
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    op.assemble(rhs=rhs, force=1.0)
+    A, b = oracle.assemble_swipdg(og, 1, kappa=kappa, force_const=1.0,
+                                  dirichlet_fn=oracle.DIRICHLET_TEST if data == "function" else oracle.DIRICHLET_CONST,
+                                  dirichlet_const=0.7, dirichlet_rhs=terms)
+    assert rel_err(op.csr()[2].cpu().numpy(), A.val) < 1e-12
+    assert rel_err(rhs.cpu().numpy(), b) < 1e-12
+    _, b0 = oracle.assemble_swipdg(og, 1, kappa=kappa, force_const=1.0)
+    assert np.abs(b - b0).max() > 1e-6 * np.abs(b0).max()  # the data terms are not negligible
+
+
+@pytest.mark.parametrize("beta", [None, 0.5])
+def test_deprecated_elliptic_ipdg_integrands(gdt, oracle, beta):
+    # LocalEllipticIpdgIntegrands (local/integrands/elliptic-ipdg.hh): sigma from the polynomial order
+    # (8 inner, 14 boundary for order 1) and the penalty length |I|^beta, beta = 1 / (d - 1) by default;
+    # in 2D the default is the LaplaceIPDG form exactly, another beta changes the penalty only
+    assert gdt.LocalEllipticIpdgIntegrands.inner_sigma(1) == 8.0
+    assert gdt.LocalEllipticIpdgIntegrands.boundary_sigma(1) == 14.0
+    assert gdt.LocalEllipticIpdgIntegrands.inner_sigma(2) == 20.0 and gdt.LocalEllipticIpdgIntegrands.boundary_sigma(3) == 74.0
+    assert gdt.LocalEllipticIpdgIntegrands.default_beta(2) == 1.0 and gdt.LocalEllipticIpdgIntegrands.default_beta(3) == 0.5
+    n = [10, 7]
+    g = gdt.make_cube_grid([0, 0], [1, 1], n, simplex=True)
+    og = oracle.grid(2, n, 0.0, 1.0, simplex=True)
+    kappa = np.exp(np.random.default_rng(22).standard_normal(g.num_elements))
+    kt = torch.tensor(kappa, device="cuda")
+    space = gdt.DiscontinuousLagrangeSpace(g, 1)
+    op = gdt.MatrixOperator(g, space, stencil=gdt.Stencil.element_and_intersection)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kt))
+    op += gdt.LocalCouplingIntersectionIntegralBilinearForm(gdt.LocalEllipticIpdgIntegrands.Inner(kt, beta=beta))
+    op += gdt.LocalIntersectionIntegralBilinearForm(gdt.LocalEllipticIpdgIntegrands.DirichletBoundary(kt, beta=beta))
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    op.assemble(rhs=rhs, force=1.0)
+    A, b = oracle.assemble_swipdg(og, 1, kappa=kappa, force_const=1.0, beta=1.0 if beta is None else beta)
+    assert rel_err(op.csr()[2].cpu().numpy(), A.val) < 1e-12
+    assert rel_err(rhs.cpu().numpy(), b) < 1e-12
+    if beta is not None:
+        A1, _ = oracle.assemble_swipdg(og, 1, kappa=kappa, force_const=1.0)
+        assert np.abs(A.val - A1.val).max() > 1e-3 * np.abs(A1.val).max()
