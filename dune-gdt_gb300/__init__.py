@@ -333,6 +333,32 @@ def _force_fields(d, force, space):
     return [ft]
 
 
+def _dirichlet_values(d, values, space, ctx):
+    """Sets dirichlet_values / dirichlet_value_const of a DiffusionDesc: a number, a per-DoF float64
+    tensor or a GridFunction (evaluated at the vertices, the DoFs of order-1 continuous spaces)."""
+    d.dirichlet_values, d.dirichlet_value_const = None, 0.0
+    if values is None:
+        return []
+    if isinstance(values, (int, float)):
+        d.dirichlet_value_const = float(values)
+        return []
+    if isinstance(values, GridFunction):
+        g = space.grid
+        dim = g.dimension
+        vn = [c + 1 for c in g.num_cells]
+        idx = torch.arange(space.num_DoFs, device=ctx.device)
+        coords = []
+        for a in range(dim):
+            i = idx % vn[a]
+            idx = idx // vn[a]
+            h = (g.upper_right[a] - g.lower_left[a]) / g.num_cells[a]
+            coords.append(g.lower_left[a] + h * i.to(torch.float64))
+        values = torch.as_tensor(values.fn(torch.stack(coords, -1)), dtype=torch.float64, device=ctx.device)
+    t = _f64(values.contiguous(), space.num_DoFs, "Dirichlet values")
+    d.dirichlet_values = t.data_ptr()
+    return [t]
+
+
 class LocalLaplaceIntegrand:
     def __init__(self, diffusion=1.0):
         self.diffusion = diffusion
@@ -601,8 +627,10 @@ class MatrixOperator:
                 self._keep_dg.append(g)
         return d
 
-    def assemble(self, parallel=True, rhs=None, force=None, dirichlet=False):
-        """MatrixOperator::assemble; optionally fused with the load vector / Dirichlet constraints."""
+    def assemble(self, parallel=True, rhs=None, force=None, dirichlet=False, dirichlet_values=None):
+        """MatrixOperator::assemble; optionally fused with the load vector / Dirichlet constraints.
+        dirichlet_values (continuous order 1): a number, a per-DoF tensor or a GridFunction of the
+        boundary values; the constrained columns move to the right-hand side."""
         if isinstance(self.source_space, DiscontinuousLagrangeSpace):
             d = self._ipdg_desc(0.0 if force is None else force)
             self.ctx.call("gdt_assemble_swipdg", self.handle, C.byref(d), _ptr(rhs))
@@ -623,7 +651,9 @@ class MatrixOperator:
                 self.ctx.call("gdt_assemble_cg_product", self.handle, C.byref(pd))
                 return self
             d = self._diffusion_desc(force, dirichlet)
+            keep = _dirichlet_values(d, dirichlet_values, self.source_space, self.ctx)
             self.ctx.call("gdt_assemble_cg_diffusion", self.handle, C.byref(d), _ptr(rhs))
+            del keep
         return self
 
     def apply(self, source, range=None):
@@ -799,10 +829,19 @@ class DirichletConstraints:
         self.ctx = ctx or default_context()
         self.applied_in_walk = False
 
-    def apply(self, matrix_operator, vector=None):
+    def apply(self, matrix_operator, vector=None, values=None):
+        """DirichletConstraints::apply(M, V); with values (continuous order 1: a number, a per-DoF tensor
+        or a GridFunction) the boundary rows get those values and the constrained columns move to V."""
         if self.applied_in_walk:
             return
-        self.ctx.call("gdt_dirichlet_apply", matrix_operator.handle, _ptr(vector))
+        if values is None:
+            self.ctx.call("gdt_dirichlet_apply", matrix_operator.handle, _ptr(vector))
+            return
+        d = capi.DiffusionDesc()
+        keep = _dirichlet_values(d, values, self.space, self.ctx)
+        self.ctx.call("gdt_dirichlet_apply_values", matrix_operator.handle, _ptr(vector), C.c_void_p(d.dirichlet_values),
+                      C.c_double(d.dirichlet_value_const))
+        del keep
 
 
 class Walker:

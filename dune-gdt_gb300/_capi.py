@@ -33,7 +33,8 @@ class DiffusionDesc(C.Structure):
     _fields_ = [("kappa", C.c_void_p), ("kappa_const", C.c_double), ("force", C.c_void_p),
                 ("force_const", C.c_double), ("dirichlet", C.c_int), ("kappa_qp", C.c_void_p),
                 ("force_qp", C.c_void_p), ("force_quad_order", C.c_int), ("kappa_tensor", C.c_void_p),
-                ("kappa_tensor_qp", C.c_void_p)]
+                ("kappa_tensor_qp", C.c_void_p), ("dirichlet_values", C.c_void_p),
+                ("dirichlet_value_const", C.c_double)]
 
 
 class ProductDesc(C.Structure):
@@ -125,6 +126,7 @@ _SIGNATURES = {
     "gdt_assemble_cg_diffusion": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_assemble_cg_rhs": (C.c_int, [P, P, C.POINTER(DiffusionDesc), P]),
     "gdt_dirichlet_apply": (C.c_int, [P, P, P]),
+    "gdt_dirichlet_apply_values": (C.c_int, [P, P, P, P, C.c_double]),
     "gdt_assemble_cg_product": (C.c_int, [P, P, C.POINTER(ProductDesc)]),
     "gdt_space_quadrature": (C.c_int, [P, P, P]),
     "gdt_space_quadrature_order": (C.c_int, [P, C.c_int, P, P]),

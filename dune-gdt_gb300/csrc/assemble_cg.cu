@@ -111,7 +111,8 @@ __global__ void __launch_bounds__(256) assemble_cg_rows(GridDesc g, const int* _
                                                         double* __restrict__ rhs, const LocalTables tab,
                                                         const double* __restrict__ kappa,
                                                         double kappa_const, const double* __restrict__ force,
-                                                        double force_const, int dirichlet) {
+                                                        double force_const, int dirichlet,
+                                                        const double* __restrict__ gD, double gD_const) {
   constexpr int NS = pow3(DIM), NSUB = num_sub(DIM, SIMPLEX), NLOC = num_local(DIM, SIMPLEX);
   const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (v >= g.nvert) return;
@@ -148,7 +149,24 @@ __global__ void __launch_bounds__(256) assemble_cg_rows(GridDesc g, const int* _
     }
   }
   const bool bnd = dirichlet && on_boundary(g, vi, DIM);
-  if (rhs) rhs[v] = bnd ? 0.0 : b;
+  // Dirichlet values g: b_v = g_v on a boundary row; elsewhere the zeroed columns move to the right-hand
+  // side, b_v -= sum over boundary neighbours w of A_vw g_w (all zero for homogeneous data)
+  const bool lift = dirichlet && rhs && (gD || gD_const != 0.0);
+  if (lift && !bnd) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      if (!slot_in_stencil(DIM, SIMPLEX, k)) continue;
+      long long w[3] = {0, 0, 0};
+      bool ok = true;
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        w[a] = vi[a] + slot_offset(k, a);
+        ok = ok && w[a] >= 0 && w[a] <= g.n[a];
+      }
+      if (ok && on_boundary(g, w, DIM)) b -= acc[k] * (gD ? gD[w[0] + g.vn[0] * (w[1] + g.vn[1] * w[2])] : gD_const);
+    }
+  }
+  if (rhs) rhs[v] = bnd ? (lift ? (gD ? gD[v] : gD_const) : 0.0) : b;
   if (!val) return;
   long long pos = rp[v];
 #pragma unroll
@@ -175,12 +193,15 @@ __global__ void __launch_bounds__(256) assemble_cg_rows(GridDesc g, const int* _
 // boundary DoFs, zero boundary columns elsewhere (pattern is symmetric), rhs[D] = 0.
 template <int DIM>
 __global__ void dirichlet_rows(GridDesc g, const int* __restrict__ rp, const int* __restrict__ col,
-                               double* __restrict__ val, double* __restrict__ rhs) {
+                               double* __restrict__ val, double* __restrict__ rhs, const double* __restrict__ gD,
+                               double gD_const) {
   const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (v >= g.nvert) return;
   long long vi[3];
   vertex_multi(g, v, vi);
   const bool bnd = on_boundary(g, vi, DIM);
+  const bool lift = rhs && (gD || gD_const != 0.0);
+  double b = (lift && !bnd) ? rhs[v] : 0.0;
   for (int k = rp[v]; k < rp[v + 1]; ++k) {
     const long long w = col[k];
     if (bnd) {
@@ -188,10 +209,14 @@ __global__ void dirichlet_rows(GridDesc g, const int* __restrict__ rp, const int
     } else {
       long long wi[3];
       vertex_multi(g, w, wi);
-      if (on_boundary(g, wi, DIM)) val[k] = 0.0;
+      if (on_boundary(g, wi, DIM)) {
+        if (lift) b -= val[k] * (gD ? gD[w] : gD_const);
+        val[k] = 0.0;
+      }
     }
   }
-  if (rhs && bnd) rhs[v] = 0.0;
+  if (rhs && bnd) rhs[v] = lift ? (gD ? gD[v] : gD_const) : 0.0;
+  else if (lift) rhs[v] = b;
 }
 
 // -lam_e^T (dA_e / dlog kappa_e) u_e = -kappa_e lam_e^T K_t u_e, Dirichlet rows and columns excluded
@@ -271,7 +296,7 @@ gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* 
   cudaStream_t s = ctx->stream;
 #define GDT_LAUNCH_ASM(D, S)                                                                                   \
   assemble_cg_rows<D, S><<<bl, th, 0, s>>>(g, m->rp, m->val, rhs, tab, d->kappa, d->kappa_const, d->force, d->force_const, \
-                                           d->dirichlet)
+                                           d->dirichlet, d->dirichlet_values, d->dirichlet_value_const)
   if (g.dim == 1) GDT_LAUNCH_ASM(1, false);
   else if (g.dim == 2 && !g.simplex) GDT_LAUNCH_ASM(2, false);
   else if (g.dim == 2) GDT_LAUNCH_ASM(2, true);
@@ -290,7 +315,7 @@ gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& sp, const gdt_dif
   cudaStream_t s = ctx->stream;
 #define GDT_LAUNCH_RHS(D, S)                                                                                  \
   assemble_cg_rows<D, S><<<bl, th, 0, s>>>(g, nullptr, nullptr, rhs, tab, d->kappa, d->kappa_const, d->force, \
-                                           d->force_const, d->dirichlet)
+                                           d->force_const, d->dirichlet, nullptr, 0.0)
   if (g.dim == 1) GDT_LAUNCH_RHS(1, false);
   else if (g.dim == 2 && !g.simplex) GDT_LAUNCH_RHS(2, false);
   else if (g.dim == 2) GDT_LAUNCH_RHS(2, true);
@@ -300,14 +325,14 @@ gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& sp, const gdt_dif
   return check_launch(ctx, "assemble_cg_rhs");
 }
 
-gdt_status dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
+gdt_status dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs, const double* values, double value_const) {
   const GridDesc& g = m->test.g;
   const int th = 256;
   const int bl = grid_blocks(g.nvert, th);
   cudaStream_t s = ctx->stream;
-  if (g.dim == 1) dirichlet_rows<1><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs);
-  else if (g.dim == 2) dirichlet_rows<2><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs);
-  else dirichlet_rows<3><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs);
+  if (g.dim == 1) dirichlet_rows<1><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs, values, value_const);
+  else if (g.dim == 2) dirichlet_rows<2><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs, values, value_const);
+  else dirichlet_rows<3><<<bl, th, 0, s>>>(g, m->rp, m->col, m->val, rhs, values, value_const);
   return check_launch(ctx, "dirichlet_rows");
 }
 

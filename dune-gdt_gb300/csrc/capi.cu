@@ -339,6 +339,9 @@ gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_di
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
   m->val_version++;
   if (d->force_qp && d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
+  const bool values = d->dirichlet && (d->dirichlet_values || d->dirichlet_value_const != 0.0);
+  if (values && (m->test.order != 1 || d->kappa_qp || d->kappa_tensor || d->kappa_tensor_qp || d->force_qp))
+    return fail(ctx, GDT_EUNSUPPORTED, "Dirichlet values are lowered for the order-1 vertex-row assembly");
   // a source at quadrature points: the matrix first, then the load vector from its own pass
   double* rhs_fused = d->force_qp ? nullptr : rhs;
   if (d->kappa_tensor || d->kappa_tensor_qp) {
@@ -376,6 +379,16 @@ gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
   if (m->test.order == 2) return ho_dirichlet(ctx, m, rhs);
   m->mf_dirichlet = 1;
   return dirichlet_apply(ctx, m, rhs);
+}
+
+gdt_status gdt_dirichlet_apply_values(gdt_context ctx, gdt_matrix m, double* rhs, const double* values,
+                                      double value_const) {
+  if (!ctx || !m || !rhs) return GDT_EINVAL;
+  if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  if (m->test.order != 1) return fail(ctx, GDT_EUNSUPPORTED, "Dirichlet values are lowered for order 1");
+  m->val_version++;
+  m->mf_dirichlet = 1;
+  return dirichlet_apply(ctx, m, rhs, values, value_const);
 }
 
 gdt_status gdt_assemble_cg_product(gdt_context ctx, gdt_matrix m, const gdt_product_desc* d) {

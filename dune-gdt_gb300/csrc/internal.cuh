@@ -136,7 +136,8 @@ gdt_status build_pattern(gdt_context ctx, gdt_matrix m);
 // assemble_cg.cu
 gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs);
 gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& s, const gdt_diffusion_desc* d, double* rhs);
-gdt_status dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs);
+gdt_status dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs, const double* values = nullptr,
+                           double value_const = 0.0);
 gdt_status cg_dlogkappa(gdt_context ctx, const gdt_space_s& s, const double* kappa, const double* u,
                         const double* lam, double* out);
 // assemble_ipdg.cu

@@ -204,6 +204,11 @@ typedef struct gdt_diffusion_desc {
                                   * with a tensor; the element-batched path, any order */
   const double* kappa_tensor_qp; /* device, the same at the points of gdt_space_quadrature
                                   * ([element][q][d][d]), or NULL */
+  const double* dirichlet_values; /* device, Dirichlet values per DoF (read on the boundary DoFs), or NULL */
+  double dirichlet_value_const;   /* the value where dirichlet_values is NULL (0: homogeneous, the
+                                   * reference's DirichletConstraints). Non-zero data (order 1): the
+                                   * zeroed columns move to the right-hand side (b_i -= A_ij g_j), then
+                                   * unit rows and columns with b_D = g_D */
 } gdt_diffusion_desc;
 
 /* continuous Lagrange: stiffness of LocalLaplaceIntegrand(kappa) into m, and (if rhs != NULL) the
@@ -219,6 +224,11 @@ gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space cg, const gdt_diffusio
 /* DirichletConstraints::apply(M, V) (tools/dirichlet-constraints.hh:153-184) on an assembled
  * matrix of a continuous space, all-Dirichlet boundary: unit_col + unit_row, rhs[D] = 0 (rhs may be NULL). */
 gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs);
+/* the same with Dirichlet values (continuous order 1): b_i -= A_ij g_j over the boundary columns j of the
+ * other rows, then unit rows and columns and b_D = g_D; values: device per DoF, or NULL for value_const.
+ * No counterpart in the reference, whose constraints are homogeneous (the lifting a caller would do). */
+gdt_status gdt_dirichlet_apply_values(gdt_context ctx, gdt_matrix m, double* rhs, const double* values,
+                                      double value_const);
 
 /* LocalElementIntegralBilinearForm(LocalElementProductIntegrand(weight))
  * (local/bilinear-forms/integrals.hh:97-134, local/integrands/product.hh:89-130): the weighted

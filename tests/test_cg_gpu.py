@@ -438,3 +438,56 @@ def test_shape_errors_are_status_codes(gdt):
     with pytest.raises(gdt.GdtError) as e:
         gdt.MatrixOperator(g, gdt.ContinuousLagrangeSpace(g, 1), stencil=gdt.Stencil.element_and_intersection)
     assert e.value.status == gdt._capi.EUNSUPPORTED
+
+
+def _lifted(A, b, dofs, gvals):
+    # the Dirichlet-constrained system with values g on the boundary DoFs: b -= A[:, D] g_D on the other
+    # rows, then unit rows and columns and b_D = g_D
+    import scipy.sparse as sp
+
+    S = A.to_scipy().tolil()
+    n = S.shape[0]
+    gfull = np.zeros(n)
+    gfull[dofs] = gvals[dofs]
+    mask = np.zeros(n, bool)
+    mask[dofs] = True
+    bb = b - S.tocsr() @ gfull
+    bb[mask] = gvals[mask]
+    S = S.tocsr()
+    keep = sp.diags((~mask).astype(float))
+    S = keep @ S @ keep + sp.diags(mask.astype(float))
+    return S.tocsr(), bb
+
+
+@pytest.mark.parametrize("dim,n,simplex", [(2, [7, 6], True), (2, [6, 5], False), (3, [4, 3, 5], False),
+                                           (3, [3, 3, 2], True)])
+@pytest.mark.parametrize("fused", [True, False])
+def test_dirichlet_values_match_lifted_oracle_system(gdt, oracle, dim, n, simplex, fused):
+    g, og = _grid(gdt, oracle, dim, n, simplex)
+    rng = np.random.default_rng(23)
+    kappa = np.exp(rng.standard_normal(g.num_elements))
+    A, b = oracle.assemble_cg(og, 1, kappa=kappa, force_const=1.0, dirichlet=False)
+    space = gdt.ContinuousLagrangeSpace(g, 1)
+    gvals = rng.uniform(-1, 1, space.num_DoFs)
+    dofs = oracle.dirichlet_dofs(og, 1)
+    S, bb = _lifted(A, b, dofs, gvals)
+    op = gdt.MatrixOperator(g, space)
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(torch.tensor(kappa, device="cuda")))
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    gt = torch.tensor(gvals, device="cuda")
+    if fused:
+        op.assemble(rhs=rhs, force=1.0, dirichlet=True, dirichlet_values=gt)
+    else:
+        op.assemble(rhs=rhs, force=1.0)
+        gdt.DirichletConstraints("dirichlet", space).apply(op, rhs, values=gt)
+    rp, col, val = (t.cpu().numpy() for t in op.csr())
+    import scipy.sparse as sp
+
+    G = sp.csr_matrix((val, col, rp), shape=S.shape)
+    assert abs(G - S).max() <= 1e-12 * abs(S).max()
+    assert rel_err(rhs.cpu().numpy(), bb) < 1e-12
+    for precision in ("fp64", "mixed"):
+        x = op.apply_inverse(rhs, opts={"tol": 1e-12, "precision": precision})
+        xd = spl.spsolve(S.tocsc(), bb)
+        assert rel_err(x.cpu().numpy(), xd) < 1e-10
+        assert np.abs(x.cpu().numpy()[dofs] - gvals[dofs]).max() < 1e-12

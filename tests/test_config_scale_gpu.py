@@ -2,7 +2,8 @@
 
 * 3D heat equation, 128^3 Q1 hexahedra (2,146,689 DoF, 57,066,625 nonzeros), lognormal kappa per cell:
   pattern bit-exact, matrix and right-hand side within 1e-12, the FP64 solution at a 1e-14 residual and
-  the mixed-precision one at 1e-13 within 1e-12 of the oracle's CG at 1e-14;
+  the mixed-precision one at 1e-12 (its FP32 Krylov sequence stalls below that) within 1e-12 of the
+  oracle's CG at 1e-14;
 * SWIPDG P1 on 256^2 squares split into triangles (393,216 DoF) with the high-contrast channels of the
   adjoint workload: pattern bit-exact, matrix and right-hand side within 1e-12, solution within 1e-9
   of the oracle's: both CG solves stop at a 1e-14 residual, and the channels' 1e4 contrast on top of
@@ -44,7 +45,7 @@ def test_heat3d_128_matches_oracle(gdt, oracle):
     assert rel_err(rhs.cpu().numpy(), b) < 1e-12
     del rp, col, val
     xo, _, _, _ = oracle.solve(A, b, tol=1e-14, max_iter=400000)
-    for precision, tol in (("fp64", 1e-14), ("mixed", 1e-13)):
+    for precision, tol in (("fp64", 1e-14), ("mixed", 1e-12)):
         x = op.apply_inverse(rhs, opts={"tol": tol, "precision": precision, "max_iter": 400000})
         assert op.last_solve_info["converged"]
         assert rel_err(x.cpu().numpy(), xo) < 1e-12, precision
