@@ -492,6 +492,72 @@ __global__ void __launch_bounds__(TH) k_mf3_true_residual(int n, Mf3 g, const in
   }
 }
 
+// the same two FP64 residual kernels on the SELL-32 copy of the matrix (where the SpMV schedule
+// tuner picked it: one lane per row, coalesced entry loads)
+__global__ void __launch_bounds__(TH) k_mf3_init_sell(SellView A, Mf3 g, const double* __restrict__ x,
+                                                     const double* __restrict__ b, float* __restrict__ r32,
+                                                     const float* __restrict__ dm, float* __restrict__ zb, MfState* st,
+                                                     double* partials, unsigned int* ticket) {
+  double a1 = 0.0;
+  for_slices(A, x, [&](int row, bool active, double s, double) {
+    if (active) {
+      const double ri = b[row] - s;
+      const float rf = float(ri);
+      const long long ip = g.vidx(row);
+      r32[ip] = rf;
+      zb[ip] = dm[ip] * rf;
+      a1 = fma(ri, ri, a1);
+    }
+  });
+  double v[1] = {a1};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    st->rr = st->rr0 = st->rr_ref = v[0];
+    st->drop = 0.01;
+    st->restarting = 0;
+    st->replaced_iter = -1;
+    st->iter = 0;
+    st->flag = 0;
+    st->updates = 0;
+    st->breakdown = 0;
+    st->converged = (v[0] == 0.0) ? 1 : 0;
+  }
+}
+
+__global__ void __launch_bounds__(TH) k_mf3_true_residual_sell(SellView A, Mf3 g, const double* __restrict__ x,
+                                                              const double* __restrict__ b, float* __restrict__ r32,
+                                                              const float* __restrict__ dm, float* __restrict__ zb,
+                                                              MfState* st, double* partials, unsigned int* ticket) {
+  if (mf_stopped(st) || !entry_flag(&st->flag)) return;
+  double a1 = 0.0;
+  for_slices(A, x, [&](int row, bool active, double s, double) {
+    if (active) {
+      const double ri = b[row] - s;
+      const float rf = float(ri);
+      const long long ip = g.vidx(row);
+      r32[ip] = rf;
+      zb[ip] = dm[ip] * rf;
+      a1 = fma(ri, ri, a1);
+    }
+  });
+  double v[1] = {a1};
+  if (grid_reduce<1>(v, partials, ticket) && threadIdx.x == 0) {
+    if (!st->restarting && v[0] > 0.25 * st->rr_ref) {
+      st->restarting = 1;
+      st->drop = 1e-6;
+    }
+    st->rr_ref = v[0];
+    st->rr = v[0];
+    st->flag = 0;
+    st->updates += 1;
+    st->replaced_iter = st->iter;
+    if (v[0] <= st->tol2 * st->rr0 || st->iter >= st->max_iter) st->converged = 1;
+    if (!isfinite(v[0])) {
+      st->breakdown = 1;
+      st->converged = 1;
+    }
+  }
+}
+
 // K_ref[i][j] = f[i ^ j] within FP32 rounding (axis-aligned boxes); false otherwise
 bool xor_structure(const float* K, float* f) {
   float mx = 0.f;
@@ -614,10 +680,16 @@ gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double
     if (!(ey > 0.f) || !std::isfinite(ed) || ed > 1e-4f * ey) return GDT_EUNSUPPORTED;
     for (float* v : {r32, zb, w}) GDT_TRY_CUDA(ctx, cudaMemsetAsync(v, 0, vb, s));
   }
+  // the FP64 residuals read the SELL-32 copy where the tuner chose it for this matrix (the copy is
+  // refreshed here: the caller may have written the CSR values)
+  const bool sell = m->use_sell && sell_prepare(ctx, m, s, true) == GDT_OK;
+  const SellView SA = sell ? sell_view(m) : SellView{};
+  const int sblocks = sell ? sell_blocks(SA.nslices, ctx->num_sms) : 0;
 #define GDT_MF3_INIT(GG, PP)                                                                                     \
   k_mf3_init<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, x, b, r32, dm, zb, st, \
                                                             partials, ticket)
-  GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_INIT)
+  if (sell) k_mf3_init_sell<<<sblocks, TH, 0, s>>>(SA, g, x, b, r32, dm, zb, st, partials, ticket);
+  else GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_INIT)
 #undef GDT_MF3_INIT
   ctx->launches++;
   m->mx_operator = GDT_MIXED_OPERATOR_MATRIX_FREE;
@@ -657,7 +729,8 @@ gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double
 #define GDT_MF3_TRUE_RESIDUAL(GG, PP)                                                                            \
   k_mf3_true_residual<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, x, b, r32, dm, \
                                                                      zb, st, partials, ticket)
-    GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_TRUE_RESIDUAL)
+    if (sell) k_mf3_true_residual_sell<<<sblocks, TH, 0, s>>>(SA, g, x, b, r32, dm, zb, st, partials, ticket);
+    else GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_TRUE_RESIDUAL)
 #undef GDT_MF3_TRUE_RESIDUAL
     timing_end(ctx, s);
     ctx->launches += 2;

@@ -627,11 +627,16 @@ void scatter(orc_csr* m, const int64_t* ri, const int64_t* ci, int n, const doub
     for (int j = 0; j < n; ++j) m->val[m->slot(ri[i], ci[j])] += A[i * n + j];
 }
 
+// element colours for the threaded walks: elements of one colour share no DoF. Cubes of equal index
+// parity are two cells apart; the d! simplices of one cube share its vertices, so the simplex type is
+// part of the colour.
 long colour_of(const Grid& g, long e) {
   long ci[3];
   g.cell_multi(e / g.nsub, ci);
-  return (ci[0] & 1) | ((ci[1] & 1) << 1) | ((ci[2] & 1) << 2);
+  const long par = (ci[0] & 1) | ((ci[1] & 1) << 1) | ((ci[2] & 1) << 2);
+  return par * g.nsub + e % g.nsub;
 }
+int num_colours(const Grid& g) { return (1 << g.dim) * g.nsub; }
 
 // all-Dirichlet boundary DoFs (DirichletConstraints::apply_local, tools/dirichlet-constraints.hh:85-110):
 // the DoFs attached to subentities of boundary faces, i.e. nodes on the domain boundary.
@@ -751,7 +756,7 @@ extern "C" orc_csr* orc_assemble_cg(const orc_grid* gd, int order, const double*
   if (rhs) std::fill(rhs, rhs + s.size, 0.0);
   int n = s.lsize;
   set_threads();
-  int ncol = g_threads > 1 ? (1 << g.dim) : 1;
+  int ncol = g_threads > 1 ? num_colours(g) : 1;
   // grid walk (MatrixOperator + VectorBasedFunctional as walker functors); with threads the cells
   // are coloured by index parity so that concurrently processed elements share no DoF.
   for (int colour = 0; colour < ncol; ++colour) {
@@ -787,7 +792,7 @@ extern "C" orc_csr* orc_assemble_cg_tensor(const orc_grid* gd, int order, const 
   if (rhs) std::fill(rhs, rhs + s.size, 0.0);
   int n = s.lsize;
   set_threads();
-  int ncol = g_threads > 1 ? (1 << g.dim) : 1;
+  int ncol = g_threads > 1 ? num_colours(g) : 1;
   for (int colour = 0; colour < ncol; ++colour) {
 #pragma omp parallel for schedule(static) if (g_threads > 1)
     for (long e = 0; e < g.nelem; ++e) {

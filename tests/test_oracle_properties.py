@@ -129,3 +129,22 @@ def test_tensor_diffusion_restatement_reduces_to_scalar(oracle, dim, n, simplex,
     M2, _ = oracle.assemble_cg_tensor(og, order, np.transpose(K, (0, 2, 1)), dirichlet=False)
     S1, S2 = M1.to_scipy(), M2.to_scipy()
     assert abs(S1 - S2.T).max() <= 1e-13 * abs(S1).max()
+
+
+@pytest.mark.parametrize("dim,n,order", [(2, [5, 4], 1), (2, [4, 3], 2), (3, [3, 2, 3], 1), (3, [2, 2, 2], 2)])
+def test_threaded_walk_equals_serial_on_simplices(oracle, dim, n, order):
+    # the threaded grid walk colours elements so that no two of one colour share a DoF: with the d!
+    # simplices of a cube in different colours its results are those of the serial walk
+    og = oracle.grid(dim, n, 0.0, 1.0, simplex=True)
+    ne = oracle.num_elements(og)
+    rng = np.random.default_rng(7)
+    kappa, force = np.exp(rng.standard_normal(ne)), rng.uniform(-1, 1, ne)
+    try:
+        oracle.set_threads(1)
+        A1, b1 = oracle.assemble_cg(og, order, kappa=kappa, force=force)
+        oracle.set_threads(8)
+        A8, b8 = oracle.assemble_cg(og, order, kappa=kappa, force=force)
+    finally:
+        oracle.set_threads(1)
+    assert np.abs(A1.val - A8.val).max() <= 1e-14 * np.abs(A1.val).max()
+    assert np.abs(b1 - b8).max() <= 1e-14 * np.abs(b1).max()
