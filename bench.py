@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--n", type=int, default=128, help="cells per axis")
     p.add_argument("--tol", type=float, default=1e-11, help="relative residual stop of both solvers")
     p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU legs (baseline and parity)")
+    p.add_argument("--spmv-schedule", default="auto", choices=["auto"] + SCHEDULE_NAMES,
+                   help="heat3d: pin the FP64 SpMV schedule instead of the autotuner's choice (for profiling)")
     p.add_argument("--headline-only", action="store_true", help="default config without the extra metric keys")
     p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg", "q2", "peaks"],
                    help="heat3d: the headline 128^3 workload (with the other metric keys); batched: 512 "
@@ -252,6 +254,9 @@ def run_gdt(args):
     sched = C.c_int()
     sched_ms = (C.c_double * len(SCHEDULE_NAMES))()
     ctx.call("gdt_matrix_tune", op.handle, C.byref(sched), sched_ms)
+    if args.spmv_schedule != "auto":
+        sched.value = SCHEDULE_NAMES.index(args.spmv_schedule)
+        op.set_spmv_schedule(sched.value)
     # FP64 reference solution at a tight tolerance (untimed) for the error statement
     u_tight = op.apply_inverse(rhs, opts={"tol": 1e-14, "max_iter": 200000}).clone()
 

@@ -517,7 +517,8 @@ struct Launch {
 void spmv_cg_sell(const Launch& L, gdt_matrix m, const double* p, double* q, KState* st) {
   const SellView A = sell_view(m);
   timing_begin(L.ctx, L.s, GDT_TIMING_SPMV_FP64);
-  k_sell_spmv_cg<<<sell_blocks(A.nslices, L.ctx->num_sms), 256, 0, L.s>>>(A, p, q, st, L.partials, L.ticket);
+  k_sell_spmv_cg<<<sell_blocks(A.nslices, L.ctx->num_sms, reinterpret_cast<const void*>(&k_sell_spmv_cg)), 256, 0,
+                   L.s>>>(A, p, q, st, L.partials, L.ticket);
   timing_end(L.ctx, L.s);
   L.ctx->launches++;
 }
@@ -747,7 +748,7 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
     block_reduce<1>(v1, red);
     if (threadIdx.x == 0) a.part[blockIdx.x] = v1[0];
     if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
-    grid_allreduce<1>(a.part, v1, red, bc);
+    grid_allreduce<1>(a.part, v1, bc);
     alpha = rho / v1[0];
     if (!(v1[0] > 0.0) || !isfinite(v1[0])) {
       brk = conv = 1;
@@ -788,7 +789,7 @@ __global__ void __launch_bounds__(PT, 1) k_pcg_persistent(PcgArgs a) {
       a.part[2 * nb + blockIdx.x] = v2[1];
     }
     if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
-    grid_allreduce<2>(a.part + nb, v2, red, bc);
+    grid_allreduce<2>(a.part + nb, v2, bc);
     beta = v2[0] / rho;
     rho = v2[0];
     rr = v2[1];

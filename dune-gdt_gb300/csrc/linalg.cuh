@@ -256,10 +256,10 @@ __device__ __forceinline__ void for_slices(const SellView& A, const double* __re
   }
 }
 
-// the SELL-32 copy of m (spmv.cu; sell_prepare must have succeeded) and the grid of its SpMV kernels
-// (blocks of 256 threads, one resident wave)
+// the SELL-32 copy of m (spmv.cu; sell_prepare must have succeeded) and the grid of a SELL kernel
+// (blocks of 256 threads, one resident wave of that kernel)
 SellView sell_view(gdt_matrix m);
-int sell_blocks(long long nslices, int num_sms);
+int sell_blocks(long long nslices, int num_sms, const void* kernel);
 
 // SpMV schedules: PL == 0 -> vector-CSR with G lanes per row; PL > 0 -> pipelined warp staging with
 // PL entries per lane; PL < 0 -> asynchronous double-buffered staging for rows of at most -PL
@@ -583,23 +583,55 @@ __device__ inline bool grid_barrier(unsigned int* bar, unsigned int& epoch, unsi
   return ok != 0;
 }
 
-// sum of the per-block partials part[k * gridDim.x + b] in block order, the same in every block;
-// result in every thread. red: NV * 32 doubles of shared memory, bc: NV.
+// Sum of the per-block partials part[k * gridDim.x + b], the same bits in every block (a fixed order:
+// lane-strided sums, then a shuffle tree); result in every thread. Warp 0 alone does the FP64 adds:
+// this part issues one FP64 warp instruction per 16 SM cycles, so a block-wide FP64 tree over every
+// warp of a large block would put microseconds on the critical path of each solver iteration.
+// bc: NV doubles of shared memory.
 template <int NV>
-__device__ __forceinline__ void grid_allreduce(const double* part, double (&v)[NV], double* red, double* bc) {
+__device__ __forceinline__ void grid_allreduce(const double* part, double (&v)[NV], double* bc) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double s = 0.0;
-    for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += part[k * gridDim.x + b];
-    v[k] = s;
+    for (int k = 0; k < NV; ++k) {
+      double s = 0.0;
+      for (int b = lane; b < gridDim.x; b += 32) s += part[k * gridDim.x + b];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) bc[k] = s;
+    }
   }
-  block_reduce<NV>(v, red);
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int k = 0; k < NV; ++k) bc[k] = v[k];
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < NV; ++k) v[k] = bc[k];
+}
+
+// Block reduction of NV per-thread FP32 sums: FP32 shuffles inside each warp, the warps' sums added in
+// FP64 by warp 0 (the FP64 tree of block_reduce costs 16 SM cycles per warp instruction here). The
+// warp stage adds 32 FP32 values, a relative error of a few 1e-7, the precision of the FP32 vectors the
+// sums come from. Result valid in thread 0. smem: NV * 32 doubles.
+template <int NV>
+__device__ inline void block_reduce_f32(float (&v)[NV], double (&out)[NV], double* smem) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = double(v[k]);
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = lane < nw ? smem[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      out[k] = s;
+    }
+  }
+  __syncthreads();
 }
 
 }  // namespace gdt

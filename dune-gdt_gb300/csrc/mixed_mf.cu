@@ -204,6 +204,7 @@ struct MfPArgs {
 // registers go to the operator's planes.
 struct MfScalars {
   double alpha, beta, gamma, gamma_prev, alpha_prev, rr;
+  float af, bf;  // alpha and beta as the update pass uses them (one conversion, by thread 0)
   int iter, done, flag, brk;
 };
 
@@ -222,6 +223,8 @@ __global__ void __launch_bounds__(MT, 1) k_mf3_persistent(MfPArgs a) {
     sc.alpha_prev = st->alpha_prev;
     sc.rr = st->rr;
     sc.iter = st->iter;
+    sc.af = float(sc.alpha);
+    sc.bf = float(sc.beta);
     sc.done = sc.flag = sc.brk = 0;
   }
   __syncthreads();
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(MT, 1) k_mf3_persistent(MfPArgs a) {
     if (pass == MF3_CONTINUE) {
       // p = z + beta p, s = w + beta s, x32 += alpha p, r -= alpha s, zb = D_m r (z = D r: D_m, or 1 where
       // D_m is 0 on a Dirichlet row; 0 in the padding, where r is 0)
-      const float af = float(sc.alpha), bf = float(sc.beta);
+      const float af = sc.af, bf = sc.bf;
       float4* p4 = reinterpret_cast<float4*>(a.p);
       float4* s4 = reinterpret_cast<float4*>(a.s);
       float4* x4 = reinterpret_cast<float4*>(a.x32);
@@ -271,15 +274,16 @@ __global__ void __launch_bounds__(MT, 1) k_mf3_persistent(MfPArgs a) {
     // w = A zb and the three dots
     float gs = 0.f, ds = 0.f, rs = 0.f;
     mf3_apply_items<DIR>(a.g, a.kap, a.zb, a.r, a.w, gs, ds, rs);
-    double v[3] = {double(gs), double(ds), double(rs)};
-    block_reduce<3>(v, red);
+    float vf[3] = {gs, ds, rs};
+    double v[3];
+    block_reduce_f32<3>(vf, v, red);
     if (threadIdx.x == 0) {
       a.part[blockIdx.x] = v[0];
       a.part[gridDim.x + blockIdx.x] = v[1];
       a.part[2 * gridDim.x + blockIdx.x] = v[2];
     }
     if (!grid_barrier(a.bar, epoch, a.wait_ns)) break;
-    grid_allreduce<3>(a.part, v, red, bc);
+    grid_allreduce<3>(a.part, v, bc);
     if (threadIdx.x == 0) {
       const double gam = v[0], del = v[1], rrn = v[2];
       if (pass == MF3_INIT) {
@@ -296,6 +300,8 @@ __global__ void __launch_bounds__(MT, 1) k_mf3_persistent(MfPArgs a) {
         sc.alpha = gam / (del - sc.beta * gam / sc.alpha_prev);
       }
       sc.gamma = gam;
+      sc.af = float(sc.alpha);
+      sc.bf = float(sc.beta);
       if (!(del > 0.0) || !isfinite(sc.alpha) || !isfinite(rrn)) {
         sc.brk = 1;
         sc.done = 1;
@@ -684,11 +690,14 @@ gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double
   // refreshed here: the caller may have written the CSR values)
   const bool sell = m->use_sell && sell_prepare(ctx, m, s, true) == GDT_OK;
   const SellView SA = sell ? sell_view(m) : SellView{};
-  const int sblocks = sell ? sell_blocks(SA.nslices, ctx->num_sms) : 0;
+  const int sblocks_init =
+      sell ? sell_blocks(SA.nslices, ctx->num_sms, reinterpret_cast<const void*>(&k_mf3_init_sell)) : 0;
+  const int sblocks =
+      sell ? sell_blocks(SA.nslices, ctx->num_sms, reinterpret_cast<const void*>(&k_mf3_true_residual_sell)) : 0;
 #define GDT_MF3_INIT(GG, PP)                                                                                     \
   k_mf3_init<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, x, b, r32, dm, zb, st, \
                                                             partials, ticket)
-  if (sell) k_mf3_init_sell<<<sblocks, TH, 0, s>>>(SA, g, x, b, r32, dm, zb, st, partials, ticket);
+  if (sell) k_mf3_init_sell<<<sblocks_init, TH, 0, s>>>(SA, g, x, b, r32, dm, zb, st, partials, ticket);
   else GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_INIT)
 #undef GDT_MF3_INIT
   ctx->launches++;

@@ -10,6 +10,7 @@
 // mixed-precision residual); when the SELL-32 schedule is faster still, the plain SpMV and the
 // graph-form CG SpMV read the SELL copy instead.
 #include <cfloat>
+#include <mutex>
 #include <vector>
 
 #include "linalg.cuh"
@@ -143,14 +144,23 @@ __global__ void __launch_bounds__(256) sell_spmv_kernel(SellView A, const double
   });
 }
 
-// one warp per slice in blocks of 8 warps, no more blocks than are resident at once
-int sell_blocks(long long nslices, int num_sms) {
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, sell_spmv_kernel, 256, 0) != cudaSuccess || b < 1) b = 4;
-    cudaGetLastError();
-    per_sm = b;
+// one warp per slice in blocks of 8 warps (256 threads), no more blocks than `kernel` keeps resident at
+// once (its own occupancy: the fused solver kernels hold more registers than the plain SpMV, and a
+// grid sized for the plain one would run a second, partial wave)
+int sell_blocks(long long nslices, int num_sms, const void* kernel) {
+  static std::mutex lock;
+  static std::vector<std::pair<const void*, int>> known;  // (kernel, resident 256-thread blocks per SM)
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> g(lock);
+    for (const auto& k : known)
+      if (k.first == kernel) per_sm = k.second;
+    if (per_sm == 0) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+      cudaGetLastError();
+      known.emplace_back(kernel, per_sm);
+    }
   }
   const long long want = (nslices + 7) / 8;
   return int(std::max(1LL, std::min<long long>(want, (long long)num_sms * per_sm)));
@@ -158,7 +168,8 @@ int sell_blocks(long long nslices, int num_sms) {
 
 void launch_sell_spmv(gdt_matrix m, const double* x, double* y, int num_sms, cudaStream_t s) {
   const SellView A = sell_view(m);
-  sell_spmv_kernel<<<sell_blocks(A.nslices, num_sms), 256, 0, s>>>(A, x, y);
+  sell_spmv_kernel<<<sell_blocks(A.nslices, num_sms, reinterpret_cast<const void*>(&sell_spmv_kernel)), 256, 0, s>>>(
+      A, x, y);
 }
 
 // probe vector of the autotuner: non-trivial values (an all-zero x would time the FMAs on zero operands)
