@@ -93,6 +93,17 @@ def hbm_peak():
     return 6800.0, "fallback 6.8 TB/s (of fallback)"
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the dominant kernels of
+# the 128^3 workload, from single-pass ncu captures:
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none \
+#       -k regex:k_mf3_persistent -c 60 python bench.py --headline-only --no-cpu-baseline --steps 1 --warmup 0
+#   (mean of the 11 launches of one solve: 76.3 MB read + 67.6 MB written)
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:sell_spmv_kernel -s 3 -c 1 \
+#       python bench.py --headline-only --no-cpu-baseline --steps 1 --warmup 0 --spmv-schedule sell32
+MIXED_TRAFFIC_PER_LAUNCH_128 = 143.9e6
+SELL_TRAFFIC_PER_SPMV_128 = 706.5e6 + 4.1e6
+
+
 def heat3d_config(n, ndof, nnz, tol, world, precision):
     """The workload of both arms (identical apart from the precision of the GPU arm's `value`)."""
     return {"workload": f"3D heat equation, {n}^3 Q1 hexes, lognormal kappa, f=1, Dirichlet 0; "
@@ -395,6 +406,7 @@ def run_gdt(args):
                          "how": "the FP64 CG's SpMV launches of one graph-form solve in timing mode (CUDA events "
                                 "around each launch; the update and direction kernels run between them)"},
         "peak": hbm, "peak_source": hbm_src, "target_frac": 0.7,
+        "traffic_sell32": SELL_TRAFFIC_PER_SPMV_128 if n == 128 else None,
         "autotuner_ms_per_launch": {name: round(sched_ms[k], 4) for k, name in enumerate(SCHEDULE_NAMES)
                                     if sched_ms[k] > 0},
     }
@@ -429,7 +441,10 @@ def run_gdt(args):
                      "achieved": by_kernel[dom]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": by_kernel[dom]["frac"], "bytes_per_launch": by_kernel[dom]["bytes_per_launch"],
                      "avg_launch_ms": by_kernel[dom]["avg_launch_ms"], "launches": by_kernel[dom]["launches"],
-                     "peak_source": hbm_src, "traffic": None,
+                     "peak_source": hbm_src,
+                     "traffic": (MIXED_TRAFFIC_PER_LAUNCH_128 if n == 128 and dom == "mixed_persistent" else None),
+                     "traffic_note": "DRAM read + write per launch from one ncu capture (caches flushed before each "
+                                     "launch), mean of the 11 launches of one solve at 128^3",
                      "note": ("the inner iteration's working set (FP32 vectors and coefficients, ~70 MB) stays in "
                               "the 129 MB L2, so the achieved rate is measured against HBM but served mostly from "
                               "L2") if inner == "matrix_free" else None},
@@ -487,7 +502,18 @@ def batched_metrics(args, gdt, cpu=True, world=1, steps=None, warmup=None):
             e = max(e, ((b.unpack(xx, i) - r).abs().max() / r.abs().max()).item())
         return e
 
+    tuning = {}
+
     def timed(precision):
+        # the autotuner (untimed): team kind per size class for this precision
+        t_tune = time.perf_counter()
+        times = b.tune(mu_t, precision=precision, tol=args.tol, max_iter=200000)
+        teams = b.teams()
+        tuning[precision] = {"ms_per_class_and_team": {str(k): {t: round(v, 3) for t, v in d.items()}
+                                                       for k, d in times.items()},
+                             "chosen": {str(int(c)): teams[int(np.nonzero(sides == c)[0][0])]
+                                        for c in sorted(set(sides.tolist()))},
+                             "tuner_s": round(time.perf_counter() - t_tune, 2)}
         for _ in range(warmup):
             b.solve(mu_t, precision=precision, tol=args.tol, x=x, max_iter=200000)
         torch.cuda.synchronize()
@@ -538,6 +564,8 @@ def batched_metrics(args, gdt, cpu=True, world=1, steps=None, warmup=None):
                    "dofs": ndof, "tol_rel_residual": args.tol,
                    "l2_flush": "not needed: each launch solves all 512 problems from their assembly (44.8 M DoF "
                                "of FP64 vectors, ~2.5 GB of solver state) well past the 129 MB L2"},
+        "autotuner": tuning,
+        "iterations_mean": {"mixed": float(np.mean(np.abs(its_mixed))), "fp64": float(np.mean(np.abs(its_fp64)))},
         "batched_mixed": {"ms": ms_mixed, "error_vs_fp64_reference": err_mixed, **info_mixed},
         "batched_fp64": {"ms": ms_fp64, "value": world * ndof / (ms_fp64 / 1e3), "error_vs_fp64_reference": err_fp64,
                          **info_fp64},
@@ -615,11 +643,19 @@ def bumps(n, seed, count=32):
     return u.reshape(-1)
 
 
-# FP64 operations of one cell and SSP-RK2 stage of the LF Burgers flux, counted on the formula: per
-# face (two faces computed per cell) u^2 + v^2 (2), the LF term max(|u|,|v|) (u - v) (2) and their
-# sum (1); per cell the divergence of the two directions' face differences (3) and the stage update
-# (2 for stage 1, 3 for stage 2)
-FV_OPS_PER_CELL_STEP = 2 * (5 + 3) + 2 + 3
+# FP64 instructions executed per cell and SSP-RK2 step of the LF Burgers stage kernels, from ncu's
+# InstructionStats (fused + non-fused FP64 warp instructions x 32 / cells) on 2048^2 periodic cells:
+#   ncu --section InstructionStats --clock-control none -k regex:fv2d_tile -s 4 -c 2 \
+#       python bench.py --config fv --fv-n 2048 --fv-steps 2 --steps 1 --warmup 0 --no-cpu-baseline
+# stage 1: (401,408 + 954,368) x 32 / 4,194,304 = 10.34; stage 2: (684,032 + 1,085,440) x 32 / 4,194,304 = 13.50
+FV_FP64_INSTR_PER_CELL_STEP = 10.344 + 13.500
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one SSP-RK2 step of the stage kernels
+# on the bench's 4096^2 state (one pass per launch, both stages of one step):
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:fv2d_tile -s 4 -c 2 \
+#       python bench.py --config fv --fv-n 4096 --fv-steps 2 --steps 1 --warmup 0 --no-cpu-baseline
+# (stage 1: 134.3 MB read + 92.5 MB written; stage 2: 268.6 + 106.3 MB)
+FV_TRAFFIC_PER_STEP_4096 = 601.7e6
 
 
 def fv_metrics(args, gdt, n, nb, cpu=True, world=1, steps=None, warmup=None):
@@ -657,7 +693,7 @@ def fv_metrics(args, gdt, n, nb, cpu=True, world=1, steps=None, warmup=None):
     hbm, hbm_src = hbm_peak()
     fma_tf, dmma_tf = fp64_peak(gdt)
     bytes_step = 40 * cells  # fused SSP-RK2: read u twice and k0, write k0 and the next state
-    fp64_ops = FV_OPS_PER_CELL_STEP * cells / per_step_s
+    fp64_instr = FV_FP64_INSTR_PER_CELL_STEP * cells / per_step_s  # FP64 instructions per second
     out = {
         "metric": "FV cell-updates/s (2D Burgers, LF flux, SSP-RK2)", "value": world * cells / per_step_s,
         "unit": "cell-updates/s", "ms_per_step": t, "steps": steps, "warmup": warmup,
@@ -669,10 +705,16 @@ def fv_metrics(args, gdt, n, nb, cpu=True, world=1, steps=None, warmup=None):
         "roofline": {"bound": "fp64 pipe", "kernel": "fv2d_tile (fused SSP-RK2 stages)",
                      "achieved": bytes_step / per_step_s / 1e9, "peak": hbm, "unit": "GB/s",
                      "frac": bytes_step / per_step_s / 1e9 / hbm, "peak_source": hbm_src,
-                     "bytes_per_step": bytes_step, "traffic": None,
-                     "fp64": {"ops_per_cell_and_step": FV_OPS_PER_CELL_STEP, "achieved_tflops": fp64_ops / 1e12,
-                              "peak_tflops": fma_tf, "frac": fp64_ops / 1e12 / fma_tf if fma_tf else None,
-                              "peak_source": "gdt_measure_fp64_peak (FMA chains, this GPU, this run)"}},
+                     "bytes_per_step": bytes_step,
+                     "traffic": (FV_TRAFFIC_PER_STEP_4096 * cells / 4096 ** 2
+                                 if FV_TRAFFIC_PER_STEP_4096 and n == 4096 else None),
+                     "fp64": {"instructions_per_cell_update": FV_FP64_INSTR_PER_CELL_STEP,
+                              "achieved_instr_per_s": fp64_instr,
+                              "peak_instr_per_s": fma_tf * 1e12 / 2 if fma_tf else None,
+                              "frac": fp64_instr / (fma_tf * 1e12 / 2) if fma_tf else None,
+                              "peak_source": "gdt_measure_fp64_peak: FMA chains on this GPU in this run "
+                                             "(TFLOP/s / 2 = FP64 FMA instructions/s)",
+                              "instructions_source": "ncu InstructionStats, 2048^2, both stages"}},
         "clocks": clk,
     }
     if cpu:

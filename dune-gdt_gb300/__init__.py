@@ -1136,21 +1136,35 @@ def element_error(space, u, reference, norm="h1_semi", quad_order=None, ctx: Con
 
 # ---------------------------------------------------------------------------------- batched ---
 class BatchedDiffusion:
-    """Many parametric problems (-div(kappa_mu grad u) = f on the unit square, P1 on cells[i]^2 squares
-    split into triangles, kappa = mu[i, q] on quadrant q) assembled and solved in one persistent launch."""
+    """Many parametric problems -div(kappa grad u) = f on the unit square, one mesh of cells[i]^2
+    squares each (sizes may differ), assembled and solved in one persistent launch: continuous P1 on
+    the squares split into two triangles (element="p1", element e = 2 cell + t) or continuous Q1 on
+    the squares (element="q1", element e = cell), homogeneous Dirichlet. kappa per quadrant of the
+    2 x 2 split (`mu`, [n, 4]) or per element (`kappa`, concatenated at `element_offsets`).
+    Each problem is solved by a team of threads: the 8 CTAs of a cluster, one CTA or one warp;
+    `tune()` times the team kinds per size class and keeps the fastest (the autotuner),
+    `set_teams()` sets them by hand."""
 
-    def __init__(self, cells, ctx: Context | None = None):
+    TEAMS = {"cluster": capi.BATCH_TEAM_CLUSTER, "cta": capi.BATCH_TEAM_CTA, "warp": capi.BATCH_TEAM_WARP}
+
+    def __init__(self, cells, ctx: Context | None = None, element="p1"):
         self.ctx = ctx or default_context()
         self.cells = [int(c) for c in cells]
+        self.element = element
+        kind = {"p1": capi.BATCH_P1_SIMPLEX, "q1": capi.BATCH_Q1_CUBE}[element]
         arr = (C.c_int64 * len(self.cells))(*self.cells)
         h = C.c_void_p()
-        self.ctx.call("gdt_batch_create", C.c_int64(len(self.cells)), arr, C.byref(h))
+        self.ctx.call("gdt_batch_create_ex", C.c_int64(len(self.cells)), arr, kind, C.byref(h))
         self.handle = h
         L = capi.load()
         self.total_dofs = int(L.gdt_batch_total_dofs(h))
+        self.total_elements = int(L.gdt_batch_total_elements(h))
         off = (C.c_int64 * (len(self.cells) + 1))()
         capi.check(L.gdt_batch_dof_offsets(h, off))
         self.offsets = [int(v) for v in off]
+        capi.check(L.gdt_batch_element_offsets(h, off))
+        self.element_offsets = [int(v) for v in off]
+        self.stencil_width = 7 if element == "p1" else 9
 
     def __del__(self):
         try:
@@ -1159,19 +1173,69 @@ class BatchedDiffusion:
         except Exception:
             pass
 
-    def solve(self, mu, force=1.0, precision="fp64", tol=1e-10, max_iter=100000, x=None, keep_stencil=False,
-              wait=True):
-        mu = _f64(mu.contiguous().reshape(-1), 4 * len(self.cells), "mu")
+    def _kappa(self, mu, kappa):
+        if (mu is None) == (kappa is None):
+            raise ValueError("give exactly one of mu (per quadrant) and kappa (per element)")
+        if mu is not None:
+            return _f64(mu.contiguous().reshape(-1), 4 * len(self.cells), "mu"), capi.BATCH_KAPPA_QUADRANTS
+        return _f64(kappa.contiguous().reshape(-1), self.total_elements, "kappa"), capi.BATCH_KAPPA_ELEMENTS
+
+    def solve(self, mu=None, force=1.0, precision="fp64", tol=1e-10, max_iter=100000, x=None, keep_stencil=False,
+              wait=True, kappa=None):
+        """Assemble and solve every problem; raises GdtError(ENAN) when a problem has non-finite data
+        (that problem is skipped with x = 0, see status()) or GdtError(ENOCONV) when one did not
+        converge; the other problems are solved all the same."""
+        k, kind = self._kappa(mu, kappa)
         if x is None:
             x = torch.empty(self.total_dofs, dtype=torch.float64, device=self.ctx.device)
-        stencil = torch.empty(self.total_dofs * 7, dtype=torch.float64, device=self.ctx.device) if keep_stencil else None
+        stencil = (torch.empty(self.total_dofs * self.stencil_width, dtype=torch.float64, device=self.ctx.device)
+                   if keep_stencil else None)
         info = capi.BatchInfo()
         prec = {"fp64": capi.PRECISION_FP64, "mixed": capi.PRECISION_MIXED}[precision]
-        self.ctx.call("gdt_batch_solve", self.handle, _ptr(mu), C.c_double(force), prec, C.c_double(tol), int(max_iter),
-                      _ptr(_f64(x, self.total_dofs, "x")), _ptr(stencil), C.byref(info) if wait else None)
-        self.last_info = {"max_iterations": info.max_iterations, "min_iterations": info.min_iterations,
-                          "max_rel_residual": info.max_rel_residual, "all_converged": bool(info.all_converged)}
+        try:
+            self.ctx.call("gdt_batch_solve_ex", self.handle, _ptr(k), kind, C.c_double(force), prec, C.c_double(tol),
+                          int(max_iter), _ptr(_f64(x, self.total_dofs, "x")), _ptr(stencil),
+                          C.byref(info) if wait else None)
+        finally:  # filled also when some problem failed (the others are solved all the same)
+            self.last_info = {"max_iterations": info.max_iterations, "min_iterations": info.min_iterations,
+                              "max_rel_residual": info.max_rel_residual, "all_converged": bool(info.all_converged),
+                              "nonfinite_problems": info.nonfinite_problems}
         return (x, stencil) if keep_stencil else x
+
+    def tune(self, mu=None, force=1.0, precision="fp64", tol=1e-10, max_iter=100000, kappa=None):
+        """The autotuner: per size class, the batch solve of that class timed with every allowed team
+        kind; the fastest is kept. Returns {cells: {team: ms}} of the timings (teams not tried absent)."""
+        k, kind = self._kappa(mu, kappa)
+        n = len(self.cells)
+        x = torch.empty(self.total_dofs, dtype=torch.float64, device=self.ctx.device)
+        nsizes = C.c_int64()
+        sizes = (C.c_int64 * n)()
+        ms = (C.c_double * (3 * n))()
+        prec = {"fp64": capi.PRECISION_FP64, "mixed": capi.PRECISION_MIXED}[precision]
+        self.ctx.call("gdt_batch_tune", self.handle, _ptr(k), kind, C.c_double(force), prec, C.c_double(tol),
+                      int(max_iter), _ptr(x), C.byref(nsizes), sizes, ms)
+        names = {v: name for name, v in self.TEAMS.items()}
+        return {int(sizes[c]): {names[t]: ms[3 * c + t] for t in range(3) if ms[3 * c + t] >= 0}
+                for c in range(nsizes.value)}
+
+    def teams(self):
+        t = (C.c_int * len(self.cells))()
+        capi.check(capi.load().gdt_batch_teams(self.handle, t))
+        names = {v: name for name, v in self.TEAMS.items()}
+        return [names[v] for v in t]
+
+    def set_teams(self, teams):
+        """teams: one name ("cluster", "cta", "warp") for all, a list per problem, or {cells: name}."""
+        if isinstance(teams, str):
+            per = [teams] * len(self.cells)
+        elif isinstance(teams, dict):
+            cur = self.teams()
+            per = [teams.get(c, cur[i]) for i, c in enumerate(self.cells)]
+        else:
+            per = list(teams)
+        arr = (C.c_int * len(self.cells))(*[self.TEAMS[t] for t in per])
+        self.ctx.call("gdt_batch_set_teams", self.handle, arr)
+        return self
 
     def iterations(self):
         import numpy as np
@@ -1181,6 +1245,14 @@ class BatchedDiffusion:
         rr = (C.c_double * n)()
         self.ctx.call("gdt_batch_iterations", self.handle, it, rr)
         return np.array(it[:]), np.array(rr[:])
+
+    def status(self):
+        """per-problem status of the last solve: capi.OK, capi.ENOCONV or capi.ENAN"""
+        import numpy as np
+
+        st = (C.c_int * len(self.cells))()
+        self.ctx.call("gdt_batch_status", self.handle, st)
+        return np.array(st[:])
 
     def unpack(self, x, i):
         return x[self.offsets[i]:self.offsets[i + 1]]

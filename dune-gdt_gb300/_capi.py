@@ -27,6 +27,9 @@ FV_BOUNDARY_NONE, FV_BOUNDARY_EXTRAPOLATE, FV_BOUNDARY_DIRICHLET, FV_BOUNDARY_FL
 TIMESTEPPER_EXPLICIT_EULER, TIMESTEPPER_SSPRK2 = 0, 1
 MIXED_OPERATOR_STENCIL, MIXED_OPERATOR_STENCIL_TILED, MIXED_OPERATOR_MATRIX_FREE = 0, 1, 2
 SOLVER_LAUNCH_AUTO, SOLVER_LAUNCH_GRAPH, SOLVER_LAUNCH_PERSISTENT = 0, 1, 2
+BATCH_P1_SIMPLEX, BATCH_Q1_CUBE = 0, 1
+BATCH_KAPPA_QUADRANTS, BATCH_KAPPA_ELEMENTS = 0, 1
+BATCH_TEAM_CLUSTER, BATCH_TEAM_CTA, BATCH_TEAM_WARP = 0, 1, 2
 
 
 class DiffusionDesc(C.Structure):
@@ -75,7 +78,8 @@ class FvDesc(C.Structure):
 
 class BatchInfo(C.Structure):
     _fields_ = [("problems", C.c_int64), ("total_dofs", C.c_int64), ("max_iterations", C.c_int),
-                ("min_iterations", C.c_int), ("max_rel_residual", C.c_double), ("all_converged", C.c_int)]
+                ("min_iterations", C.c_int), ("max_rel_residual", C.c_double), ("all_converged", C.c_int),
+                ("nonfinite_problems", C.c_int64)]
 
 
 class GdtError(RuntimeError):
@@ -147,11 +151,20 @@ _SIGNATURES = {
     "gdt_fv_estimate_dt": (C.c_int, [P, P, C.POINTER(FvDesc), P, C.POINTER(C.c_double)]),
     "gdt_fv_timestep": (C.c_int, [P, P, C.POINTER(FvDesc), C.c_int, C.c_double, C.c_int64, C.c_int64, P, P]),
     "gdt_batch_create": (C.c_int, [P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(P)]),
+    "gdt_batch_create_ex": (C.c_int, [P, C.c_int64, C.POINTER(C.c_int64), C.c_int, C.POINTER(P)]),
     "gdt_batch_destroy": (C.c_int, [P]),
     "gdt_batch_total_dofs": (C.c_int64, [P]),
+    "gdt_batch_total_elements": (C.c_int64, [P]),
     "gdt_batch_dof_offsets": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "gdt_batch_element_offsets": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "gdt_batch_set_teams": (C.c_int, [P, P, C.POINTER(C.c_int)]),
+    "gdt_batch_teams": (C.c_int, [P, C.POINTER(C.c_int)]),
     "gdt_batch_solve": (C.c_int, [P, P, P, C.c_double, C.c_int, C.c_double, C.c_int, P, P, P]),
+    "gdt_batch_solve_ex": (C.c_int, [P, P, P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, P, P, P]),
+    "gdt_batch_tune": (C.c_int, [P, P, P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, P,
+                                 C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "gdt_batch_iterations": (C.c_int, [P, P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "gdt_batch_status": (C.c_int, [P, P, C.POINTER(C.c_int)]),
     "gdt_cg_dlogkappa": (C.c_int, [P, P, P, P, P, P]),
     "gdt_swipdg_dlogkappa": (C.c_int, [P, P, C.POINTER(IpdgDesc), P, P, P]),
 }

@@ -535,6 +535,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 // Grid barrier (all blocks are co-resident: cooperative launch). Barrier number `epoch` (counted by
 // thread 0 of every block) is complete when the 64-bit arrival count reaches epoch * blocks; the last
 // block to arrive publishes the epoch as the generation the others poll (no reset of the count, so
@@ -542,6 +544,12 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // first poll and every 256 polls) and by count, after which the fault flag is set and every block
 // returns false from then on. Data written before the barrier by any block is read after it with
 // plain (coherent) loads, not through the non-coherent read-only path.
+// Ordering: the block's writes are gathered by __syncthreads, released by thread 0 with
+// fence.acq_rel.gpu before its relaxed arrival (the last arrival acquires the others' releases through
+// the arrival count and releases the generation behind a second fence), and acquired by the waiters
+// with fence.acq_rel.gpu after they observe the generation; the closing __syncthreads passes that on
+// to the block (a sequentially consistent fence is not needed). The poll does not sleep: one thread
+// per SM polls one L2 line.
 __device__ inline bool grid_barrier(unsigned int* bar, unsigned int& epoch, unsigned long long wait_ns) {
   __shared__ int ok;
   __syncthreads();
@@ -549,12 +557,12 @@ __device__ inline bool grid_barrier(unsigned int* bar, unsigned int& epoch, unsi
     ++epoch;
     volatile unsigned int* vgen = bar + kBarGen;
     volatile unsigned int* vfault = bar + kBarFault;
-    __threadfence();
+    fence_acq_rel_gpu();
     int good = *vfault == 0u;
     if (good) {
       const unsigned long long target = (unsigned long long)epoch * gridDim.x;
       if (atomicAdd(reinterpret_cast<unsigned long long*>(bar), 1ull) == target - 1) {
-        __threadfence();
+        fence_acq_rel_gpu();
         atomicExch(bar + kBarGen, epoch);
       } else {
         const unsigned long long t0 = global_ns();
@@ -572,11 +580,10 @@ __device__ inline bool grid_barrier(unsigned int* bar, unsigned int& epoch, unsi
               break;
             }
           }
-          __nanosleep(40);
         }
       }
     }
-    __threadfence();
+    fence_acq_rel_gpu();
     ok = good;
   }
   __syncthreads();

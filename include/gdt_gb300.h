@@ -422,10 +422,19 @@ gdt_status gdt_fv_timestep(gdt_context ctx, gdt_space fv, const gdt_fv_desc* des
 /* ------------------------------------------------------------------ batched --- */
 /* Many parametric stationary problems in one persistent launch (the pyMOR-style parameter sweeps of
  * python/dune/gdt/gamm-2019-talk-on-conservative-rb.cc:74-95 run as one GPU job): problem i is
- * -div(kappa grad u) = force on the unit square with cells[i] x cells[i] squares split into two
- * triangles each, continuous P1, kappa = mu[4 i + q] on quadrant q = qx + 2 qy of the 2 x 2 split,
- * homogeneous Dirichlet boundary. cells[i] even. Sizes may differ between problems. */
+ * -div(kappa grad u) = force on the unit square with cells[i] x cells[i] squares, continuous P1 on
+ * the squares split into two triangles each (GDT_BATCH_P1_SIMPLEX, element e = 2 cell + t) or
+ * continuous Q1 on the squares (GDT_BATCH_Q1_CUBE, element e = cell), cells lexicographic with x
+ * fastest, homogeneous Dirichlet boundary. Sizes may differ between problems. kappa is given either
+ * per quadrant of the 2 x 2 split (GDT_BATCH_KAPPA_QUADRANTS: kappa[4 i + q], q = qx + 2 qy; cells[i]
+ * even) or per element (GDT_BATCH_KAPPA_ELEMENTS: kappa[eoff[i] + e] with the element offsets of
+ * gdt_batch_element_offsets). */
 typedef struct gdt_batch_s* gdt_batch;
+
+enum { GDT_BATCH_P1_SIMPLEX = 0, GDT_BATCH_Q1_CUBE = 1 };
+enum { GDT_BATCH_KAPPA_QUADRANTS = 0, GDT_BATCH_KAPPA_ELEMENTS = 1 };
+/* who solves a problem: the 8 CTAs of a thread-block cluster together, one CTA, or one warp */
+enum { GDT_BATCH_TEAM_CLUSTER = 0, GDT_BATCH_TEAM_CTA = 1, GDT_BATCH_TEAM_WARP = 2 };
 
 typedef struct gdt_batch_info {
   int64_t problems;
@@ -434,21 +443,49 @@ typedef struct gdt_batch_info {
   int min_iterations;
   double max_rel_residual;  /* ||b - A x|| / ||b|| of the returned iterates, FP64 */
   int all_converged;
+  int64_t nonfinite_problems; /* problems skipped for non-finite kappa or load (x = 0, status GDT_ENAN) */
 } gdt_batch_info;
 
+/* P1 batch (gdt_batch_create_ex with GDT_BATCH_P1_SIMPLEX) */
 gdt_status gdt_batch_create(gdt_context ctx, int64_t nproblems, const int64_t* cells, gdt_batch* out);
+/* cells[i] in [1, 16384]; element GDT_BATCH_P1_SIMPLEX or GDT_BATCH_Q1_CUBE. Every problem starts on
+ * cluster teams (gdt_batch_set_teams / gdt_batch_tune change that). */
+gdt_status gdt_batch_create_ex(gdt_context ctx, int64_t nproblems, const int64_t* cells, int element, gdt_batch* out);
 gdt_status gdt_batch_destroy(gdt_batch b);
 int64_t gdt_batch_total_dofs(gdt_batch b);
-/* host array of nproblems + 1 DoF offsets into the concatenated solution vector */
+int64_t gdt_batch_total_elements(gdt_batch b);
+/* host arrays of nproblems + 1 offsets into the concatenated solution vector / per-element kappa */
 gdt_status gdt_batch_dof_offsets(gdt_batch b, int64_t* offsets);
+gdt_status gdt_batch_element_offsets(gdt_batch b, int64_t* offsets);
+/* team kind per problem (host array of nproblems GDT_BATCH_TEAM_* values) */
+gdt_status gdt_batch_set_teams(gdt_context ctx, gdt_batch b, const int* teams);
+gdt_status gdt_batch_teams(gdt_batch b, int* teams);
 /* assemble (FP64) and solve every problem to ||b - A x|| <= tol ||b|| in one persistent launch (CUDA
- * graph, re-captured when the arguments change). mu: device [4 * nproblems]; x: device [total_dofs];
- * stencil_out: optional device [total_dofs][7] receiving the assembled rows in CSR column order (NULL to
- * skip); precision: GDT_PRECISION_FP64 or GDT_PRECISION_MIXED. info (optional) makes the call wait. */
+ * graph, re-captured when the arguments or the teams change). kappa: device array (see above); x:
+ * device [total_dofs]; stencil_out: optional device [total_dofs][7 (P1) or 9 (Q1)] receiving the
+ * assembled rows in CSR column order (NULL to skip); precision: GDT_PRECISION_FP64 or
+ * GDT_PRECISION_MIXED. info (optional) makes the call wait; then a problem with non-finite data makes
+ * the call return GDT_ENAN and one that did not converge GDT_ENOCONV (the other problems are solved
+ * all the same: see gdt_batch_status). */
+gdt_status gdt_batch_solve_ex(gdt_context ctx, gdt_batch b, const double* kappa, int kappa_kind, double force,
+                              int precision, double tol, int max_iter, double* x, double* stencil_out,
+                              gdt_batch_info* info);
+/* gdt_batch_solve_ex with kappa per quadrant (mu: device [4 * nproblems]) */
 gdt_status gdt_batch_solve(gdt_context ctx, gdt_batch b, const double* mu, double force, int precision, double tol,
                            int max_iter, double* x, double* stencil_out, gdt_batch_info* info);
+/* Autotuner of the team kinds: for every size class (problems with the same cells, largest first) the
+ * batch solve of that class alone is timed (CUDA events, after one warm-up launch) with cluster, CTA
+ * and (for at most 20000 DoFs per problem) warp teams, on the caller's data; the fastest kind is kept
+ * for the class. Optional outputs: nsizes (classes), sizes[k] (cells of class k), ms[3 k + team]
+ * (-1 where not tried); sizes and ms need room for nproblems classes. Waits; x receives the last
+ * timed solve of every class. */
+gdt_status gdt_batch_tune(gdt_context ctx, gdt_batch b, const double* kappa, int kappa_kind, double force,
+                          int precision, double tol, int max_iter, double* x, int64_t* nsizes, int64_t* sizes,
+                          double* ms);
 /* per-problem iteration counts (negative: -(count + 1) when not converged) and relative residuals (host) */
 gdt_status gdt_batch_iterations(gdt_context ctx, gdt_batch b, int* iterations, double* rel_residuals);
+/* per-problem status of the last solve (host): GDT_OK, GDT_ENOCONV or GDT_ENAN */
+gdt_status gdt_batch_status(gdt_context ctx, gdt_batch b, int* status);
 
 /* ------------------------------------------------------------------ adjoint --- */
 /* out[e] = -d/dlog(kappa_e) [lam^T A(kappa) u]: the gradient of J(u(kappa)) w.r.t. log kappa when
