@@ -70,7 +70,8 @@ struct gdt_batch_s {
   int* d_iters = nullptr;
   double* d_relres = nullptr;
   int* d_status = nullptr;
-  int nclusters = 0;
+  int nclusters = 0;                     // clusters resident at once (the larger of the two kernels')
+  int nclusters_prec[2] = {0, 0};        // per precision: FP64, mixed
   double* scratch64 = nullptr;           // [nclusters][scratch_words]
   float* scratch32 = nullptr;
   long long scratch_words = 0;
@@ -514,7 +515,7 @@ __device__ bool cg_reliable(const BatchArgs& a, Team& t, int n, int lo, int hi, 
 }
 
 // one problem, start to finish, by one team
-template <int NS, class Team>
+template <int NS, bool MIXED, class Team>
 __device__ void solve_problem(const BatchArgs& a, Team& t, int prob, double* s64, float* s32, long long stride) {
   const int n = a.cells[prob];
   const int nv = n + 1;
@@ -526,7 +527,7 @@ __device__ void solve_problem(const BatchArgs& a, Team& t, int prob, double* s64
   const double bad = assemble_rows<NS>(a, t, prob, n, lo, hi, w, x);
   int iters = 0, conv = 0, st = GDT_OK;
   double relres = 0.0;
-  if (!a.mixed) {
+  if constexpr (!MIXED) {
     if (cg_fp64<NS>(a, t, n, lo, hi, w, x, bad, iters, conv)) {
       // true relative residual of the returned iterate
       t.sync();
@@ -554,10 +555,14 @@ __device__ void solve_problem(const BatchArgs& a, Team& t, int prob, double* s64
   }
 }
 
-// at most 64 registers: four CTAs per SM, so twice as many clusters (problems in flight) as at the
-// 128 registers the compiler would otherwise use; the iterations are latency-bound at low occupancy
-template <int NS>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BT, 4) batch_kernel(const __grid_constant__ BatchArgs a) {
+// At most 64 registers: four CTAs per SM, so twice as many clusters (problems in flight) as at the
+// 128 registers the compiler would otherwise use. One instantiation per precision: the FP64 one then
+// needs no spills. The mixed one (the FP32 sequence next to the FP64 residual replacement) spills some
+// 300 bytes per thread, and still runs the 512-problem bench 1.4x faster than at three CTAs per SM
+// and 80 registers (the large problems want the loads of more CTAs in flight).
+template <int NS, bool MIXED>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BT, 4)
+    batch_kernel(const __grid_constant__ BatchArgs a) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = int(cl.block_rank());
   const long long cid = blockIdx.x / CL;
@@ -575,28 +580,31 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(BT, 4) batch_kernel
     const BatchItem item = a.items[it];
     if (item.team == GDT_BATCH_TEAM_CLUSTER) {
       ClusterTeam t{cl, rank, slots};
-      solve_problem<NS>(a, t, a.probs[item.first], s64, s32, item.stride);
+      solve_problem<NS, MIXED>(a, t, a.probs[item.first], s64, s32, item.stride);
     } else if (item.team == GDT_BATCH_TEAM_CTA) {
       if (rank < item.count) {
         CtaTeam t{slots};
         const long long base = rank * kWords * item.stride;
-        solve_problem<NS>(a, t, a.probs[item.first + rank], s64 + base, s32 + base, item.stride);
+        solve_problem<NS, MIXED>(a, t, a.probs[item.first + rank], s64 + base, s32 + base, item.stride);
       }
     } else {
       const int k = rank * WPC + int(threadIdx.x >> 5);
       if (k < item.count) {
         WarpTeam t;
         const long long base = k * kWords * item.stride;
-        solve_problem<NS>(a, t, a.probs[item.first + k], s64 + base, s32 + base, item.stride);
+        solve_problem<NS, MIXED>(a, t, a.probs[item.first + k], s64 + base, s32 + base, item.stride);
       }
     }
     cl.sync();  // the item's teams are done before the scratch is reused
   }
 }
 
-const void* kernel_of(int element) {
-  return element == GDT_BATCH_Q1_CUBE ? reinterpret_cast<const void*>(&batch_kernel<9>)
-                                      : reinterpret_cast<const void*>(&batch_kernel<7>);
+const void* kernel_of(int element, bool mixed) {
+  if (element == GDT_BATCH_Q1_CUBE)
+    return mixed ? reinterpret_cast<const void*>(&batch_kernel<9, true>)
+                 : reinterpret_cast<const void*>(&batch_kernel<9, false>);
+  return mixed ? reinterpret_cast<const void*>(&batch_kernel<7, true>)
+               : reinterpret_cast<const void*>(&batch_kernel<7, false>);
 }
 int stencil_of(int element) { return element == GDT_BATCH_Q1_CUBE ? 9 : 7; }
 
@@ -765,8 +773,14 @@ BatchArgs make_args(gdt_batch b, const SolveArgs& s) {
 
 void launch(gdt_batch b, const BatchArgs& a, cudaStream_t s) {
   cudaMemsetAsync(b->d_queue, 0, sizeof(int), s);
-  if (b->element == GDT_BATCH_Q1_CUBE) batch_kernel<9><<<b->nclusters * CL, BT, 0, s>>>(a);
-  else batch_kernel<7><<<b->nclusters * CL, BT, 0, s>>>(a);
+  const dim3 grid(b->nclusters_prec[a.mixed ? 1 : 0] * CL);
+  if (b->element == GDT_BATCH_Q1_CUBE) {
+    if (a.mixed) batch_kernel<9, true><<<grid, BT, 0, s>>>(a);
+    else batch_kernel<9, false><<<grid, BT, 0, s>>>(a);
+  } else {
+    if (a.mixed) batch_kernel<7, true><<<grid, BT, 0, s>>>(a);
+    else batch_kernel<7, false><<<grid, BT, 0, s>>>(a);
+  }
 }
 
 // per-problem results of the last launch over `subset` into info; the status of the call
@@ -893,8 +907,8 @@ gdt_status gdt_batch_create_ex(gdt_context ctx, int64_t nproblems, const int64_t
   b->total = b->offsets[nproblems];
   b->total_elems = b->eoffsets[nproblems];
   b->teams.assign(nproblems, GDT_BATCH_TEAM_CLUSTER);
-  int max_clusters = 0;
-  {
+  for (int mixed = 0; mixed < 2; ++mixed) {
+    int max_clusters = 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(CL * 64);
     cfg.blockDim = dim3(BT);
@@ -905,11 +919,13 @@ gdt_status gdt_batch_create_ex(gdt_context ctx, int64_t nproblems, const int64_t
     attr.val.clusterDim.z = 1;
     cfg.attrs = &attr;
     cfg.numAttrs = 1;
-    if (cudaOccupancyMaxActiveClusters(&max_clusters, kernel_of(element), &cfg) != cudaSuccess || max_clusters < 1)
+    if (cudaOccupancyMaxActiveClusters(&max_clusters, kernel_of(element, mixed), &cfg) != cudaSuccess ||
+        max_clusters < 1)
       max_clusters = std::max(1, ctx->num_sms / CL);
     cudaGetLastError();
+    b->nclusters_prec[mixed] = int(std::min<long long>(max_clusters, nproblems));
   }
-  b->nclusters = int(std::min<long long>(max_clusters, nproblems));
+  b->nclusters = std::max(b->nclusters_prec[0], b->nclusters_prec[1]);
   std::vector<int> c32(b->cells.begin(), b->cells.end());
   cudaError_t e = cudaMalloc(&b->d_items, sizeof(BatchItem) * nproblems);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_probs, sizeof(int) * nproblems);
