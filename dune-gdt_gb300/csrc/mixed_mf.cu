@@ -103,9 +103,12 @@ __device__ __forceinline__ float cross_of(const float (&f)[8], const U4& u) {
 // layer z - 1 pairs (with planes z - 1 and z) are summed one step ahead into `carry`, so a step loads
 // plane z + 1 and layer z and keeps two planes in registers.
 template <bool DIR>
+// (w restrict: its stores do not alias the loads, so the next plane's loads may be issued before this
+// plane's store; zb and r are read with plain coherent loads, never the read-only path: other blocks
+// wrote them before the last grid barrier)
 __device__ __forceinline__ void mf3_column(const Mf3& g, int x, int y, int z0, int z1, const float* __restrict__ kap,
-                                           const float* zb, const float* r, float* w, float& gam, float& del,
-                                           float& rr) {
+                                           const float* zb, const float* r, float* __restrict__ w, float& gam,
+                                           float& del, float& rr) {
   const long long vb = (x + 1) + (long long)g.PX * (y + 1) + g.PXY;  // vertex (x, y, 0)
   const float* zc = zb + vb;
   const float* rc = r + vb;
@@ -172,7 +175,8 @@ __device__ __forceinline__ void mf3_column(const Mf3& g, int x, int y, int z0, i
 // the operator pass over the grid's (column, z chunk) items, grid-stride
 template <bool DIR>
 __device__ __forceinline__ void mf3_apply_items(const Mf3& g, const float* __restrict__ kap, const float* zb,
-                                                const float* r, float* w, float& gam, float& del, float& rr) {
+                                                const float* r, float* __restrict__ w, float& gam, float& del,
+                                                float& rr) {
   const long long items = (long long)g.ncol * g.chunks;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items; it += stride) {
@@ -240,13 +244,14 @@ __global__ void __launch_bounds__(MT, 1) k_mf3_persistent(MfPArgs a) {
       // p = z + beta p, s = w + beta s, x32 += alpha p, r -= alpha s, zb = D_m r (z = D r: D_m, or 1 where
       // D_m is 0 on a Dirichlet row; 0 in the padding, where r is 0)
       const float af = sc.af, bf = sc.bf;
-      float4* p4 = reinterpret_cast<float4*>(a.p);
-      float4* s4 = reinterpret_cast<float4*>(a.s);
-      float4* x4 = reinterpret_cast<float4*>(a.x32);
-      float4* r4 = reinterpret_cast<float4*>(a.r);
+      // (the written arrays restrict: the next group's loads may be issued before this group's stores)
+      float4* __restrict__ p4 = reinterpret_cast<float4*>(a.p);
+      float4* __restrict__ s4 = reinterpret_cast<float4*>(a.s);
+      float4* __restrict__ x4 = reinterpret_cast<float4*>(a.x32);
+      float4* __restrict__ r4 = reinterpret_cast<float4*>(a.r);
       const float4* w4 = reinterpret_cast<const float4*>(a.w);
       const float4* d4 = reinterpret_cast<const float4*>(a.dm);
-      float4* z4 = reinterpret_cast<float4*>(a.zb);
+      float4* __restrict__ z4 = reinterpret_cast<float4*>(a.zb);
       for (long long i = t0; i < a.n4; i += stride) {
         float4 pv = p4[i], sv = s4[i], xv = x4[i], rv = r4[i];
         const float4 wv = w4[i], dv = __ldg(d4 + i);
