@@ -591,22 +591,34 @@ __device__ inline bool grid_barrier(unsigned int* bar, unsigned int& epoch, unsi
 }
 
 // Sum of the per-block partials part[k * gridDim.x + b], the same bits in every block (a fixed order:
-// lane-strided sums, then a shuffle tree); result in every thread. Warp 0 alone does the FP64 adds:
-// this part issues one FP64 warp instruction per 16 SM cycles, so a block-wide FP64 tree over every
-// warp of a large block would put microseconds on the critical path of each solver iteration.
-// bc: NV doubles of shared memory.
+// per lane the partials b = lane + 32 u in order of u, then a shuffle tree); result in every thread.
+// Warp k sums component k: its lanes issue all their loads before the first add (a loop that adds
+// each partial as it arrives waits one L2 latency per partial, several microseconds per iteration of
+// a persistent solver), and only these NV warps issue FP64 adds (this part runs one FP64 warp
+// instruction per 16 SM cycles). Needs blockDim.x >= 32 NV. bc: NV doubles of shared memory.
 template <int NV>
 __device__ __forceinline__ void grid_allreduce(const double* part, double (&v)[NV], double* bc) {
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < NV) {
+    const double* pk = part + (long long)warp * gridDim.x;
+    constexpr int U = 8;
+    double s = 0.0;
+    int b = lane;
+    for (; b + 32 * (U - 1) < (int)gridDim.x; b += 32 * U) {
+      double t[U];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double s = 0.0;
-      for (int b = lane; b < gridDim.x; b += 32) s += part[k * gridDim.x + b];
+      for (int u = 0; u < U; ++u) t[u] = pk[b + 32 * u];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) bc[k] = s;
+      for (int u = 0; u < U; ++u) s += t[u];
     }
+    double t[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) t[u] = b + 32 * u < (int)gridDim.x ? pk[b + 32 * u] : 0.0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) s += t[u];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) bc[warp] = s;
   }
   __syncthreads();
 #pragma unroll
