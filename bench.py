@@ -97,10 +97,10 @@ def hbm_peak():
 # the 128^3 workload, from single-pass ncu captures:
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none \
 #       -k regex:k_mf3_persistent -c 60 python bench.py --headline-only --no-cpu-baseline --steps 1 --warmup 0
-#   (mean of the 11 launches of one solve: 76.3 MB read + 67.6 MB written)
+#   (mean of the 11 launches of one solve: 75.9 MB read + 67.7 MB written)
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:sell_spmv_kernel -s 3 -c 1 \
 #       python bench.py --headline-only --no-cpu-baseline --steps 1 --warmup 0 --spmv-schedule sell32
-MIXED_TRAFFIC_PER_LAUNCH_128 = 143.9e6
+MIXED_TRAFFIC_PER_LAUNCH_128 = 143.6e6
 SELL_TRAFFIC_PER_SPMV_128 = 706.5e6 + 4.1e6
 
 

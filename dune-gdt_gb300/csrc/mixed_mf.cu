@@ -37,7 +37,10 @@ namespace gdt {
 namespace {
 
 constexpr int TH = 256;
-constexpr int MT = 768;  // threads per block of the persistent kernel (one block per SM)
+// threads per block of the persistent kernel (one block per SM): 768 at 80 registers, no spills.
+// 1024 at 64 registers (some spills) measured slower in the solver (28.6 against 27.8 us per
+// iteration at 128^3).
+constexpr int MT = 768;
 // residual replacement when the iterated residual's square dropped by this factor since the last one
 // (10x in the residual norm; 100x saved 5 of 11 replacements at 128^3 but cost 10 % more iterations)
 constexpr double kReplaceDrop2 = 1e-2;
@@ -420,6 +423,26 @@ __global__ void __launch_bounds__(TH) k_mf3_compare(int n, Mf3 g, const int* __r
   }
 }
 
+// the same check on the SELL-32 copy of the matrix
+__global__ void __launch_bounds__(TH) k_mf3_compare_sell(SellView A, Mf3 g, const double* __restrict__ v64,
+                                                        const float* __restrict__ w, unsigned int* err) {
+  float md = 0.f, my = 0.f;
+  for_slices(A, v64, [&](int row, bool active, double y, double) {
+    if (active) {
+      md = fmaxf(md, float(fabs(y - double(w[g.vidx(row)]))));
+      my = fmaxf(my, float(fabs(y)));
+    }
+  });
+  for (int o = 16; o > 0; o >>= 1) {
+    md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+    my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(err, __float_as_uint(md));
+    atomicMax(err + 1, __float_as_uint(my));
+  }
+}
+
 // start: r64 = b - A x (FP64), r32 = r64, zb = D_m r32; rr0
 template <int G, int PL>
 __global__ void __launch_bounds__(TH) k_mf3_init(int n, Mf3 g, const int* __restrict__ rp, const int* __restrict__ col,
@@ -675,6 +698,10 @@ gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double
   // FP32 rounding is ~1e-6): values changed after assembly make the caller take the stencil path
   GDT_CHECK(ctx, tune_spmv(ctx, m));
   const LaunchShape sh = schedule_shape<double>(m->spmv_sched, n, ctx->num_sms);
+  // the FP64 products (this check, the residuals) read the SELL-32 copy where the tuner chose it for
+  // this matrix (the copy is refreshed here: the caller may have written the CSR values)
+  const bool sell = m->use_sell && sell_prepare(ctx, m, s, true) == GDT_OK;
+  const SellView SA = sell ? sell_view(m) : SellView{};
   {
     const int ablocks = int(std::min<long long>(((long long)g.ncol * g.chunks + TH - 1) / TH, 1LL << 30));
     k_mf3_probe<<<vec_blocks, TH, 0, s>>>(n, g, dir ? 1 : 0, v64, r32, zb);
@@ -682,7 +709,10 @@ gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double
     else k_mf3_apply<false><<<ablocks, TH, 0, s>>>(g, kap, zb, r32, w);
 #define GDT_MF3_COMPARE(GG, PP) \
   k_mf3_compare<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, v64, w, err)
-    GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_COMPARE)
+    if (sell)
+      k_mf3_compare_sell<<<sell_blocks(SA.nslices, ctx->num_sms, reinterpret_cast<const void*>(&k_mf3_compare_sell)),
+                           TH, 0, s>>>(SA, g, v64, w, err);
+    else GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_COMPARE)
 #undef GDT_MF3_COMPARE
     unsigned int herr[2] = {0u, 0u};
     GDT_TRY_CUDA(ctx, cudaMemcpyAsync(herr, err, sizeof(herr), cudaMemcpyDeviceToHost, s));
@@ -694,10 +724,6 @@ gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double
     if (!(ey > 0.f) || !std::isfinite(ed) || ed > 1e-4f * ey) return GDT_EUNSUPPORTED;
     for (float* v : {r32, zb, w}) GDT_TRY_CUDA(ctx, cudaMemsetAsync(v, 0, vb, s));
   }
-  // the FP64 residuals read the SELL-32 copy where the tuner chose it for this matrix (the copy is
-  // refreshed here: the caller may have written the CSR values)
-  const bool sell = m->use_sell && sell_prepare(ctx, m, s, true) == GDT_OK;
-  const SellView SA = sell ? sell_view(m) : SellView{};
   const int sblocks_init =
       sell ? sell_blocks(SA.nslices, ctx->num_sms, reinterpret_cast<const void*>(&k_mf3_init_sell)) : 0;
   const int sblocks =
