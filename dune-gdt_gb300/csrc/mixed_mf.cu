@@ -755,28 +755,36 @@ gdt_status solve_mixed_mf(gdt_context ctx, gdt_matrix m, const double* b, double
   MfState fin{};
   unsigned int fault = 0;
   int cycles = 0;
-  for (; cycles < 100000; ++cycles) {
-    a.start = cycles == 0 ? MF3_INIT : MF3_REPLACE;
-    GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar, 0, sizeof(unsigned long long), s));
-    GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarGen, 0, sizeof(unsigned int), s));
-    GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarFault, 0, sizeof(unsigned int), s));
-    void* args[] = {&a};
-    timing_begin(ctx, s, GDT_TIMING_MIXED_PERSISTENT);
-    const cudaError_t le = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(MT), args, 0, s);
-    timing_end(ctx, s);
-    GDT_TRY_CUDA(ctx, le);
-    ctx->launches++;
-    // the FP64 reliable update (both kernels return at once unless a replacement is due)
-    timing_begin(ctx, s, GDT_TIMING_RELIABLE_UPDATE);
-    k_mf3_accumulate<<<vec_blocks, TH, 0, s>>>(n, g, x, x32, st, 0);
+  // Cycles are enqueued four at a time and the host reads the state once per group: every kernel of a
+  // cycle returns at entry once the solve has converged, so a group's surplus launches cost only their
+  // launch, and the GPU does not idle for a host round trip after every replacement. The fault flag is
+  // cleared once per solve: a barrier wait that runs out in any cycle stays visible, and the group's
+  // remaining launches leave at their first barrier.
+  constexpr int kCyclesPerCheck = 4;
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarFault, 0, sizeof(unsigned int), s));
+  while (cycles < 100000) {
+    for (int k = 0; k < kCyclesPerCheck && cycles < 100000; ++k, ++cycles) {
+      a.start = cycles == 0 ? MF3_INIT : MF3_REPLACE;
+      GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar, 0, sizeof(unsigned long long), s));
+      GDT_TRY_CUDA(ctx, cudaMemsetAsync(a.bar + kBarGen, 0, sizeof(unsigned int), s));
+      void* args[] = {&a};
+      timing_begin(ctx, s, GDT_TIMING_MIXED_PERSISTENT);
+      const cudaError_t le = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(MT), args, 0, s);
+      timing_end(ctx, s);
+      GDT_TRY_CUDA(ctx, le);
+      ctx->launches++;
+      // the FP64 reliable update (both kernels return at once unless a replacement is due)
+      timing_begin(ctx, s, GDT_TIMING_RELIABLE_UPDATE);
+      k_mf3_accumulate<<<vec_blocks, TH, 0, s>>>(n, g, x, x32, st, 0);
 #define GDT_MF3_TRUE_RESIDUAL(GG, PP)                                                                            \
   k_mf3_true_residual<GG, PP><<<sh.blocks, sh.threads, sh.smem, s>>>(n, g, m->rp, m->col, m->val, x, b, r32, dm, \
                                                                      zb, st, partials, ticket)
-    if (sell) k_mf3_true_residual_sell<<<sblocks, TH, 0, s>>>(SA, g, x, b, r32, dm, zb, st, partials, ticket);
-    else GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_TRUE_RESIDUAL)
+      if (sell) k_mf3_true_residual_sell<<<sblocks, TH, 0, s>>>(SA, g, x, b, r32, dm, zb, st, partials, ticket);
+      else GDT_SCHEDULE_SWITCH(m->spmv_sched, GDT_MF3_TRUE_RESIDUAL)
 #undef GDT_MF3_TRUE_RESIDUAL
-    timing_end(ctx, s);
-    ctx->launches += 2;
+      timing_end(ctx, s);
+      ctx->launches += 2;
+    }
     GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fin, st, sizeof(MfState), cudaMemcpyDeviceToHost, s));
     GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&fault, a.bar + kBarFault, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
