@@ -401,6 +401,32 @@ struct ChunkSum {
   __device__ __forceinline__ double sum() const { return total + double(part); }
 };
 
+// Reliable update of the mixed sequence: x += d32, d32 = 0, then r32 = b - A x from the FP64 stencil;
+// t2 = (r32 . D r32, |r|^2) reduced over the team. Not inlined: its FP64 pointers and temporaries stay
+// out of the register allocation of the FP32 iteration (which runs hundreds of times per call of this).
+template <int NS, class Team>
+__device__ __noinline__ void replace_residual(Team& t, int n, int lo, int hi, const Scratch<NS>& w, double* x,
+                                              double* t2) {
+  const int nv = n + 1;
+  for (int i = lo + t.tid(); i < hi; i += t.stride()) {
+    x[i] += double(w.d32()[i]);
+    w.d32()[i] = 0.0f;
+  }
+  t.sync();  // x complete before the FP64 residual reads the neighbours' rows
+  double v[2] = {0.0, 0.0};
+  for (int i = lo + t.tid(); i < hi; i += t.stride()) {
+    const int ix = i % nv, iy = i / nv;
+    const double ri = w.b()[i] - stencil_row<NS, double>(t, w.S(), x, i, nv, vbnd(ix, iy, n));
+    const float rf = float(ri);
+    w.r32()[i] = rf;
+    v[0] += double(rf) * double(w.dinv32()[i] * rf);
+    v[1] += ri * ri;
+  }
+  t.reduce(v, 6);
+  t2[0] = v[0];
+  t2[1] = v[1];
+}
+
 // Mixed-precision CG with reliable updates: x (FP64) = 0 on entry, b the FP64 load; the FP32 sequence
 // iterates d32 (correction), r32, p32, q32. Convergence is decided on the true FP64 residual only;
 // relres = ||b - A x|| / ||b|| of the returned x.
@@ -459,21 +485,8 @@ __device__ bool cg_reliable(const BatchArgs& a, Team& t, int n, int lo, int hi, 
     rho = w2[0];
     if (w2[1] <= drop * rr_ref || w2[1] <= a.tol2 * rr0 || iters >= a.max_iter) {
       // reliable update: x += d, d = 0; r = b - A x (FP64), r32 = r; beta from the replaced residual
-      for (int i = lo + t.tid(); i < hi; i += t.stride()) {
-        x[i] += double(w.d32()[i]);
-        w.d32()[i] = 0.0f;
-      }
-      t.sync();  // x complete before the FP64 residual reads the neighbours' rows
-      double t2[2] = {0.0, 0.0};
-      for (int i = lo + t.tid(); i < hi; i += t.stride()) {
-        const int ix = i % nv, iy = i / nv;
-        const double ri = w.b()[i] - stencil_row<NS, double>(t, w.S(), x, i, nv, vbnd(ix, iy, n));
-        const float rf = float(ri);
-        w.r32()[i] = rf;
-        t2[0] += double(rf) * double(w.dinv32()[i] * rf);
-        t2[1] += ri * ri;
-      }
-      t.reduce(t2, 6);
+      double t2[2];
+      replace_residual<NS>(t, n, lo, hi, w, x, t2);
       // Stagnation guard: when a whole cycle gained less than 2x on the true residual, the gap between
       // the FP32 and FP64 operators dominates. From then on every replacement restarts the direction
       // (beta = 0) and waits for a 1000x drop: FP64 iterative refinement around FP32 CG.
@@ -496,20 +509,10 @@ __device__ bool cg_reliable(const BatchArgs& a, Team& t, int n, int lo, int hi, 
   }
   if (!conv) {  // stopped by breakdown or the iteration limit: fold in the correction, report the true residual
     t.sync();
-    for (int i = lo + t.tid(); i < hi; i += t.stride()) {
-      x[i] += double(w.d32()[i]);
-      w.d32()[i] = 0.0f;
-    }
-    t.sync();
-    double t1[1] = {0.0};
-    for (int i = lo + t.tid(); i < hi; i += t.stride()) {
-      const int ix = i % nv, iy = i / nv;
-      const double ri = w.b()[i] - stencil_row<NS, double>(t, w.S(), x, i, nv, vbnd(ix, iy, n));
-      t1[0] += ri * ri;
-    }
-    t.reduce(t1, 6);
-    relres = rr0 > 0.0 ? sqrt(t1[0] / rr0) : 0.0;
-    if (t1[0] <= a.tol2 * rr0) conv = 1;
+    double t2[2];
+    replace_residual<NS>(t, n, lo, hi, w, x, t2);
+    relres = rr0 > 0.0 ? sqrt(t2[1] / rr0) : 0.0;
+    if (t2[1] <= a.tol2 * rr0) conv = 1;
   }
   return true;
 }
