@@ -106,6 +106,7 @@ _SIGNATURES = {
                                           C.POINTER(C.c_int64), C.c_int]),
     "gdt_context_kernel_timing": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int]),
     "gdt_measure_fp64_peak": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gdt_measure_l2_bandwidth": (C.c_int, [P, C.POINTER(C.c_double)]),
     "gdt_grid_create_cube": (C.c_int, [C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(P)]),
     "gdt_grid_destroy": (C.c_int, [P]),

@@ -1,5 +1,5 @@
-// FP64 throughput of the GPU at hand, measured with CUDA events (no reference counterpart: the
-// denominators of the FP64-bound kernels' rooflines). GB300 runs FP64 at a small fraction of its
+// FP64 throughput and L2 bandwidth of the GPU at hand, measured with CUDA events (no reference
+// counterpart: the denominators of the FP64-bound and the L2-resident kernels' rooflines). GB300 runs FP64 at a small fraction of its
 // FP32 rate, so the FV stage kernel, the FP64 CSR SpMV and the element assembly are measured against
 // these numbers rather than against a nominal figure.
 //
@@ -49,8 +49,54 @@ __global__ void __launch_bounds__(kPeakThreads) k_peak_dmma(int iters, double se
   if (s == -1.0) sink[blockIdx.x] = s;
 }
 
+// L2 bandwidth: float4 copies between two 24 MB buffers (together well inside the 129 MB L2),
+// `reps` passes in one launch; the empty asm statement between passes keeps the compiler from
+// hoisting the loads out of the pass loop
+__global__ void __launch_bounds__(kPeakThreads) k_l2_copy(const float4* __restrict__ a, float4* __restrict__ b,
+                                                          long long n4, int reps) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (int r = 0; r < reps; ++r) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += stride) b[i] = a[i];
+    asm volatile("" ::: "memory");
+  }
+}
+
 }  // namespace
 }  // namespace gdt
+
+extern "C" gdt_status gdt_measure_l2_bandwidth(gdt_context ctx, double* gbs) {
+  using namespace gdt;
+  if (!ctx || !gbs) return GDT_EINVAL;
+  cudaStream_t s = ctx->stream;
+  const long long n4 = (24ll << 20) / 16;  // 24 MB per buffer
+  const int reps = 64;
+  float4* buf = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&buf, sizeof(float4) * 2 * n4, s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(buf, 0, sizeof(float4) * 2 * n4, s));
+  int per_sm = 0;
+  GDT_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_l2_copy, kPeakThreads, 0));
+  const int blocks = ctx->num_sms * std::max(per_sm, 1);
+  cudaEvent_t e0, e1;
+  GDT_TRY_CUDA(ctx, cudaEventCreate(&e0));
+  GDT_TRY_CUDA(ctx, cudaEventCreate(&e1));
+  float best = 1e30f;
+  k_l2_copy<<<blocks, kPeakThreads, 0, s>>>(buf, buf + n4, n4, reps);  // warm-up: the buffers into L2
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(e0, s);
+    k_l2_copy<<<blocks, kPeakThreads, 0, s>>>(buf, buf + n4, n4, reps);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0.f && ms < best) best = ms;
+  }
+  ctx->launches += 4;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(buf, s);
+  // read + write bytes
+  *gbs = 2.0 * 16.0 * double(n4) * reps / (double(best) * 1e-3) / 1e9;
+  return check_launch(ctx, "l2 bandwidth");
+}
 
 extern "C" gdt_status gdt_measure_fp64_peak(gdt_context ctx, double* fma_tflops, double* dmma_tflops) {
   using namespace gdt;

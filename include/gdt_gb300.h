@@ -102,6 +102,10 @@ gdt_status gdt_context_kernel_timing(gdt_context ctx, int kind, double* ms, int6
  * (no reference counterpart; the denominator of FP64-bound rooflines): independent FMA chains on
  * every SM (fma_tflops) and m8n8k4 FP64 tensor-core products (dmma_tflops). Either may be NULL. */
 gdt_status gdt_measure_fp64_peak(gdt_context ctx, double* fma_tflops, double* dmma_tflops);
+/* L2 bandwidth (read + write GB/s) of float4 copies between two 24 MB device buffers, 64 passes in one
+ * launch, best of 3 after a warm-up (no reference counterpart: the ceiling of the L2-resident mixed
+ * inner iteration). Allocates and frees 48 MB on the context stream. */
+gdt_status gdt_measure_l2_bandwidth(gdt_context ctx, double* gbs);
 
 /* How gdt_solve runs FP64 CG with Jacobi or no preconditioner (no reference counterpart: the launch
  * form of the device solver). GRAPH: one kernel per step (SpMV, update, direction), iterations
