@@ -110,6 +110,7 @@ class Grid:
         self.num_cells = [int(n) for n in num_elements]
         self.simplex = bool(simplex)
         self.periodic = bool(periodic)
+        self.vertices = None  # the coordinates of a mapped grid ([num_vertices, dim] float64)
         self.lib = capi.load()
         h = C.c_void_p()
         n = (C.c_int64 * 3)(*self.num_cells, *([1] * (3 - dim)))
@@ -118,6 +119,26 @@ class Grid:
         capi.check(self.lib.gdt_grid_create_cube(dim, n, lo, hi, int(simplex), int(periodic), C.byref(h)),
                    what="make_cube_grid")
         self.handle = h
+
+    def map_vertices(self, coords):
+        """Moves the vertices to `coords` ([num_vertices, dim], vertices lexicographic with x fastest;
+        numpy or torch, host or device): a mapped structured grid whose elements take their geometry
+        from their own vertices (gdt_grid_set_vertices). Call before creating spaces; a mapped grid
+        takes continuous order-1 spaces and the Laplace stiffness / load vector assembly."""
+        import numpy as np
+
+        nv = int(self.lib.gdt_grid_num_vertices(self.handle))
+        if isinstance(coords, torch.Tensor):
+            keep = coords.detach().to(torch.float64).contiguous()
+            shape, ptr = tuple(keep.shape), keep.data_ptr()
+        else:
+            keep = np.ascontiguousarray(coords, dtype=np.float64)
+            shape, ptr = keep.shape, keep.ctypes.data
+        if shape != (nv, self.dimension):
+            raise ValueError(f"coords must have shape ({nv}, {self.dimension}), got {shape}")
+        capi.check(self.lib.gdt_grid_set_vertices(self.handle, C.c_void_p(ptr)), what="map_vertices")
+        self.vertices = torch.as_tensor(keep).clone()
+        return self
 
     def __del__(self):
         try:
@@ -342,7 +363,9 @@ def _dirichlet_values(d, values, space, ctx):
     if isinstance(values, (int, float)):
         d.dirichlet_value_const = float(values)
         return []
-    if isinstance(values, GridFunction):
+    if isinstance(values, GridFunction) and getattr(space.grid, "vertices", None) is not None:
+        values = torch.as_tensor(values.fn(space.grid.vertices.to(ctx.device)), dtype=torch.float64, device=ctx.device)
+    elif isinstance(values, GridFunction):
         g = space.grid
         dim = g.dimension
         vn = [c + 1 for c in g.num_cells]

@@ -106,6 +106,56 @@ __device__ __forceinline__ bool on_boundary(const GridDesc& g, const long long* 
   return b;
 }
 
+// Row v of the assembled operator from its gathered stencil acc (slots of the 3^d neighbourhood) and
+// load b: Dirichlet unit row / zero columns with the lifting of given boundary values, then the
+// right-hand side entry and the CSR row (slots in ascending column order)
+template <int DIM, bool SIMPLEX>
+__device__ __forceinline__ void finish_row(const GridDesc& g, long long v, const long long (&vi)[3],
+                                           const double (&acc)[pow3(DIM)], double b, const int* __restrict__ rp,
+                                           double* __restrict__ val, double* __restrict__ rhs, int dirichlet,
+                                           const double* __restrict__ gD, double gD_const) {
+  constexpr int NS = pow3(DIM);
+  const bool bnd = dirichlet && on_boundary(g, vi, DIM);
+  // Dirichlet values g: b_v = g_v on a boundary row; elsewhere the zeroed columns move to the right-hand
+  // side, b_v -= sum over boundary neighbours w of A_vw g_w (all zero for homogeneous data)
+  const bool lift = dirichlet && rhs && (gD || gD_const != 0.0);
+  if (lift && !bnd) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      if (!slot_in_stencil(DIM, SIMPLEX, k)) continue;
+      long long w[3] = {0, 0, 0};
+      bool ok = true;
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) {
+        w[a] = vi[a] + slot_offset(k, a);
+        ok = ok && w[a] >= 0 && w[a] <= g.n[a];
+      }
+      if (ok && on_boundary(g, w, DIM)) b -= acc[k] * (gD ? gD[w[0] + g.vn[0] * (w[1] + g.vn[1] * w[2])] : gD_const);
+    }
+  }
+  if (rhs) rhs[v] = bnd ? (lift ? (gD ? gD[v] : gD_const) : 0.0) : b;
+  if (!val) return;
+  long long pos = rp[v];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    if (!slot_in_stencil(DIM, SIMPLEX, k)) continue;
+    long long w[3] = {0, 0, 0};
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      w[a] = vi[a] + slot_offset(k, a);
+      ok = ok && w[a] >= 0 && w[a] <= g.n[a];
+    }
+    if (!ok) continue;
+    double value = acc[k];
+    if (dirichlet) {
+      if (bnd) value = (k == center_slot(DIM)) ? 1.0 : 0.0;  // unit_row
+      else if (on_boundary(g, w, DIM)) value = 0.0;          // unit_col
+    }
+    val[pos++] = value;
+  }
+}
+
 template <int DIM, bool SIMPLEX>
 __global__ void __launch_bounds__(256) assemble_cg_rows(GridDesc g, const int* __restrict__ rp, double* __restrict__ val,
                                                         double* __restrict__ rhs, const LocalTables tab,
@@ -148,45 +198,198 @@ __global__ void __launch_bounds__(256) assemble_cg_rows(GridDesc g, const int* _
       }
     }
   }
-  const bool bnd = dirichlet && on_boundary(g, vi, DIM);
-  // Dirichlet values g: b_v = g_v on a boundary row; elsewhere the zeroed columns move to the right-hand
-  // side, b_v -= sum over boundary neighbours w of A_vw g_w (all zero for homogeneous data)
-  const bool lift = dirichlet && rhs && (gD || gD_const != 0.0);
-  if (lift && !bnd) {
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-      if (!slot_in_stencil(DIM, SIMPLEX, k)) continue;
-      long long w[3] = {0, 0, 0};
-      bool ok = true;
-#pragma unroll
-      for (int a = 0; a < DIM; ++a) {
-        w[a] = vi[a] + slot_offset(k, a);
-        ok = ok && w[a] >= 0 && w[a] <= g.n[a];
-      }
-      if (ok && on_boundary(g, w, DIM)) b -= acc[k] * (gD ? gD[w[0] + g.vn[0] * (w[1] + g.vn[1] * w[2])] : gD_const);
-    }
+  finish_row<DIM, SIMPLEX>(g, v, vi, acc, b, rp, val, rhs, dirichlet, gD, gD_const);
+}
+
+// The same row gather on a mapped grid (vertex coordinates g.xv): every element's contribution to the
+// row is formed from its own vertices, as DefaultGlobalBasis::jacobians does from the element geometry
+// (spaces/basis/default.hh:152-175), with the quadrature of LocalElementIntegralBilinearForm at the
+// integrand's order (local/bilinear-forms/integrals.hh:97-134):
+// - simplices (P1, affine): constant gradients grad phi_j = J^{-T} grad phi_hat_j; the stiffness
+//   kappa |det J| / d! grad phi_i . grad phi_j and the load f |det J| / (d! (d + 1)) are exact;
+// - cubes (Q1, multilinear map): the stiffness at the 2^d Gauss points of order 2 (two per axis,
+//   J, J^{-1} and |det J| at each point) and the load of a source per element at the one-point rule of
+//   order 1 (the element centre: phi_i = 2^{-d} there).
+template <int DIM>
+__device__ __forceinline__ double inv_det(const double (&J)[DIM][DIM], double (&Ji)[DIM][DIM]) {
+  if constexpr (DIM == 1) {
+    Ji[0][0] = 1.0 / J[0][0];
+    return J[0][0];
+  } else if constexpr (DIM == 2) {
+    const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    Ji[0][0] = J[1][1] / det;
+    Ji[0][1] = -J[0][1] / det;
+    Ji[1][0] = -J[1][0] / det;
+    Ji[1][1] = J[0][0] / det;
+    return det;
+  } else {
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+    Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+    Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    return det;
   }
-  if (rhs) rhs[v] = bnd ? (lift ? (gD ? gD[v] : gD_const) : 0.0) : b;
-  if (!val) return;
-  long long pos = rp[v];
+}
+
+template <int DIM, bool SIMPLEX>
+__global__ void __launch_bounds__(128) assemble_cg_rows_mapped(GridDesc g, const int* __restrict__ rp,
+                                                               double* __restrict__ val, double* __restrict__ rhs,
+                                                               const double* __restrict__ kappa, double kappa_const,
+                                                               const double* __restrict__ force, double force_const,
+                                                               int dirichlet, const double* __restrict__ gD,
+                                                               double gD_const) {
+  constexpr int NS = pow3(DIM), NSUB = num_sub(DIM, SIMPLEX), NLOC = num_local(DIM, SIMPLEX), NC = 1 << DIM;
+  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (v >= g.nvert) return;
+  long long vi[3];
+  vertex_multi(g, v, vi);
+  double acc[NS];
 #pragma unroll
-  for (int k = 0; k < NS; ++k) {
-    if (!slot_in_stencil(DIM, SIMPLEX, k)) continue;
-    long long w[3] = {0, 0, 0};
-    bool ok = true;
+  for (int k = 0; k < NS; ++k) acc[k] = 0.0;
+  double b = 0.0;
+  double fact = 1.0;  // d!
+#pragma unroll
+  for (int a = 2; a <= DIM; ++a) fact *= a;
+#pragma unroll
+  for (int cv = 0; cv < NC; ++cv) {
+    long long ci[3] = {0, 0, 0};
+    bool inside = true;
 #pragma unroll
     for (int a = 0; a < DIM; ++a) {
-      w[a] = vi[a] + slot_offset(k, a);
-      ok = ok && w[a] >= 0 && w[a] <= g.n[a];
+      ci[a] = vi[a] - ((cv >> a) & 1);
+      inside = inside && ci[a] >= 0 && ci[a] < g.n[a];
     }
-    if (!ok) continue;
-    double value = acc[k];
-    if (dirichlet) {
-      if (bnd) value = (k == center_slot(DIM)) ? 1.0 : 0.0;  // unit_row
-      else if (on_boundary(g, w, DIM)) value = 0.0;          // unit_col
+    if (!inside) continue;
+    const long long cell = cell_index(g, ci);
+    // the cell's corner coordinates, corner c at bits c
+    double X[NC][DIM];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      long long w[3] = {ci[0], ci[1], ci[2]};
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) w[a] += (c >> a) & 1;
+      const long long wv = w[0] + g.vn[0] * (w[1] + g.vn[1] * w[2]);
+#pragma unroll
+      for (int a = 0; a < DIM; ++a) X[c][a] = g.xv[wv * DIM + a];
     }
-    val[pos++] = value;
+    if constexpr (SIMPLEX) {
+#pragma unroll
+      for (int t = 0; t < NSUB; ++t) {
+#pragma unroll
+        for (int li = 0; li < NLOC; ++li) {
+          if (local_corner(DIM, true, t, li) != cv) continue;
+          const long long e = cell * NSUB + t;
+          const double kap = kappa ? kappa[e] : kappa_const;
+          // J[a][k] = x_{k+1} - x_0 (local vertices in Kuhn order)
+          double J[DIM][DIM], Ji[DIM][DIM];
+          const int c0 = local_corner(DIM, true, t, 0);
+#pragma unroll
+          for (int k = 0; k < DIM; ++k)
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) J[a][k] = X[local_corner(DIM, true, t, k + 1)][a] - X[c0][a];
+          const double vol = fabs(inv_det<DIM>(J, Ji)) / fact;
+          // grad phi_j = J^{-T} e_{j-1} (j >= 1): column j-1 of J^{-T}, i.e. row j-1 of J^{-1};
+          // grad phi_0 = -sum of the others
+          double G[NLOC][DIM];
+#pragma unroll
+          for (int a = 0; a < DIM; ++a) {
+            double s0 = 0.0;
+#pragma unroll
+            for (int j = 1; j < NLOC; ++j) {
+              G[j][a] = Ji[j - 1][a];
+              s0 += Ji[j - 1][a];
+            }
+            G[0][a] = -s0;
+          }
+#pragma unroll
+          for (int lj = 0; lj < NLOC; ++lj) {
+            double d = 0.0;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) d += G[lj][a] * G[li][a];
+            acc[slot_between(DIM, cv, local_corner(DIM, true, t, lj))] += kap * d * vol;
+          }
+          if (rhs) b += (force ? force[e] : force_const) * vol / double(DIM + 1);
+        }
+      }
+    } else {
+      const double kap = kappa ? kappa[cell] : kappa_const;
+      const double gp[2] = {0.5 - 0.5 / sqrt(3.0), 0.5 + 0.5 / sqrt(3.0)};
+      const double wq = 1.0 / double(NC);  // Gauss weights 1/2 per axis
+#pragma unroll
+      for (int q = 0; q < NC; ++q) {
+        double xh[DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) xh[a] = gp[(q >> a) & 1];
+        // reference gradients of the bilinear/trilinear shape functions at xh
+        double gr[NC][DIM];
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            double d = ((c >> k) & 1) ? 1.0 : -1.0;
+#pragma unroll
+            for (int s2 = 0; s2 < DIM; ++s2)
+              if (s2 != k) d *= ((c >> s2) & 1) ? xh[s2] : 1.0 - xh[s2];
+            gr[c][k] = d;
+          }
+        double J[DIM][DIM], Ji[DIM][DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            double sj = 0.0;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) sj += gr[c][k] * X[c][a];
+            J[a][k] = sj;
+          }
+        const double factor = fabs(inv_det<DIM>(J, Ji)) * wq;
+        // grad phi_c = J^{-T} grad_hat phi_c: component a = sum_k Ji[k][a] gr[c][k]
+        double gi[DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+          double sg = 0.0;
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) sg += Ji[k][a] * gr[cv][k];
+          gi[a] = sg;
+        }
+#pragma unroll
+        for (int lj = 0; lj < NC; ++lj) {
+          double d = 0.0;
+#pragma unroll
+          for (int a = 0; a < DIM; ++a) {
+            double sg = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) sg += Ji[k][a] * gr[lj][k];
+            d += sg * gi[a];
+          }
+          acc[slot_between(DIM, cv, lj)] += kap * d * factor;
+        }
+      }
+      if (rhs) {
+        // one-point rule at the centre: |det J(1/2, ...)|, phi = 2^{-d}, weight 1
+        double J[DIM][DIM], Ji[DIM][DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            double sj = 0.0;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) sj += (((c >> k) & 1) ? 1.0 : -1.0) * X[c][a];
+            J[a][k] = sj / double(NC / 2);
+          }
+        b += (force ? force[cell] : force_const) * fabs(inv_det<DIM>(J, Ji)) / double(NC);
+      }
+    }
   }
+  finish_row<DIM, SIMPLEX>(g, v, vi, acc, b, rp, val, rhs, dirichlet, gD, gD_const);
 }
 
 // DirichletConstraints::apply(M, V) as a separate pass over an assembled matrix: unit rows for
@@ -288,8 +491,30 @@ gdt_status mf_capture(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d
   return check_launch(ctx, "mf_capture");
 }
 
+// mapped grids: the row gather that forms each element's geometry
+gdt_status assemble_cg_mapped(gdt_context ctx, const GridDesc& g, const int* rp, double* val,
+                              const gdt_diffusion_desc* d, double* rhs, const double* gD, double gD_const) {
+  const int th = 128;
+  const int bl = grid_blocks(g.nvert, th);
+  cudaStream_t s = ctx->stream;
+#define GDT_LAUNCH_MAPPED(D, S)                                                                              \
+  assemble_cg_rows_mapped<D, S><<<bl, th, 0, s>>>(g, rp, val, rhs, d->kappa, d->kappa_const, d->force,        \
+                                                  d->force_const, d->dirichlet, gD, gD_const)
+  if (g.dim == 1) GDT_LAUNCH_MAPPED(1, false);
+  else if (g.dim == 2 && !g.simplex) GDT_LAUNCH_MAPPED(2, false);
+  else if (g.dim == 2) GDT_LAUNCH_MAPPED(2, true);
+  else if (!g.simplex) GDT_LAUNCH_MAPPED(3, false);
+  else GDT_LAUNCH_MAPPED(3, true);
+#undef GDT_LAUNCH_MAPPED
+  return check_launch(ctx, "assemble_cg_rows_mapped");
+}
+
 gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs) {
   const GridDesc& g = m->test.g;
+  if (g.xv) {
+    m->mf_valid = 0;  // the matrix-free mixed operator assumes one geometry for all elements
+    return assemble_cg_mapped(ctx, g, m->rp, m->val, d, rhs, d->dirichlet_values, d->dirichlet_value_const);
+  }
   const LocalTables tab = make_tables(g);
   const int th = 256;
   const int bl = grid_blocks(g.nvert, th);
@@ -309,6 +534,7 @@ gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* 
 
 gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& sp, const gdt_diffusion_desc* d, double* rhs) {
   const GridDesc& g = sp.g;
+  if (g.xv) return assemble_cg_mapped(ctx, g, nullptr, nullptr, d, rhs, nullptr, 0.0);
   const LocalTables tab = make_tables(g);
   const int th = 256;
   const int bl = grid_blocks(g.nvert, th);

@@ -212,6 +212,27 @@ gdt_status gdt_grid_create_cube(int dim, const int64_t* num_elements, const doub
   return GDT_OK;
 }
 
+gdt_status gdt_grid_set_vertices(gdt_grid g, const double* coords) {
+  if (!g || !coords) return GDT_EINVAL;
+  GridDesc& d = g->d;
+  if (d.periodic) return GDT_EUNSUPPORTED;
+  const size_t bytes = sizeof(double) * size_t(d.nvert) * d.dim;
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return GDT_ENOMEM;
+  }
+  // host or device coordinates (unified addressing)
+  if (cudaMemcpy(buf, coords, bytes, cudaMemcpyDefault) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(buf);
+    return GDT_ECUDA;
+  }
+  g->xv_owner = std::shared_ptr<double>(buf, [](double* q) { cudaFree(q); });
+  d.xv = buf;
+  return GDT_OK;
+}
+
 gdt_status gdt_grid_destroy(gdt_grid g) {
   if (!g) return GDT_EINVAL;
   delete g;
@@ -228,8 +249,11 @@ gdt_status gdt_space_create(gdt_grid g, int kind, int order, gdt_space* out) {
   const GridDesc& d = g->d;
   gdt_space_s s;
   s.g = d;
+  s.xv_owner = g->xv_owner;
   s.kind = kind;
   s.order = order;
+  // mapped grids: continuous order-1 spaces only (their assembly forms each element's geometry)
+  if (d.xv && !(kind == GDT_SPACE_CG && order == 1)) return GDT_EUNSUPPORTED;
   if (kind == GDT_SPACE_CG) {
     if (order != 1 && order != 2) return GDT_EUNSUPPORTED;
     if (d.periodic) return GDT_EUNSUPPORTED;
@@ -339,6 +363,8 @@ gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_di
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
   m->val_version++;
   if (d->force_qp && d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
+  if (m->test.g.xv && (d->kappa_qp || d->kappa_tensor || d->kappa_tensor_qp || d->force_qp))
+    return fail(ctx, GDT_EUNSUPPORTED, "mapped grids: kappa and source per element or constant");
   const bool values = d->dirichlet && (d->dirichlet_values || d->dirichlet_value_const != 0.0);
   if (values && (m->test.order != 1 || d->kappa_qp || d->kappa_tensor || d->kappa_tensor_qp || d->force_qp))
     return fail(ctx, GDT_EUNSUPPORTED, "Dirichlet values are lowered for the order-1 vertex-row assembly");
@@ -365,6 +391,7 @@ gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space s, const gdt_diffusion
   if (!ctx || !s || !d || !rhs) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
   if (d->force_qp) {
+    if (s->g.xv) return fail(ctx, GDT_EUNSUPPORTED, "mapped grids: source per element or constant");
     if (d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
     return ho_rhs_qp(ctx, *s, d->force_qp, d->force_quad_order, d->dirichlet, rhs);
   }
@@ -394,6 +421,7 @@ gdt_status gdt_dirichlet_apply_values(gdt_context ctx, gdt_matrix m, double* rhs
 gdt_status gdt_assemble_cg_product(gdt_context ctx, gdt_matrix m, const gdt_product_desc* d) {
   if (!ctx || !m || !d) return GDT_EINVAL;
   if (m->test.kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "matrix does not belong to a continuous space");
+  if (m->test.g.xv) return fail(ctx, GDT_EUNSUPPORTED, "mapped grids: the Laplace form only");
   m->mf_valid = 0;
   m->val_version++;
   GDT_CHECK(ctx, ho_prepare(ctx, m));
@@ -417,6 +445,7 @@ gdt_status gdt_element_error(gdt_context ctx, gdt_space s, int norm, int quad_or
   if (quad_order < 0 || quad_order > 40) return fail(ctx, GDT_EINVAL, "quadrature order out of range");
   if (s->kind == GDT_SPACE_FV || (s->kind == GDT_SPACE_DG && s->order != 1))
     return fail(ctx, GDT_EUNSUPPORTED, "element error of continuous (order 1, 2) and DG (order 1) spaces");
+  if (s->g.xv) return fail(ctx, GDT_EUNSUPPORTED, "element error on mapped grids");
   return element_error(ctx, *s, norm, quad_order, u, ref_qp, eta2, total);
 }
 
@@ -506,6 +535,7 @@ gdt_status gdt_cg_dlogkappa(gdt_context ctx, gdt_space s, const double* kappa, c
   if (!ctx || !s || !kappa || !u || !lam || !out) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
   if (s->order != 1) return fail(ctx, GDT_EUNSUPPORTED, "log-kappa gradient of order-2 spaces");
+  if (s->g.xv) return fail(ctx, GDT_EUNSUPPORTED, "log-kappa gradient on mapped grids");
   return cg_dlogkappa(ctx, *s, kappa, u, lam, out);
 }
 

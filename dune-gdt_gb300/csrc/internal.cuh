@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -26,6 +27,9 @@ struct GridDesc {
   double hi[3] = {1, 1, 1};
   double h[3] = {1, 1, 1};
   long long ncells = 1, nelem = 1, nvert = 1;
+  // vertex coordinates of a mapped grid (device, [vertex][dim], vertices lexicographic with x fastest);
+  // null for the equidistant grid of lo, hi and n
+  const double* xv = nullptr;
 };
 
 }  // namespace gdt
@@ -57,6 +61,7 @@ struct gdt_context_s {
 
 struct gdt_grid_s {
   gdt::GridDesc d;
+  std::shared_ptr<double> xv_owner;  // the device coordinates of a mapped grid (d.xv)
 };
 
 struct gdt_space_s {
@@ -65,6 +70,7 @@ struct gdt_space_s {
   int order = 1;
   int lsize = 1;
   long long size = 0;
+  std::shared_ptr<double> xv_owner;  // keeps g.xv alive with every copy of the space
 };
 
 struct gdt_matrix_s {

@@ -135,6 +135,15 @@ gdt_status gdt_context_set_persistent_limits(gdt_context ctx, int blocks, int64_
  * (element = cube * d! + permutation in std::next_permutation order). dim in {1,2,3}. */
 gdt_status gdt_grid_create_cube(int dim, const int64_t* num_elements, const double* lower_left,
                                 const double* upper_right, int simplex, int periodic, gdt_grid* out);
+/* Moves the vertices of a cube grid (or its simplex split) to the given coordinates: a mapped
+ * structured grid with the same topology and numbering, each element's geometry (J, J^{-T}, |det J|
+ * at the quadrature points, as DefaultGlobalBasis::jacobians, spaces/basis/default.hh:152-175, forms
+ * them from the element geometry) computed from its own vertices. coords: host or device
+ * [num_vertices][dim], vertices lexicographic with x fastest; copied. Call before creating spaces.
+ * A mapped grid takes continuous order-1 spaces, their Laplace stiffness and load vector (kappa and
+ * source per element or constant, Dirichlet values) and everything that works on assembled matrices
+ * (SpMV, solvers, Dirichlet constraints, lincomb); other forms return GDT_EUNSUPPORTED. */
+gdt_status gdt_grid_set_vertices(gdt_grid grid, const double* coords);
 gdt_status gdt_grid_destroy(gdt_grid grid);
 int64_t gdt_grid_num_elements(gdt_grid grid);
 int64_t gdt_grid_num_vertices(gdt_grid grid);

@@ -47,10 +47,13 @@ class Grid(C.Structure):
         ("hi", C.c_double * 3),
         ("simplex", C.c_int),
         ("periodic", C.c_int),
+        ("vertices", C.c_void_p),
     ]
 
 
-def grid(dim, n, lo=0.0, hi=1.0, simplex=False, periodic=False) -> Grid:
+def grid(dim, n, lo=0.0, hi=1.0, simplex=False, periodic=False, vertices=None) -> Grid:
+    """vertices: optional coordinates [vertex, dim] (vertices lexicographic, x fastest) of a mapped grid;
+    the array is kept alive by the returned structure."""
     g = Grid()
     g.dim = dim
     ns = list(n) if hasattr(n, "__len__") else [n] * dim
@@ -62,6 +65,14 @@ def grid(dim, n, lo=0.0, hi=1.0, simplex=False, periodic=False) -> Grid:
         g.hi[i] = his[i] if i < dim else 1.0
     g.simplex = int(bool(simplex))
     g.periodic = int(bool(periodic))
+    if vertices is not None:
+        import numpy as np
+
+        xv = np.ascontiguousarray(vertices, dtype=np.float64)
+        g._vertices = xv  # keeps the buffer alive
+        g.vertices = xv.ctypes.data
+    else:
+        g.vertices = None
     return g
 
 

@@ -235,6 +235,9 @@ struct Grid {
   long ncells = 1, nelem = 1, nvert = 1;
   long vn[3] = {1, 1, 1};
   std::vector<std::array<int, 3>> perms;  // simplex permutations
+  // vertex coordinates of a mapped grid ([vertex][dim], lexicographic, x fastest), or null for the
+  // equidistant grid of lo, hi and n
+  const double* xv = nullptr;
 
   Grid() = default;
   Grid(int d, const long* nn, const double* l, const double* u, bool smplx, bool per)
@@ -274,6 +277,11 @@ struct Grid {
   long vertex_index(const long* vi) const { return vi[0] + vn[0] * (vi[1] + vn[1] * vi[2]); }
   Vec3 vertex_coord(const long* vi) const {
     Vec3 x{0, 0, 0};
+    if (xv) {
+      const long v = vertex_index(vi);
+      for (int i = 0; i < dim; ++i) x[i] = xv[v * dim + i];
+      return x;
+    }
     for (int i = 0; i < dim; ++i) x[i] = lo[i] + vi[i] * h[i];
     return x;
   }

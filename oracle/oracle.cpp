@@ -40,7 +40,11 @@ extern "C" int orc_max_threads(void) {
 
 namespace {
 
-Grid make_grid(const orc_grid* g) { return Grid(g->dim, g->n, g->lo, g->hi, g->simplex != 0, g->periodic != 0); }
+Grid make_grid(const orc_grid* g) {
+  Grid out(g->dim, g->n, g->lo, g->hi, g->simplex != 0, g->periodic != 0);
+  out.xv = g->vertices;
+  return out;
+}
 
 // ------------------------------------------------------------------- spaces ---
 // Mappers: ContinuousMapper (spaces/mapper/continuous.hh:117-182): DoF = MCMG offset of the
@@ -643,6 +647,16 @@ int num_colours(const Grid& g) { return (1 << g.dim) * g.nsub; }
 std::vector<int64_t> dirichlet_dofs(const Grid& g, const Space& s) {
   std::vector<char> flag(s.size, 0);
   long gv[8];
+  if (g.xv) {  // mapped grid (order-1 continuous spaces): the vertices of the index boundary
+    std::vector<int64_t> out;
+    for (long v = 0; v < g.nvert; ++v) {
+      const long vi[3] = {v % g.vn[0], (v / g.vn[0]) % g.vn[1], v / (g.vn[0] * g.vn[1])};
+      bool b = false;
+      for (int k = 0; k < g.dim; ++k) b = b || vi[k] == 0 || vi[k] == g.n[k];
+      if (b) out.push_back(v);
+    }
+    return out;
+  }
   for (long e = 0; e < g.nelem; ++e) {
     Geometry geo = element_geometry(g, e, gv);
     for (int i = 0; i < s.lsize; ++i) {

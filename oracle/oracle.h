@@ -25,6 +25,7 @@ typedef struct orc_grid {
   double hi[3];     /* upper-right corner */
   int simplex;      /* 0: cubes (YaspGrid), 1: Kuhn simplices */
   int periodic;     /* periodic in every axis (cube grids, FV only) */
+  const double* vertices; /* mapped grid: vertex coordinates [vertex][dim] (x fastest), or NULL */
 } orc_grid;
 
 enum { ORC_CG = 0, ORC_DG = 1, ORC_FV = 2 };
