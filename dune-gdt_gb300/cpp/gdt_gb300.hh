@@ -110,8 +110,20 @@ class CubeGrid {
   }
   gdt_grid handle() const { return handle_.get(); }
   int64_t num_elements() const { return gdt_grid_num_elements(handle()); }
+  // A mapped grid (a Dune::GeometryGrid over this grid's topology): moves every vertex to `coords`
+  // ([num_vertices * d], vertices lexicographic with x fastest). Call before making spaces; the
+  // continuous order-1 Laplace stiffness and load vector (data per element or constant) then form each
+  // element's geometry on the device.
+  void set_vertices(const std::vector<double>& coords) {
+    if (coords.size() != size_t(gdt_grid_num_vertices(handle())) * d)
+      throw Exception(GDT_ESHAPE, "set_vertices: expected num_vertices * d coordinates");
+    check(gdt_grid_set_vertices(handle(), coords.data()), nullptr, "set_vertices");
+    mapped_ = true;
+  }
+  bool mapped() const { return mapped_; }
   // element barycentre (elements numbered cube * d! + simplex, cubes lexicographic, x fastest)
   FieldVector<d> barycentre(int64_t e) const {
+    if (mapped_) throw Exception(GDT_EUNSUPPORTED, "points of a mapped grid: data per element or constant");
     const int nsub = simplex_ ? (d == 2 ? 2 : d == 3 ? 6 : 1) : 1;
     int64_t c = e / nsub;
     FieldVector<d> x;
@@ -134,6 +146,7 @@ class CubeGrid {
   // J_e the cube's scaling (times the Kuhn simplex's corner matrix: column m is the sum of the unit
   // vectors of the first m + 1 axes of its permutation, permutations in std::next_permutation order)
   FieldVector<d> global(int64_t e, const double* xref) const {
+    if (mapped_) throw Exception(GDT_EUNSUPPORTED, "points of a mapped grid: data per element or constant");
     const int nsub = simplex_ ? (d == 2 ? 2 : d == 3 ? 6 : 1) : 1;
     int64_t c = e / nsub;
     std::array<double, d> loc{};
@@ -160,6 +173,7 @@ class CubeGrid {
   FieldVector<d> lower_, upper_;
   std::array<int64_t, d> cells_;
   bool simplex_;
+  bool mapped_ = false;
   std::shared_ptr<gdt_grid_s> handle_;
 };
 

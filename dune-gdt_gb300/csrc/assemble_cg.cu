@@ -201,15 +201,22 @@ __global__ void __launch_bounds__(256) assemble_cg_rows(GridDesc g, const int* _
   finish_row<DIM, SIMPLEX>(g, v, vi, acc, b, rp, val, rhs, dirichlet, gD, gD_const);
 }
 
-// The same row gather on a mapped grid (vertex coordinates g.xv): every element's contribution to the
-// row is formed from its own vertices, as DefaultGlobalBasis::jacobians does from the element geometry
-// (spaces/basis/default.hh:152-175), with the quadrature of LocalElementIntegralBilinearForm at the
-// integrand's order (local/bilinear-forms/integrals.hh:97-134):
-// - simplices (P1, affine): constant gradients grad phi_j = J^{-T} grad phi_hat_j; the stiffness
-//   kappa |det J| / d! grad phi_i . grad phi_j and the load f |det J| / (d! (d + 1)) are exact;
-// - cubes (Q1, multilinear map): the stiffness at the 2^d Gauss points of order 2 (two per axis,
-//   J, J^{-1} and |det J| at each point) and the load of a source per element at the one-point rule of
-//   order 1 (the element centre: phi_i = 2^{-d} there).
+// Mapped grids (vertex coordinates g.xv) in two passes, so that each element's geometry is formed once:
+// 1. mapped_cell_tables: one thread per cube forms J, J^{-1} and |det J| of its elements from its own
+//    corners, as DefaultGlobalBasis::jacobians does from the element geometry
+//    (spaces/basis/default.hh:152-175), with the quadrature of LocalElementIntegralBilinearForm at the
+//    integrand's order (local/bilinear-forms/integrals.hh:97-134), and writes the cube's local stiffness
+//    (kappa included; entries (i, j), i <= j, of its 2^d corners, entry-major so that a warp's stores are
+//    contiguous) and its load per corner:
+//    - simplices (P1, affine): grad phi_j = J^{-T} grad phi_hat_j is constant; the stiffness
+//      kappa |det J| / d! grad phi_i . grad phi_j and the load f |det J| / (d! (d + 1)) are exact, and
+//      the d! simplices of a cube are summed into its corner pairs (only corners whose bit sets are
+//      nested share a simplex);
+//    - cubes (Q1, multilinear map): the stiffness at the 2^d Gauss points of order 2 (two per axis, J,
+//      J^{-1} and |det J| at each point), the load of a source per element at the one-point rule of
+//      order 1 (the element centre: phi_i = 2^{-d} there), the same for every corner.
+// 2. assemble_cg_rows_tabled: the output-stationary row gather of the equidistant kernel, reading the
+//    tables of the <= 2^d cubes around the row's vertex instead of per-type constants.
 template <int DIM>
 __device__ __forceinline__ double inv_det(const double (&J)[DIM][DIM], double (&Ji)[DIM][DIM]) {
   if constexpr (DIM == 1) {
@@ -217,118 +224,135 @@ __device__ __forceinline__ double inv_det(const double (&J)[DIM][DIM], double (&
     return J[0][0];
   } else if constexpr (DIM == 2) {
     const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-    Ji[0][0] = J[1][1] / det;
-    Ji[0][1] = -J[0][1] / det;
-    Ji[1][0] = -J[1][0] / det;
-    Ji[1][1] = J[0][0] / det;
+    const double r = 1.0 / det;
+    Ji[0][0] = J[1][1] * r;
+    Ji[0][1] = -J[0][1] * r;
+    Ji[1][0] = -J[1][0] * r;
+    Ji[1][1] = J[0][0] * r;
     return det;
   } else {
-    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
-                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-    Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
-    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
-    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
-    Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
-    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
-    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
-    Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
-    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
-    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1], c01 = J[0][2] * J[2][1] - J[0][1] * J[2][2],
+                 c02 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    const double det = J[0][0] * c00 + J[1][0] * c01 + J[2][0] * c02;
+    const double r = 1.0 / det;
+    Ji[0][0] = c00 * r;
+    Ji[0][1] = c01 * r;
+    Ji[0][2] = c02 * r;
+    Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * r;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+    Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * r;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
     return det;
   }
 }
 
+// entry of corner pair (i, j) in the cube table: the upper triangle, row by row
+__host__ __device__ constexpr int pair_entry(int nc, int i, int j) {
+  return i <= j ? i * nc - i * (i - 1) / 2 + (j - i) : j * nc - j * (j - 1) / 2 + (i - j);
+}
+// do cube corners i and j share an element? (all pairs of a cube; nested bit sets for the Kuhn split)
+__host__ __device__ constexpr bool pair_shared(bool simplex, int i, int j) {
+  return !simplex || (i & j) == i || (i & j) == j;
+}
+
 template <int DIM, bool SIMPLEX>
-__global__ void __launch_bounds__(128) assemble_cg_rows_mapped(GridDesc g, const int* __restrict__ rp,
-                                                               double* __restrict__ val, double* __restrict__ rhs,
-                                                               const double* __restrict__ kappa, double kappa_const,
-                                                               const double* __restrict__ force, double force_const,
-                                                               int dirichlet, const double* __restrict__ gD,
-                                                               double gD_const) {
-  constexpr int NS = pow3(DIM), NSUB = num_sub(DIM, SIMPLEX), NLOC = num_local(DIM, SIMPLEX), NC = 1 << DIM;
-  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (v >= g.nvert) return;
-  long long vi[3];
-  vertex_multi(g, v, vi);
-  double acc[NS];
+__global__ void __launch_bounds__(128) mapped_cell_tables(GridDesc g, double* __restrict__ tm, double* __restrict__ tb,
+                                                          const double* __restrict__ kappa, double kappa_const,
+                                                          const double* __restrict__ force, double force_const) {
+  constexpr int NC = 1 << DIM, NP = NC * (NC + 1) / 2, NSUB = num_sub(DIM, SIMPLEX), NLOC = num_local(DIM, SIMPLEX);
+  const long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (cell >= g.ncells) return;
+  const long long nc = g.ncells;
+  long long ci[3] = {0, 0, 0};
+  cell_multi(g, cell, ci);
+  // the cube's corner coordinates, corner c at bits c
+  double X[NC][DIM];
 #pragma unroll
-  for (int k = 0; k < NS; ++k) acc[k] = 0.0;
-  double b = 0.0;
-  double fact = 1.0;  // d!
+  for (int c = 0; c < NC; ++c) {
+    long long w[3] = {ci[0], ci[1], ci[2]};
 #pragma unroll
-  for (int a = 2; a <= DIM; ++a) fact *= a;
+    for (int a = 0; a < DIM; ++a) w[a] += (c >> a) & 1;
+    const long long wv = w[0] + g.vn[0] * (w[1] + g.vn[1] * w[2]);
 #pragma unroll
-  for (int cv = 0; cv < NC; ++cv) {
-    long long ci[3] = {0, 0, 0};
-    bool inside = true;
+    for (int a = 0; a < DIM; ++a) X[c][a] = g.xv[wv * DIM + a];
+  }
+  if constexpr (SIMPLEX) {
+    double fact = 1.0;  // d!
 #pragma unroll
-    for (int a = 0; a < DIM; ++a) {
-      ci[a] = vi[a] - ((cv >> a) & 1);
-      inside = inside && ci[a] >= 0 && ci[a] < g.n[a];
-    }
-    if (!inside) continue;
-    const long long cell = cell_index(g, ci);
-    // the cell's corner coordinates, corner c at bits c
-    double X[NC][DIM];
+    for (int a = 2; a <= DIM; ++a) fact *= a;
+    double A[NP], B[NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      long long w[3] = {ci[0], ci[1], ci[2]};
+    for (int k = 0; k < NP; ++k) A[k] = 0.0;
 #pragma unroll
-      for (int a = 0; a < DIM; ++a) w[a] += (c >> a) & 1;
-      const long long wv = w[0] + g.vn[0] * (w[1] + g.vn[1] * w[2]);
+    for (int c = 0; c < NC; ++c) B[c] = 0.0;
 #pragma unroll
-      for (int a = 0; a < DIM; ++a) X[c][a] = g.xv[wv * DIM + a];
-    }
-    if constexpr (SIMPLEX) {
+    for (int t = 0; t < NSUB; ++t) {
+      const long long e = cell * NSUB + t;
+      // J[a][k] = x_{k+1} - x_0 (local vertices in Kuhn order)
+      double J[DIM][DIM], Ji[DIM][DIM];
+      const int c0 = local_corner(DIM, true, t, 0);
 #pragma unroll
-      for (int t = 0; t < NSUB; ++t) {
+      for (int k = 0; k < DIM; ++k)
 #pragma unroll
-        for (int li = 0; li < NLOC; ++li) {
-          if (local_corner(DIM, true, t, li) != cv) continue;
-          const long long e = cell * NSUB + t;
-          const double kap = kappa ? kappa[e] : kappa_const;
-          // J[a][k] = x_{k+1} - x_0 (local vertices in Kuhn order)
-          double J[DIM][DIM], Ji[DIM][DIM];
-          const int c0 = local_corner(DIM, true, t, 0);
+        for (int a = 0; a < DIM; ++a) J[a][k] = X[local_corner(DIM, true, t, k + 1)][a] - X[c0][a];
+      const double vol = fabs(inv_det<DIM>(J, Ji)) / fact;
+      if (tm) {
+        // grad phi_j = row j-1 of J^{-1} (j >= 1); grad phi_0 = minus the sum of the others
+        double G[NLOC][DIM];
 #pragma unroll
-          for (int k = 0; k < DIM; ++k)
+        for (int a = 0; a < DIM; ++a) {
+          double s0 = 0.0;
 #pragma unroll
-            for (int a = 0; a < DIM; ++a) J[a][k] = X[local_corner(DIM, true, t, k + 1)][a] - X[c0][a];
-          const double vol = fabs(inv_det<DIM>(J, Ji)) / fact;
-          // grad phi_j = J^{-T} e_{j-1} (j >= 1): column j-1 of J^{-T}, i.e. row j-1 of J^{-1};
-          // grad phi_0 = -sum of the others
-          double G[NLOC][DIM];
-#pragma unroll
-          for (int a = 0; a < DIM; ++a) {
-            double s0 = 0.0;
-#pragma unroll
-            for (int j = 1; j < NLOC; ++j) {
-              G[j][a] = Ji[j - 1][a];
-              s0 += Ji[j - 1][a];
-            }
-            G[0][a] = -s0;
+          for (int j = 1; j < NLOC; ++j) {
+            G[j][a] = Ji[j - 1][a];
+            s0 += Ji[j - 1][a];
           }
+          G[0][a] = -s0;
+        }
+        const double kv = (kappa ? kappa[e] : kappa_const) * vol;
 #pragma unroll
-          for (int lj = 0; lj < NLOC; ++lj) {
+        for (int li = 0; li < NLOC; ++li)
+#pragma unroll
+          for (int lj = li; lj < NLOC; ++lj) {
             double d = 0.0;
 #pragma unroll
-            for (int a = 0; a < DIM; ++a) d += G[lj][a] * G[li][a];
-            acc[slot_between(DIM, cv, local_corner(DIM, true, t, lj))] += kap * d * vol;
+            for (int a = 0; a < DIM; ++a) d += G[li][a] * G[lj][a];
+            A[pair_entry(NC, local_corner(DIM, true, t, li), local_corner(DIM, true, t, lj))] += kv * d;
           }
-          if (rhs) b += (force ? force[e] : force_const) * vol / double(DIM + 1);
-        }
       }
-    } else {
+      if (tb) {
+        const double bl = (force ? force[e] : force_const) * vol / double(DIM + 1);
+#pragma unroll
+        for (int li = 0; li < NLOC; ++li) B[local_corner(DIM, true, t, li)] += bl;
+      }
+    }
+    if (tm) {
+#pragma unroll
+      for (int i = 0; i < NC; ++i)
+#pragma unroll
+        for (int j = i; j < NC; ++j)
+          if (pair_shared(true, i, j)) tm[pair_entry(NC, i, j) * nc + cell] = A[pair_entry(NC, i, j)];
+    }
+    if (tb) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) tb[c * nc + cell] = B[c];
+    }
+  } else {
+    if (tm) {
       const double kap = kappa ? kappa[cell] : kappa_const;
-      const double gp[2] = {0.5 - 0.5 / sqrt(3.0), 0.5 + 0.5 / sqrt(3.0)};
-      const double wq = 1.0 / double(NC);  // Gauss weights 1/2 per axis
+      // Gauss points of order 2 on [0, 1]: (3 -+ sqrt 3) / 6, weights 1/2 per axis
+      constexpr double gp0 = 0.21132486540518711775, gp1 = 0.78867513459481288225;
+      double A[NP];
+#pragma unroll
+      for (int k = 0; k < NP; ++k) A[k] = 0.0;
 #pragma unroll
       for (int q = 0; q < NC; ++q) {
         double xh[DIM];
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) xh[a] = gp[(q >> a) & 1];
-        // reference gradients of the bilinear/trilinear shape functions at xh
+        for (int a = 0; a < DIM; ++a) xh[a] = ((q >> a) & 1) ? gp1 : gp0;
+        // reference gradients of the multilinear shape functions at xh (constants after unrolling)
         double gr[NC][DIM];
 #pragma unroll
         for (int c = 0; c < NC; ++c)
@@ -350,44 +374,92 @@ __global__ void __launch_bounds__(128) assemble_cg_rows_mapped(GridDesc g, const
             for (int c = 0; c < NC; ++c) sj += gr[c][k] * X[c][a];
             J[a][k] = sj;
           }
-        const double factor = fabs(inv_det<DIM>(J, Ji)) * wq;
-        // grad phi_c = J^{-T} grad_hat phi_c: component a = sum_k Ji[k][a] gr[c][k]
-        double gi[DIM];
+        const double factor = kap * fabs(inv_det<DIM>(J, Ji)) / double(NC);
+        // grad phi_i . grad phi_j = gr_i^T (J^{-1} J^{-T}) gr_j: M = factor J^{-1} J^{-T} (symmetric)
+        double M[DIM][DIM];
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) {
-          double sg = 0.0;
+        for (int k = 0; k < DIM; ++k)
 #pragma unroll
-          for (int k = 0; k < DIM; ++k) sg += Ji[k][a] * gr[cv][k];
-          gi[a] = sg;
-        }
+          for (int l = k; l < DIM; ++l) {
+            double s = 0.0;
 #pragma unroll
-        for (int lj = 0; lj < NC; ++lj) {
-          double d = 0.0;
-#pragma unroll
-          for (int a = 0; a < DIM; ++a) {
-            double sg = 0.0;
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) sg += Ji[k][a] * gr[lj][k];
-            d += sg * gi[a];
+            for (int a = 0; a < DIM; ++a) s += Ji[k][a] * Ji[l][a];
+            M[k][l] = s * factor;
+            M[l][k] = M[k][l];
           }
-          acc[slot_between(DIM, cv, lj)] += kap * d * factor;
-        }
-      }
-      if (rhs) {
-        // one-point rule at the centre: |det J(1/2, ...)|, phi = 2^{-d}, weight 1
-        double J[DIM][DIM], Ji[DIM][DIM];
 #pragma unroll
-        for (int a = 0; a < DIM; ++a)
+        for (int i = 0; i < NC; ++i) {
+          double hi[DIM];
 #pragma unroll
           for (int k = 0; k < DIM; ++k) {
-            double sj = 0.0;
+            double s = 0.0;
 #pragma unroll
-            for (int c = 0; c < NC; ++c) sj += (((c >> k) & 1) ? 1.0 : -1.0) * X[c][a];
-            J[a][k] = sj / double(NC / 2);
+            for (int l = 0; l < DIM; ++l) s += M[k][l] * gr[i][l];
+            hi[k] = s;
           }
-        b += (force ? force[cell] : force_const) * fabs(inv_det<DIM>(J, Ji)) / double(NC);
+#pragma unroll
+          for (int j = i; j < NC; ++j) {
+            double d = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) d += gr[j][k] * hi[k];
+            A[pair_entry(NC, i, j)] += d;
+          }
+        }
       }
+#pragma unroll
+      for (int k = 0; k < NP; ++k) tm[k * nc + cell] = A[k];
     }
+    if (tb) {
+      // one-point rule at the centre: |det J(1/2, ...)| f, phi = 2^{-d}, weight 1
+      double J[DIM][DIM], Ji[DIM][DIM];
+#pragma unroll
+      for (int a = 0; a < DIM; ++a)
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          double sj = 0.0;
+#pragma unroll
+          for (int c = 0; c < NC; ++c) sj += (((c >> k) & 1) ? 1.0 : -1.0) * X[c][a];
+          J[a][k] = sj / double(NC / 2);
+        }
+      tb[cell] = (force ? force[cell] : force_const) * fabs(inv_det<DIM>(J, Ji)) / double(NC);
+    }
+  }
+}
+
+template <int DIM, bool SIMPLEX>
+__global__ void __launch_bounds__(256) assemble_cg_rows_tabled(GridDesc g, const int* __restrict__ rp,
+                                                               double* __restrict__ val, double* __restrict__ rhs,
+                                                               const double* __restrict__ tm,
+                                                               const double* __restrict__ tb, int dirichlet,
+                                                               const double* __restrict__ gD, double gD_const) {
+  constexpr int NS = pow3(DIM), NC = 1 << DIM;
+  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (v >= g.nvert) return;
+  const long long nc = g.ncells;
+  long long vi[3];
+  vertex_multi(g, v, vi);
+  double acc[NS];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) acc[k] = 0.0;
+  double b = 0.0;
+#pragma unroll
+  for (int cv = 0; cv < NC; ++cv) {
+    // v is corner cv of cell vi - bits(cv)
+    long long ci[3] = {0, 0, 0};
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      ci[a] = vi[a] - ((cv >> a) & 1);
+      inside = inside && ci[a] >= 0 && ci[a] < g.n[a];
+    }
+    if (!inside) continue;
+    const long long cell = cell_index(g, ci);
+    if (val) {
+#pragma unroll
+      for (int lj = 0; lj < NC; ++lj)
+        if (pair_shared(SIMPLEX, cv, lj)) acc[slot_between(DIM, cv, lj)] += tm[pair_entry(NC, cv, lj) * nc + cell];
+    }
+    if (rhs) b += tb[(SIMPLEX ? cv : 0) * nc + cell];
   }
   finish_row<DIM, SIMPLEX>(g, v, vi, acc, b, rp, val, rhs, dirichlet, gD, gD_const);
 }
@@ -491,22 +563,36 @@ gdt_status mf_capture(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d
   return check_launch(ctx, "mf_capture");
 }
 
-// mapped grids: the row gather that forms each element's geometry
+// mapped grids: the cube tables (stiffness and/or load), then the row gather over them
 gdt_status assemble_cg_mapped(gdt_context ctx, const GridDesc& g, const int* rp, double* val,
                               const gdt_diffusion_desc* d, double* rhs, const double* gD, double gD_const) {
-  const int th = 128;
-  const int bl = grid_blocks(g.nvert, th);
+  const int nc = 1 << g.dim, np = nc * (nc + 1) / 2, nb = g.simplex ? nc : 1;
   cudaStream_t s = ctx->stream;
-#define GDT_LAUNCH_MAPPED(D, S)                                                                              \
-  assemble_cg_rows_mapped<D, S><<<bl, th, 0, s>>>(g, rp, val, rhs, d->kappa, d->kappa_const, d->force,        \
-                                                  d->force_const, d->dirichlet, gD, gD_const)
+  double* tm = nullptr;
+  double* tb = nullptr;
+  if (val) GDT_TRY_CUDA(ctx, cudaMallocAsync(&tm, sizeof(double) * size_t(np) * g.ncells, s));
+  if (rhs && cudaMallocAsync(&tb, sizeof(double) * size_t(nb) * g.ncells, s) != cudaSuccess) {
+    cudaGetLastError();
+    if (tm) cudaFreeAsync(tm, s);
+    return fail(ctx, GDT_ENOMEM, "mapped assembly tables");
+  }
+  const int bl1 = grid_blocks(g.ncells, 128), bl2 = grid_blocks(g.nvert, 256);
+#define GDT_LAUNCH_MAPPED(D, S)                                                                                \
+  do {                                                                                                          \
+    mapped_cell_tables<D, S><<<bl1, 128, 0, s>>>(g, tm, tb, d->kappa, d->kappa_const, d->force, d->force_const); \
+    assemble_cg_rows_tabled<D, S><<<bl2, 256, 0, s>>>(g, rp, val, rhs, tm, tb, d->dirichlet, gD, gD_const);      \
+  } while (0)
   if (g.dim == 1) GDT_LAUNCH_MAPPED(1, false);
   else if (g.dim == 2 && !g.simplex) GDT_LAUNCH_MAPPED(2, false);
   else if (g.dim == 2) GDT_LAUNCH_MAPPED(2, true);
   else if (!g.simplex) GDT_LAUNCH_MAPPED(3, false);
   else GDT_LAUNCH_MAPPED(3, true);
 #undef GDT_LAUNCH_MAPPED
-  return check_launch(ctx, "assemble_cg_rows_mapped");
+  ctx->launches++;  // the second of the two launches; check_launch counts the other
+  const gdt_status st = check_launch(ctx, "assemble_cg mapped");
+  if (tm) cudaFreeAsync(tm, s);
+  if (tb) cudaFreeAsync(tb, s);
+  return st;
 }
 
 gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs) {
