@@ -37,9 +37,10 @@ namespace gdt {
 namespace {
 
 constexpr int TH = 256;
-// threads per block of the persistent kernel (one block per SM): 768 at 80 registers, no spills.
-// 1024 at 64 registers (some spills) measured slower in the solver (28.6 against 27.8 us per
-// iteration at 128^3).
+// threads per block of the persistent kernel (one block per SM): 768 at 80 registers (the column's
+// two-plane-ahead loads spill 48-84 bytes to L1; 26.8 us per iteration at 128^3). 640 threads at 96
+// registers without spills measured slower (fewer columns in flight), as did 1024 threads at 64
+// registers with one-plane-ahead loads (28.6 against 27.8 us).
 constexpr int MT = 768;
 // residual replacement when the iterated residual's square dropped by this factor since the last one
 // (10x in the residual norm; 100x saved 5 of 11 replacements at 128^3 but cost 10 % more iterations)
@@ -103,8 +104,9 @@ __device__ __forceinline__ float cross_of(const float (&f)[8], const U4& u) {
 
 // w = A zb over rows z0 .. z1 - 1 of vertex column (x, y); accumulates r.z, z.w and r.r of those rows.
 // Row z is the sum over the cell layers z - 1 and z of their pairs with the planes they touch: the
-// layer z - 1 pairs (with planes z - 1 and z) are summed one step ahead into `carry`, so a step loads
-// plane z + 1 and layer z and keeps two planes in registers.
+// layer z - 1 pairs (with planes z - 1 and z) are summed one step ahead into `carry`. The loads run two
+// planes ahead: step z computes with plane z + 1 and layer z, loaded by step z - 1, while the loads of
+// plane z + 2, layer z + 1 and r of row z + 1 are in flight, so a step does not wait a full L2 latency.
 template <bool DIR>
 // (w restrict: its stores do not alias the loads, so the next plane's loads may be issued before this
 // plane's store; zb and r are read with plain coherent loads, never the read-only path: other blocks
@@ -127,34 +129,47 @@ __device__ __forceinline__ void mf3_column(const Mf3& g, int x, int y, int z0, i
 #pragma unroll
     for (int k = 0; k < 9; ++k) v[k] = q[(k % 3 - 1) + (k / 3 - 1) * PX];
   };
-  // the 2 x 2 coefficients of cell layer cz, their row sums over y (a = 0, 1), over x (b = 0, 1) and total
-  auto load_layer = [&](int cz, float(&k)[4], float(&sm)[5]) {
+  // the 2 x 2 coefficients of cell layer cz
+  auto load_layer = [&](int cz, float(&k)[4]) {
     const float* q = kc + cz * CPXY;
 #pragma unroll
     for (int j = 0; j < 4; ++j) k[j] = __ldg(q + (j & 1) + (j >> 1) * CPX);
+  };
+  // their row sums over y (a = 0, 1), over x (b = 0, 1) and total
+  auto layer_sums = [](const float(&k)[4], float(&sm)[5]) {
     sm[0] = k[0] + k[2];
     sm[1] = k[1] + k[3];
     sm[2] = k[0] + k[1];
     sm[3] = k[2] + k[3];
     sm[4] = sm[0] + sm[1];
   };
-  float P[2][9], kl[4], sl[5];
-  float carry;
+  float P[3][9], K[2][4];
+  float carry, rnext;
   {
-    float pm[9];
+    float pm[9], km[4], sm[5];
     load_plane(z0 - 1, pm);
     load_plane(z0, P[0]);
-    load_layer(z0 - 1, kl, sl);
-    carry = cross_of(f, plane_layer(pm, kl, sl)) + same_of(f, plane_layer(P[0], kl, sl));
+    load_layer(z0 - 1, km);
+    load_plane(z0 + 1, P[1]);  // z0 < z1 <= nz: at most the padding plane nz
+    load_layer(z0, K[0]);
+    rnext = rc[z0 * PXY];
+    layer_sums(km, sm);
+    carry = cross_of(f, plane_layer(pm, km, sm)) + same_of(f, plane_layer(P[0], km, sm));
   }
   auto step = [&](auto ph, int z) {
     constexpr int PH = decltype(ph)::value;
-    float(&pc)[9] = P[PH];
-    float(&pn)[9] = P[PH ^ 1];
-    load_plane(z + 1, pn);
-    load_layer(z, kl, sl);
+    const float(&pc)[9] = P[PH % 3];
+    const float(&pn)[9] = P[(PH + 1) % 3];
+    const float(&kl)[4] = K[PH % 2];
+    const float rv = rnext;
+    if (z + 1 < z1) {  // the next step's operands: plane z + 2 <= z1 <= nz, layer z + 1 <= nz - 1
+      load_plane(z + 2, P[(PH + 2) % 3]);
+      load_layer(z + 1, K[(PH + 1) % 2]);
+      rnext = rc[(z + 1) * PXY];
+    }
+    float sl[5];
+    layer_sums(kl, sl);
     const U4 uc = plane_layer(pc, kl, sl), un = plane_layer(pn, kl, sl);
-    const float rv = rc[z * PXY];
     float wv = carry + (same_of(f, uc) + cross_of(f, un));
     carry = cross_of(f, uc) + same_of(f, un);
     float zv = pc[4];
@@ -168,11 +183,19 @@ __device__ __forceinline__ void mf3_column(const Mf3& g, int x, int y, int z0, i
     rr = fmaf(rv, rv, rr);
   };
   int z = z0;
-  for (; z + 2 <= z1; z += 2) {
+  for (; z + 6 <= z1; z += 6) {
     step(Ph<0>{}, z);
     step(Ph<1>{}, z + 1);
+    step(Ph<2>{}, z + 2);
+    step(Ph<3>{}, z + 3);
+    step(Ph<4>{}, z + 4);
+    step(Ph<5>{}, z + 5);
   }
-  if (z < z1) step(Ph<0>{}, z);
+  if (z < z1) step(Ph<0>{}, z++);
+  if (z < z1) step(Ph<1>{}, z++);
+  if (z < z1) step(Ph<2>{}, z++);
+  if (z < z1) step(Ph<3>{}, z++);
+  if (z < z1) step(Ph<4>{}, z++);
 }
 
 // the operator pass over the grid's (column, z chunk) items, grid-stride
