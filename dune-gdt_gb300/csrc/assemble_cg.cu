@@ -257,6 +257,157 @@ __host__ __device__ constexpr bool pair_shared(bool simplex, int i, int j) {
   return !simplex || (i & j) == i || (i & j) == j;
 }
 
+// 1D factors of the trilinear shape functions at the two Gauss points g_0, g_1 of order 2 on [0, 1]
+// ((3 -+ sqrt 3) / 6): ell_x(g_q) = 1 - g_q for x = 0, g_q for x = 1; q1_pair(e, q) the product of two
+// of them by pair class e = 0: (0, 0), 1: (0, 1) or (1, 0), 2: (1, 1)
+constexpr double kGauss0 = 0.21132486540518711775, kGauss1 = 0.78867513459481288225;
+__host__ __device__ constexpr double q1_ell(int x, int q) {
+  return x == 0 ? 1.0 - (q == 0 ? kGauss0 : kGauss1) : (q == 0 ? kGauss0 : kGauss1);
+}
+__host__ __device__ constexpr double q1_pair(int e, int q) {
+  return e == 0 ? q1_ell(0, q) * q1_ell(0, q) : e == 1 ? q1_ell(0, q) * q1_ell(1, q) : q1_ell(1, q) * q1_ell(1, q);
+}
+__host__ __device__ constexpr int q1_class(int x, int y) { return x + y; }
+__host__ __device__ constexpr double q1_sign(int x) { return x ? 1.0 : -1.0; }
+// the other two axes of axis k, ascending
+__host__ __device__ constexpr int q1_other(int k, int m) { return k == 0 ? 1 + m : (k == 1 ? 2 * m : m); }
+
+// Local Q1 stiffness of a trilinear hexahedron (corners X, coefficient kap) in sum-factorised form,
+// written as the upper triangle of its corner pairs to tm (entry-major, stride nc). The same integral
+// as the direct 8-point loop (2 x 2 x 2 Gauss points, J, J^{-1} and |det J| at each) in about half the
+// FP64 operations:
+//   M_q = kap w |det J| J^{-1} J^{-T} = kap w adj(J) adj(J)^T / |det J| (w = 1/8) at every point q;
+//   A_ij = sum_q sum_ab M_q[a][b] d_a phi_i(q) d_b phi_j(q), with d_a phi_i = s(i_a) prod_{k != a}
+//   ell_{i_k}: the diagonal terms a = b need sum over q_a of M_q[a][a] against the pair classes of the
+//   two other axes (T_a, 3 x 3 values), the mixed terms a < b the sums W_ab[x][y][e] of M_q[a][b]
+//   ell_x(q_a) ell_y(q_b) pair_e(q_c) (2 x 2 x 3 values, contracted one axis at a time), and
+//   A_ij = sum_a s(i_a) s(j_a) T_a[e_b][e_c] + sum_{a<b} (s(i_a) s(j_b) W_ab[j_a][i_b][e_c] +
+//   s(i_b) s(j_a) W_ab[i_a][j_b][e_c]).
+// Column k of J at a Gauss point depends only on the other two coordinates, so the 12 distinct
+// columns are formed once from the 12 edge vectors.
+__device__ __forceinline__ void q1_hex_stiffness(const double (&X)[8][3], double kap, double* __restrict__ tm,
+                                                 long long nc, long long cell) {
+  double Jc[3][2][2][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int o1 = q1_other(k, 0), o2 = q1_other(k, 1);
+#pragma unroll
+    for (int q1 = 0; q1 < 2; ++q1)
+#pragma unroll
+      for (int q2 = 0; q2 < 2; ++q2)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) Jc[k][q1][q2][a] = 0.0;
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int c0 = (u << o1) | (v << o2), c1 = c0 | (1 << k);
+        double E[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) E[a] = X[c1][a] - X[c0][a];
+#pragma unroll
+        for (int q1 = 0; q1 < 2; ++q1)
+#pragma unroll
+          for (int q2 = 0; q2 < 2; ++q2) {
+            const double wgt = q1_ell(u, q1) * q1_ell(v, q2);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) Jc[k][q1][q2][a] = fma(wgt, E[a], Jc[k][q1][q2][a]);
+          }
+      }
+  }
+  // M_q: components 00, 11, 22, 01, 02, 12 at point q = q0 | q1 << 1 | q2 << 2
+  double Mq[6][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int qb[3] = {q & 1, (q >> 1) & 1, (q >> 2) & 1};
+    double J[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) J[a][k] = Jc[k][qb[q1_other(k, 0)]][qb[q1_other(k, 1)]][a];
+    double ad[3][3];  // adj(J) = det J * J^{-1}
+    ad[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    ad[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    ad[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    ad[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    ad[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    ad[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    ad[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    ad[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    ad[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const double det = J[0][0] * ad[0][0] + J[0][1] * ad[1][0] + J[0][2] * ad[2][0];
+    const double f = (0.125 * kap) / fabs(det);
+    constexpr int ka[6] = {0, 1, 2, 0, 0, 1}, kb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int m = 0; m < 6; ++m)
+      Mq[m][q] = f * fma(ad[ka[m]][0], ad[kb[m]][0], fma(ad[ka[m]][1], ad[kb[m]][1], ad[ka[m]][2] * ad[kb[m]][2]));
+  }
+  // T_a[e_b][e_c] (a = b terms)
+  double T[3][3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int b = q1_other(a, 0), c = q1_other(a, 1);
+    double mm[2][2];
+#pragma unroll
+    for (int qb = 0; qb < 2; ++qb)
+#pragma unroll
+      for (int qc = 0; qc < 2; ++qc) mm[qb][qc] = Mq[a][(qb << b) | (qc << c)] + Mq[a][(1 << a) | (qb << b) | (qc << c)];
+#pragma unroll
+    for (int eb = 0; eb < 3; ++eb) {
+      double u[2];
+#pragma unroll
+      for (int qc = 0; qc < 2; ++qc) u[qc] = fma(mm[0][qc], q1_pair(eb, 0), mm[1][qc] * q1_pair(eb, 1));
+#pragma unroll
+      for (int ec = 0; ec < 3; ++ec) T[a][eb][ec] = fma(u[0], q1_pair(ec, 0), u[1] * q1_pair(ec, 1));
+    }
+  }
+  // W_ab[x][y][e_c] (a < b terms), one axis at a time: pair m = 3 (01), 4 (02), 5 (12)
+  double W[3][2][2][3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const int a = m == 2 ? 1 : 0, b = m == 0 ? 1 : 2, c = 3 - a - b;
+    double Y[2][2][2];  // [x][q_b][q_c]
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+      for (int qb = 0; qb < 2; ++qb)
+#pragma unroll
+        for (int qc = 0; qc < 2; ++qc)
+          Y[x][qb][qc] = fma(Mq[3 + m][(qb << b) | (qc << c)], q1_ell(x, 0),
+                             Mq[3 + m][(1 << a) | (qb << b) | (qc << c)] * q1_ell(x, 1));
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+      for (int y = 0; y < 2; ++y) {
+        double Z[2];
+#pragma unroll
+        for (int qc = 0; qc < 2; ++qc) Z[qc] = fma(Y[x][0][qc], q1_ell(y, 0), Y[x][1][qc] * q1_ell(y, 1));
+#pragma unroll
+        for (int e = 0; e < 3; ++e) W[m][x][y][e] = fma(Z[0], q1_pair(e, 0), Z[1] * q1_pair(e, 1));
+      }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = i; j < 8; ++j) {
+      const int bi[3] = {i & 1, (i >> 1) & 1, (i >> 2) & 1}, bj[3] = {j & 1, (j >> 1) & 1, (j >> 2) & 1};
+      double v = 0.0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const int b = q1_other(a, 0), c = q1_other(a, 1);
+        v += q1_sign(bi[a]) * q1_sign(bj[a]) * T[a][q1_class(bi[b], bj[b])][q1_class(bi[c], bj[c])];
+      }
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const int a = m == 2 ? 1 : 0, b = m == 0 ? 1 : 2, c = 3 - a - b;
+        const int e = q1_class(bi[c], bj[c]);
+        v += q1_sign(bi[a]) * q1_sign(bj[b]) * W[m][bj[a]][bi[b]][e];
+        v += q1_sign(bi[b]) * q1_sign(bj[a]) * W[m][bi[a]][bj[b]][e];
+      }
+      tm[pair_entry(8, i, j) * nc + cell] = v;
+    }
+}
+
 template <int DIM, bool SIMPLEX>
 __global__ void __launch_bounds__(128) mapped_cell_tables(GridDesc g, double* __restrict__ tm, double* __restrict__ tb,
                                                           const double* __restrict__ kappa, double kappa_const,
@@ -340,7 +491,9 @@ __global__ void __launch_bounds__(128) mapped_cell_tables(GridDesc g, double* __
       for (int c = 0; c < NC; ++c) tb[c * nc + cell] = B[c];
     }
   } else {
-    if (tm) {
+    if constexpr (DIM == 3) {
+      if (tm) q1_hex_stiffness(X, kappa ? kappa[cell] : kappa_const, tm, nc, cell);
+    } else if (tm) {
       const double kap = kappa ? kappa[cell] : kappa_const;
       // Gauss points of order 2 on [0, 1]: (3 -+ sqrt 3) / 6, weights 1/2 per axis
       constexpr double gp0 = 0.21132486540518711775, gp1 = 0.78867513459481288225;
