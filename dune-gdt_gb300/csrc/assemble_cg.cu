@@ -723,8 +723,8 @@ gdt_status assemble_cg_mapped(gdt_context ctx, const GridDesc& g, const int* rp,
   cudaStream_t s = ctx->stream;
   double* tm = nullptr;
   double* tb = nullptr;
-  if (val) GDT_TRY_CUDA(ctx, cudaMallocAsync(&tm, sizeof(double) * size_t(np) * g.ncells, s));
-  if (rhs && cudaMallocAsync(&tb, sizeof(double) * size_t(nb) * g.ncells, s) != cudaSuccess) {
+  if ((val && cudaMallocAsync(&tm, sizeof(double) * size_t(np) * g.ncells, s) != cudaSuccess) ||
+      (rhs && cudaMallocAsync(&tb, sizeof(double) * size_t(nb) * g.ncells, s) != cudaSuccess)) {
     cudaGetLastError();
     if (tm) cudaFreeAsync(tm, s);
     return fail(ctx, GDT_ENOMEM, "mapped assembly tables");
