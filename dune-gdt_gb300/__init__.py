@@ -17,7 +17,8 @@ from . import replicas
 from ._capi import GdtError
 
 __all__ = [
-    "Context", "default_context", "make_cube_grid", "Grid", "ContinuousLagrangeSpace",
+    "Context", "default_context", "make_cube_grid", "Grid", "make_simplex_mesh", "SimplexMesh",
+    "ContinuousLagrangeSpace",
     "DiscontinuousLagrangeSpace", "FiniteVolumeSpace", "Stencil", "LocalLaplaceIntegrand",
     "LocalElementProductIntegrand", "LocalElementIntegralBilinearForm", "LocalElementIntegralFunctional",
     "LocalLaplaceIPDGInnerCoupling", "LocalLaplaceIPDGDirichletCoupling", "LocalIPDGInnerPenalty",
@@ -167,6 +168,63 @@ class Grid:
         return v
 
 
+class SimplexMesh:
+    """An unstructured simplex mesh: the leaf view of a DUNE simplex grid (ALUGrid, UGGrid, a gmsh
+    import) exported in its index-set order (gdt_grid_create_simplex_mesh). coords [num_vertices, dim]
+    (dim 2 or 3), cells [num_elements, dim + 1] vertex indices; numpy or torch, host or device.
+    Continuous order-1 spaces (DoF = vertex index), their Laplace stiffness and load vector (kappa and
+    source per element or constant), Dirichlet constraints on the boundary vertices (vertices of faces
+    of one element), the solvers and the log-kappa gradient work on it."""
+
+    def __init__(self, coords, cells):
+        import numpy as np
+
+        self.lib = capi.load()
+        if isinstance(coords, torch.Tensor):
+            xk = coords.detach().to(torch.float64).contiguous()
+            xp = xk.data_ptr()
+        else:
+            xk = np.ascontiguousarray(coords, dtype=np.float64)
+            xp = xk.ctypes.data
+        if isinstance(cells, torch.Tensor):
+            ck = cells.detach().to(torch.int64).contiguous()
+            cp = ck.data_ptr()
+        else:
+            ck = np.ascontiguousarray(cells, dtype=np.int64)
+            cp = ck.ctypes.data
+        if len(xk.shape) != 2 or xk.shape[1] not in (2, 3) or len(ck.shape) != 2 or ck.shape[1] != xk.shape[1] + 1:
+            raise ValueError(f"coords [num_vertices, 2 or 3] and cells [num_elements, dim + 1] expected, got "
+                             f"{tuple(xk.shape)} and {tuple(ck.shape)}")
+        self.dimension = int(xk.shape[1])
+        self.simplex, self.periodic = True, False
+        h = C.c_void_p()
+        capi.check(self.lib.gdt_grid_create_simplex_mesh(self.dimension, int(xk.shape[0]), C.c_void_p(xp),
+                                                         int(ck.shape[0]), C.c_void_p(cp), C.byref(h)),
+                   what="make_simplex_mesh")
+        self.handle = h
+        self.vertices = torch.as_tensor(xk).clone()
+        self.cells = torch.as_tensor(ck).clone()
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.gdt_grid_destroy(self.handle)
+        except Exception:
+            pass
+
+    @property
+    def num_elements(self):
+        return int(self.lib.gdt_grid_num_elements(self.handle))
+
+    @property
+    def num_vertices(self):
+        return int(self.lib.gdt_grid_num_vertices(self.handle))
+
+
+def make_simplex_mesh(coords, cells) -> SimplexMesh:
+    return SimplexMesh(coords, cells)
+
+
 def make_cube_grid(lower_left, upper_right, num_elements, simplex=False, periodic=False) -> Grid:
     dim = len(num_elements)
     if not hasattr(lower_left, "__len__"):
@@ -230,6 +288,8 @@ class _Space:
 
         x, _ = self.quadrature(order)
         g = self.grid
+        if getattr(g, "vertices", None) is not None:
+            raise GdtError(capi.EUNSUPPORTED, "quadrature points of mapped grids and simplex meshes")
         d = g.dimension
         device = device or torch.device("cuda", torch.cuda.current_device())
         lo = torch.tensor(g.lower_left, dtype=torch.float64, device=device)

@@ -110,6 +110,7 @@ _SIGNATURES = {
     "gdt_grid_create_cube": (C.c_int, [C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(P)]),
     "gdt_grid_set_vertices": (C.c_int, [P, P]),
+    "gdt_grid_create_simplex_mesh": (C.c_int, [C.c_int, C.c_int64, P, C.c_int64, P, C.POINTER(P)]),
     "gdt_grid_destroy": (C.c_int, [P]),
     "gdt_grid_num_elements": (C.c_int64, [P]),
     "gdt_grid_num_vertices": (C.c_int64, [P]),

@@ -215,7 +215,7 @@ gdt_status gdt_grid_create_cube(int dim, const int64_t* num_elements, const doub
 gdt_status gdt_grid_set_vertices(gdt_grid g, const double* coords) {
   if (!g || !coords) return GDT_EINVAL;
   GridDesc& d = g->d;
-  if (d.periodic) return GDT_EUNSUPPORTED;
+  if (d.periodic || d.mesh) return GDT_EUNSUPPORTED;
   const size_t bytes = sizeof(double) * size_t(d.nvert) * d.dim;
   double* buf = nullptr;
   if (cudaMalloc(&buf, bytes) != cudaSuccess) {
@@ -250,6 +250,7 @@ gdt_status gdt_space_create(gdt_grid g, int kind, int order, gdt_space* out) {
   gdt_space_s s;
   s.g = d;
   s.xv_owner = g->xv_owner;
+  s.mesh_owner = g->mesh_owner;
   s.kind = kind;
   s.order = order;
   // mapped grids: continuous order-1 spaces only (their assembly forms each element's geometry)
@@ -300,7 +301,8 @@ gdt_status gdt_matrix_create(gdt_context ctx, gdt_space test, gdt_space ansatz, 
   if (stencil < GDT_STENCIL_ELEMENT || stencil > GDT_STENCIL_ELEMENT_AND_INTERSECTION)
     return fail(ctx, GDT_EINVAL, "unknown stencil");
   if (test->kind != ansatz->kind || test->order != ansatz->order ||
-      std::memcmp(test->g.n, ansatz->g.n, sizeof(test->g.n)) != 0 || test->g.simplex != ansatz->g.simplex)
+      std::memcmp(test->g.n, ansatz->g.n, sizeof(test->g.n)) != 0 || test->g.simplex != ansatz->g.simplex ||
+      test->g.mcells != ansatz->g.mcells)
     return fail(ctx, GDT_EUNSUPPORTED, "test and ansatz space must coincide");
   if (test->kind == GDT_SPACE_FV) return fail(ctx, GDT_EUNSUPPORTED, "no matrix for finite-volume spaces");
   if (test->kind == GDT_SPACE_CG && stencil != GDT_STENCIL_ELEMENT)
@@ -365,6 +367,11 @@ gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_di
   if (d->force_qp && d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
   if (m->test.g.xv && (d->kappa_qp || d->kappa_tensor || d->kappa_tensor_qp || d->force_qp))
     return fail(ctx, GDT_EUNSUPPORTED, "mapped grids: kappa and source per element or constant");
+  if (m->test.g.mesh) {
+    m->mf_valid = 0;
+    return mesh_assemble(ctx, m->test.g, m->rp, m->col, m->val, d, rhs, d->dirichlet ? d->dirichlet_values : nullptr,
+                         d->dirichlet ? d->dirichlet_value_const : 0.0);
+  }
   const bool values = d->dirichlet && (d->dirichlet_values || d->dirichlet_value_const != 0.0);
   if (values && (m->test.order != 1 || d->kappa_qp || d->kappa_tensor || d->kappa_tensor_qp || d->force_qp))
     return fail(ctx, GDT_EUNSUPPORTED, "Dirichlet values are lowered for the order-1 vertex-row assembly");
@@ -390,6 +397,7 @@ gdt_status gdt_assemble_cg_diffusion(gdt_context ctx, gdt_matrix m, const gdt_di
 gdt_status gdt_assemble_cg_rhs(gdt_context ctx, gdt_space s, const gdt_diffusion_desc* d, double* rhs) {
   if (!ctx || !s || !d || !rhs) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
+  if (s->g.mesh && !d->force_qp) return mesh_assemble(ctx, s->g, nullptr, nullptr, nullptr, d, rhs, nullptr, 0.0);
   if (d->force_qp) {
     if (s->g.xv) return fail(ctx, GDT_EUNSUPPORTED, "mapped grids: source per element or constant");
     if (d->force_quad_order < 0) return fail(ctx, GDT_EINVAL, "negative quadrature order");
@@ -405,6 +413,7 @@ gdt_status gdt_dirichlet_apply(gdt_context ctx, gdt_matrix m, double* rhs) {
   m->val_version++;
   if (m->test.order == 2) return ho_dirichlet(ctx, m, rhs);
   m->mf_dirichlet = 1;
+  if (m->test.g.mesh) return mesh_dirichlet(ctx, m, rhs, nullptr, 0.0);
   return dirichlet_apply(ctx, m, rhs);
 }
 
@@ -415,6 +424,7 @@ gdt_status gdt_dirichlet_apply_values(gdt_context ctx, gdt_matrix m, double* rhs
   if (m->test.order != 1) return fail(ctx, GDT_EUNSUPPORTED, "Dirichlet values are lowered for order 1");
   m->val_version++;
   m->mf_dirichlet = 1;
+  if (m->test.g.mesh) return mesh_dirichlet(ctx, m, rhs, values, value_const);
   return dirichlet_apply(ctx, m, rhs, values, value_const);
 }
 
@@ -535,6 +545,7 @@ gdt_status gdt_cg_dlogkappa(gdt_context ctx, gdt_space s, const double* kappa, c
   if (!ctx || !s || !kappa || !u || !lam || !out) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_CG) return fail(ctx, GDT_ESHAPE, "not a continuous space");
   if (s->order != 1) return fail(ctx, GDT_EUNSUPPORTED, "log-kappa gradient of order-2 spaces");
+  if (s->g.mesh) return mesh_dlogkappa(ctx, s->g, kappa, u, lam, out);
   if (s->g.xv) return fail(ctx, GDT_EUNSUPPORTED, "log-kappa gradient on mapped grids");
   return cg_dlogkappa(ctx, *s, kappa, u, lam, out);
 }

@@ -28,8 +28,17 @@ struct GridDesc {
   double h[3] = {1, 1, 1};
   long long ncells = 1, nelem = 1, nvert = 1;
   // vertex coordinates of a mapped grid (device, [vertex][dim], vertices lexicographic with x fastest);
-  // null for the equidistant grid of lo, hi and n
+  // null for the equidistant grid of lo, hi and n. Also the coordinates of a simplex mesh.
   const double* xv = nullptr;
+  // Unstructured simplex mesh (mesh = 1; the fields above other than dim, simplex, nelem, nvert and
+  // xv are unused): element vertex lists [element][dim + 1], vertex -> element adjacency (CSR over the
+  // vertices, elements ascending) and boundary-vertex flags (vertices of faces of one element), all
+  // on the device
+  int mesh = 0;
+  const int* mcells = nullptr;
+  const int* v2e_ptr = nullptr;
+  const int* v2e = nullptr;
+  const unsigned char* mbnd = nullptr;
 };
 
 }  // namespace gdt
@@ -62,6 +71,7 @@ struct gdt_context_s {
 struct gdt_grid_s {
   gdt::GridDesc d;
   std::shared_ptr<double> xv_owner;  // the device coordinates of a mapped grid (d.xv)
+  std::shared_ptr<void> mesh_owner;  // the device arrays of a simplex mesh
 };
 
 struct gdt_space_s {
@@ -71,6 +81,7 @@ struct gdt_space_s {
   int lsize = 1;
   long long size = 0;
   std::shared_ptr<double> xv_owner;  // keeps g.xv alive with every copy of the space
+  std::shared_ptr<void> mesh_owner;  // and the mesh arrays
 };
 
 struct gdt_matrix_s {
@@ -139,6 +150,14 @@ void timing_harvest(gdt_context ctx);
 // ---------------------------------------------------------------- kernels (host launchers) ---
 // pattern.cu
 gdt_status build_pattern(gdt_context ctx, gdt_matrix m);
+// unstructured simplex meshes (mesh.cu)
+gdt_status mesh_pattern(gdt_context ctx, gdt_matrix m);
+gdt_status mesh_assemble(gdt_context ctx, const GridDesc& g, const int* rp, const int* col, double* val,
+                         const gdt_diffusion_desc* d, double* rhs, const double* gD, double gD_const);
+gdt_status mesh_dirichlet(gdt_context ctx, gdt_matrix m, double* rhs, const double* values, double value_const);
+gdt_status mesh_dlogkappa(gdt_context ctx, const GridDesc& g, const double* kappa, const double* u, const double* lam,
+                          double* out);
+gdt_status mesh_global_indices(gdt_context ctx, const GridDesc& g, int64_t* out);
 // assemble_cg.cu
 gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs);
 gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& s, const gdt_diffusion_desc* d, double* rhs);

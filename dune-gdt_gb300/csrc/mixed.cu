@@ -784,7 +784,8 @@ bool encode_tensor_map_f32(CUtensorMap* map, int rank, void* base, const uint64_
 }
 
 bool mixed_stencil_supported(gdt_matrix m) {
-  return m->test.kind == GDT_SPACE_CG && m->rows == m->test.g.nvert && m->max_row > 0 && m->max_row <= 32;
+  return m->test.kind == GDT_SPACE_CG && !m->test.g.mesh && m->rows == m->test.g.nvert && m->max_row > 0 &&
+         m->max_row <= 32;
 }
 
 gdt_status solve_mixed_stencil(gdt_context ctx, gdt_matrix m, const double* b, double* x, const gdt_solver_opts* o,

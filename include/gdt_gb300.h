@@ -144,6 +144,21 @@ gdt_status gdt_grid_create_cube(int dim, const int64_t* num_elements, const doub
  * source per element or constant, Dirichlet values) and everything that works on assembled matrices
  * (SpMV, solvers, Dirichlet constraints, lincomb); other forms return GDT_EUNSUPPORTED. */
 gdt_status gdt_grid_set_vertices(gdt_grid grid, const double* coords);
+/* Unstructured simplex mesh: the leaf view of a DUNE simplex grid (ALUGrid, UGGrid, a gmsh import),
+ * exported in its index-set order (replaces the grid object that make_cube_grid / GridProvider hand to
+ * make_continuous_lagrange_space, spaces/h1/continuous-lagrange.hh:189-203). dim 2 (triangles) or 3
+ * (tetrahedra); coords [num_vertices][dim], cells [num_elements][dim + 1] vertex indices; host or
+ * device pointers, copied. Elements must have distinct vertices and a volume above rounding (|det J|
+ * above 1e-12 times the product of its edge lengths), and a face may belong to at most two elements
+ * (GDT_EINVAL otherwise). Boundary vertices (the Dirichlet DoFs of
+ * DirichletConstraints, tools/dirichlet-constraints.hh:153-184) are the vertices of faces that belong
+ * to one element. Such a grid takes continuous order-1 spaces (DoF = vertex index, the ContinuousMapper
+ * of spaces/mapper/continuous.hh:139-150), their element pattern, the Laplace stiffness and load
+ * vector (kappa and source per element or constant, Dirichlet data homogeneous or given values), the
+ * log-kappa gradient and everything that works on assembled matrices; other forms return
+ * GDT_EUNSUPPORTED. */
+gdt_status gdt_grid_create_simplex_mesh(int dim, int64_t num_vertices, const double* coords, int64_t num_elements,
+                                        const int64_t* cells, gdt_grid* out);
 gdt_status gdt_grid_destroy(gdt_grid grid);
 int64_t gdt_grid_num_elements(gdt_grid grid);
 int64_t gdt_grid_num_vertices(gdt_grid grid);

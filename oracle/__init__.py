@@ -121,6 +121,9 @@ def lib():
             "orc_fv_explicit_euler": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, C.c_double, C.c_long, ip,
                                              dp]),
             "orc_fv_ssprk2": (None, [g, C.c_int, dp, C.c_int, C.c_double, dp, C.c_double, C.c_long, ip, dp]),
+            "orc_mesh_assemble": (C.c_void_p, [C.c_int, C.c_long, dp, C.c_long, lp, dp, C.c_double, dp, C.c_double,
+                                               C.c_int, dp]),
+            "orc_mesh_boundary": (C.c_long, [C.c_int, C.c_long, C.c_long, lp, lp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -195,6 +198,27 @@ def global_indices(g, kind, order):
     out = np.empty(num_elements(g) * ls, np.int64)
     lib().orc_global_indices(C.byref(g), kind, order, _lp(out))
     return out.reshape(-1, ls)
+
+
+def mesh_assemble(coords, cells, kappa=None, kappa_const=1.0, force=None, force_const=1.0, dirichlet=True):
+    """P1 stiffness + load vector on an unstructured simplex mesh (coords [nv, dim], cells [ne, dim + 1])."""
+    x = np.ascontiguousarray(coords, dtype=np.float64)
+    c = np.ascontiguousarray(cells, dtype=np.int64)
+    rhs = np.zeros(x.shape[0])
+    kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+    frc = None if force is None else np.ascontiguousarray(force, dtype=np.float64)
+    h = lib().orc_mesh_assemble(x.shape[1], x.shape[0], _dp(x), c.shape[0], _lp(c), _dp(kap), kappa_const, _dp(frc),
+                                force_const, int(dirichlet), _dp(rhs))
+    return CSR(h), rhs
+
+
+def mesh_boundary(num_vertices, cells):
+    c = np.ascontiguousarray(cells, dtype=np.int64)
+    dim = c.shape[1] - 1
+    n = lib().orc_mesh_boundary(dim, num_vertices, c.shape[0], _lp(c), None)
+    out = np.empty(n, np.int64)
+    lib().orc_mesh_boundary(dim, num_vertices, c.shape[0], _lp(c), _lp(out))
+    return out
 
 
 def dirichlet_dofs(g, order):

@@ -1,7 +1,11 @@
 // ORACLE — test infrastructure only (see oracle.h). CPU restatement of the reference path.
 #include "oracle.h"
 
+#include <algorithm>
+#include <array>
 #include <cfloat>
+#include <cmath>
+#include <map>
 #include <limits>
 #include <numeric>
 
@@ -1372,4 +1376,124 @@ extern "C" void orc_fv_ssprk2(const orc_grid* gd, int flux, const double* vel, i
     for (long i = 0; i < N; ++i) u[i] += k0[i] * bb;
     for (long i = 0; i < N; ++i) u[i] += k1[i] * bb;
   }
+}
+
+// -------------------------------------------------------------- unstructured simplex meshes ---
+// A simplex grid given by its index sets (vertex coordinates, element vertex lists in index-set
+// order), as the leaf view of an ALUGrid/UGGrid: the continuous P1 element loop of
+// MatrixOperator::assemble (operators/matrix-based.hh:496-500) with LocalLaplaceIntegrand and the
+// product right-hand side, the element pattern of make_element_sparsity_pattern
+// (tools/sparsity-pattern.hh:33-50) and DirichletConstraints on the boundary vertices.
+namespace {
+
+struct Mesh {
+  int dim;
+  long nv, ne;
+  const double* x;
+  const int64_t* c;
+};
+
+// boundary vertices: the vertices of faces (an element's vertices without one of them) that belong to
+// one element only, i.e. of the boundary intersections (Intersection::boundary()), ascending
+std::vector<int64_t> mesh_boundary(const Mesh& M) {
+  std::map<std::array<int64_t, 3>, int> faces;
+  for (long e = 0; e < M.ne; ++e)
+    for (int skip = 0; skip <= M.dim; ++skip) {
+      std::array<int64_t, 3> f = {-1, -1, -1};
+      int k = 0;
+      for (int j = 0; j <= M.dim; ++j)
+        if (j != skip) f[k++] = M.c[e * (M.dim + 1) + j];
+      std::sort(f.begin(), f.begin() + M.dim);
+      ++faces[f];
+    }
+  std::vector<char> flag(M.nv, 0);
+  for (const auto& kv : faces)
+    if (kv.second == 1)
+      for (int a = 0; a < M.dim; ++a) flag[kv.first[a]] = 1;
+  std::vector<int64_t> out;
+  for (long v = 0; v < M.nv; ++v)
+    if (flag[v]) out.push_back(v);
+  return out;
+}
+
+// P1 on element e: physical gradients of the barycentric basis (the reference gradients mapped by
+// J^{-T}, J = [x_1 - x_0, ..., x_d - x_0]) and the volume |det J| / d!
+double mesh_gradients(const Mesh& M, long e, int64_t* w, double G[4][3]) {
+  const int d = M.dim;
+  double X[4][3] = {};
+  for (int j = 0; j <= d; ++j) {
+    w[j] = M.c[e * (d + 1) + j];
+    for (int a = 0; a < d; ++a) X[j][a] = M.x[w[j] * d + a];
+  }
+  double J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int k = 0; k < d; ++k)
+    for (int a = 0; a < d; ++a) J[a][k] = X[k + 1][a] - X[0][a];
+  // inverse by cofactors (the 2D case is the 3D one with J[2][2] = 1)
+  double cof[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+      cof[r][c] = J[r1][c1] * J[r2][c2] - J[r1][c2] * J[r2][c1];
+    }
+  const double det = J[0][0] * cof[0][0] + J[0][1] * cof[0][1] + J[0][2] * cof[0][2];
+  // (J^{-1})[k][a] = cof[a][k] / det; grad phi_j = J^{-T} e_{j-1}: component a = (J^{-1})[j-1][a]
+  for (int a = 0; a < d; ++a) {
+    double s0 = 0.0;
+    for (int j = 1; j <= d; ++j) {
+      G[j][a] = cof[a][j - 1] / det;
+      s0 += G[j][a];
+    }
+    G[0][a] = -s0;
+  }
+  return std::fabs(det) / (d == 2 ? 2.0 : 6.0);
+}
+
+}  // namespace
+
+extern "C" long orc_mesh_boundary(int dim, long nv, long ne, const int64_t* cells, int64_t* out) {
+  Mesh M{dim, nv, ne, nullptr, cells};
+  std::vector<int64_t> b = mesh_boundary(M);
+  if (out) std::copy(b.begin(), b.end(), out);
+  return long(b.size());
+}
+
+extern "C" orc_csr* orc_mesh_assemble(int dim, long nv, const double* x, long ne, const int64_t* cells,
+                                      const double* kappa, double kappa_const, const double* force,
+                                      double force_const, int dirichlet, double* rhs) {
+  Mesh M{dim, nv, ne, x, cells};
+  const int n = dim + 1;
+  // element pattern: row i holds the vertices of every element that contains vertex i
+  std::vector<std::vector<int32_t>> rows(nv);
+  for (long e = 0; e < ne; ++e)
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) rows[cells[e * n + i]].push_back(int32_t(cells[e * n + j]));
+  orc_csr* m = new orc_csr;
+  m->n = nv;
+  m->rp.assign(nv + 1, 0);
+  for (long r = 0; r < nv; ++r) {
+    std::sort(rows[r].begin(), rows[r].end());
+    rows[r].erase(std::unique(rows[r].begin(), rows[r].end()), rows[r].end());
+    m->rp[r + 1] = m->rp[r] + int64_t(rows[r].size());
+    m->col.insert(m->col.end(), rows[r].begin(), rows[r].end());
+  }
+  m->val.assign(m->col.size(), 0.0);
+  if (rhs) std::fill(rhs, rhs + nv, 0.0);
+  for (long e = 0; e < ne; ++e) {
+    int64_t w[4];
+    double G[4][3] = {};
+    const double vol = mesh_gradients(M, e, w, G);
+    const double kv = (kappa ? kappa[e] : kappa_const) * vol;
+    double A[16];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double s = 0.0;
+        for (int a = 0; a < dim; ++a) s += G[i][a] * G[j][a];
+        A[i * n + j] = kv * s;
+      }
+    scatter(m, w, w, n, A);
+    if (rhs)
+      for (int i = 0; i < n; ++i) rhs[w[i]] += (force ? force[e] : force_const) * vol / double(n);
+  }
+  if (dirichlet) apply_dirichlet(m, rhs, mesh_boundary(M));
+  return m;
 }

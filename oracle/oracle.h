@@ -63,6 +63,14 @@ void orc_csr_free(orc_csr* m);
 orc_csr* orc_assemble_cg(const orc_grid* g, int order, const double* kappa, double kappa_const,
                          const double* force, double force_const, int force_fn, int force_order,
                          int dirichlet, double* rhs);
+/* Unstructured simplex mesh (triangles or tetrahedra given by vertex coordinates [nv][dim] and element
+ * vertex lists [ne][dim + 1]): continuous P1 stiffness with kappa per element (or constant), load of a
+ * source per element (or constant), DirichletConstraints on the boundary vertices (vertices of faces
+ * of one element) when dirichlet != 0. */
+orc_csr* orc_mesh_assemble(int dim, long nv, const double* coords, long ne, const int64_t* cells, const double* kappa,
+                           double kappa_const, const double* force, double force_const, int dirichlet, double* rhs);
+/* the boundary vertices of such a mesh, ascending; returns the count (out may be NULL) */
+long orc_mesh_boundary(int dim, long nv, long ne, const int64_t* cells, int64_t* out);
 /* the same with a d x d diffusion tensor per element, row-major (local/integrands/laplace.hh:81-102) */
 orc_csr* orc_assemble_cg_tensor(const orc_grid* g, int order, const double* kappa_tensor, const double* force,
                                 double force_const, int dirichlet, double* rhs);

@@ -1,0 +1,62 @@
+"""CPU checks of the oracle's unstructured simplex meshes, pinning the mesh restatement to the structured
+one that the reference's known answers pin: the Kuhn split of a cube grid handed over as a mesh gives
+the same pattern, matrix, load vector and boundary; on Delaunay meshes, linear functions pass the patch
+test and a unit source integrates the area."""
+import numpy as np
+import pytest
+
+spatial = pytest.importorskip("scipy.spatial")
+
+
+def kuhn_mesh(oracle, dim, n):
+    """The Kuhn simplex grid of the unit box as (oracle grid, coords, cells)."""
+    og = oracle.grid(dim, n, 0.0, 1.0, simplex=True)
+    ne = oracle.num_elements(og)
+    cells = oracle.global_indices(og, oracle.CG, 1).reshape(ne, dim + 1)
+    grids = np.meshgrid(*[np.linspace(0.0, 1.0, k + 1) for k in n], indexing="ij")
+    coords = np.stack([gr.transpose(*reversed(range(dim))).reshape(-1) for gr in grids], axis=1)
+    return og, coords, cells
+
+
+def delaunay_mesh(dim, n, seed):
+    """Delaunay simplices of a jittered lattice of (n + 1)^dim points in the unit box (corners kept)."""
+    rng = np.random.default_rng(seed)
+    t = np.linspace(0.0, 1.0, n + 1)
+    X = np.stack(np.meshgrid(*([t] * dim), indexing="ij"), -1).reshape(-1, dim)
+    inner = np.all((X > 0) & (X < 1), axis=1)
+    X[inner] += (0.3 / n) * rng.uniform(-1, 1, (inner.sum(), dim))
+    cells = spatial.Delaunay(X).simplices.astype(np.int64)
+    # the flat simplices Delaunay leaves on the box faces (coplanar boundary points) have no volume
+    J = np.stack([X[cells[:, k + 1]] - X[cells[:, 0]] for k in range(dim)], axis=-1)
+    vol = np.abs(np.linalg.det(J))
+    return X, cells[vol > 1e-9 * vol.max()]
+
+
+@pytest.mark.parametrize("dim,n", [(2, [6, 5]), (3, [3, 4, 2])])
+def test_kuhn_grid_as_mesh_equals_structured(oracle, dim, n):
+    og, coords, cells = kuhn_mesh(oracle, dim, n)
+    rng = np.random.default_rng(4)
+    ne = cells.shape[0]
+    kappa, force = np.exp(rng.standard_normal(ne)), rng.uniform(-1, 2, ne)
+    for dirichlet in (False, True):
+        A, b = oracle.assemble_cg(og, 1, kappa=kappa, force=force, dirichlet=dirichlet)
+        M, bm = oracle.mesh_assemble(coords, cells, kappa=kappa, force=force, dirichlet=dirichlet)
+        assert np.array_equal(M.row_ptr, A.row_ptr) and np.array_equal(M.col, A.col)
+        assert np.abs(M.val - A.val).max() <= 1e-14 * np.abs(A.val).max()
+        assert np.abs(bm - b).max() <= 1e-14 * np.abs(b).max()
+    assert np.array_equal(oracle.mesh_boundary(coords.shape[0], cells), oracle.dirichlet_dofs(og, 1))
+
+
+@pytest.mark.parametrize("dim,n", [(2, 9), (3, 4)])
+def test_delaunay_mesh_patch_test_and_area(oracle, dim, n):
+    X, cells = delaunay_mesh(dim, n, 11)
+    A, b = oracle.mesh_assemble(X, cells, force_const=1.0, dirichlet=False)
+    S = A.to_scipy().tocsr()
+    assert abs(S - S.T).max() <= 1e-14 * abs(S).max()
+    u = 0.3 + X @ np.array([1.0, -0.5, 2.0][:dim])
+    r = S @ u
+    inner = np.ones(X.shape[0], bool)
+    inner[oracle.mesh_boundary(X.shape[0], cells)] = False
+    assert inner.any()
+    assert np.abs(r[inner]).max() <= 1e-12 * abs(S).max() * np.abs(u).max()
+    assert abs(b.sum() - 1.0) <= 1e-13
