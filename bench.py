@@ -60,12 +60,12 @@ def parse():
     p.add_argument("--spmv-schedule", default="auto", choices=["auto"] + SCHEDULE_NAMES,
                    help="heat3d: pin the FP64 SpMV schedule instead of the autotuner's choice (for profiling)")
     p.add_argument("--headline-only", action="store_true", help="default config without the extra metric keys")
-    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg", "q2", "mapped", "peaks"],
+    p.add_argument("--config", default="heat3d", choices=["heat3d", "batched", "fv", "swipdg", "q2", "mapped", "mesh", "peaks"],
                    help="heat3d: the headline 128^3 workload (with the other metric keys); batched: 512 "
                         "parametric P1 problems of uneven size in one persistent launch; fv: 2D Burgers FV, "
                         "SSP-RK2; swipdg: SWIPDG P1 forward solve + adjoint log-kappa gradient on 256^2 "
                         "squares; q2: 3D Q2 assembly + solve; mapped: 3D Q1 assembly + solve on a mapped "
-                        "(curved) 128^3 grid; peaks: FP64 FMA / tensor-core throughput")
+                        "(curved) 128^3 grid; mesh: P1 on an unstructured tetrahedral mesh; peaks: FP64 FMA / tensor-core throughput")
     p.add_argument("--problems", type=int, default=512, help="batched: number of problems")
     p.add_argument("--fv-n", type=int, default=4096, help="fv: cells per axis")
     p.add_argument("--fv-steps", type=int, default=500, help="fv: SSP-RK2 steps per bench step")
@@ -73,6 +73,7 @@ def parse():
     p.add_argument("--dg-n", type=int, default=256, help="swipdg: squares per axis (2 triangles each)")
     p.add_argument("--q2-n", type=int, default=64, help="q2: hexahedra per axis")
     p.add_argument("--mapped-n", type=int, default=128, help="mapped: hexahedra per axis")
+    p.add_argument("--mesh-n", type=int, default=96, help="mesh: cubes per axis of the tetrahedral mesh")
     p.add_argument("--dg-fd", type=int, default=64, help="swipdg: elements of the finite-difference check")
     return p.parse_args()
 
@@ -969,6 +970,91 @@ def run_mapped(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mesh(args):
+    """-div(kappa grad u) = 1 on the unit cube meshed by tetrahedra given as an unstructured mesh
+    (vertex coordinates + element vertex lists: the 6 n^3 tetrahedra of the Kuhn split with every
+    interior vertex moved by up to 0.2 h and the vertices renumbered by a seeded random permutation, so
+    that nothing of the lattice order is left), continuous P1, kappa = exp(N(0,1)) per element,
+    Dirichlet 0. One step = assembly (stiffness + load + constraints) + FP64 CG-Jacobi solve."""
+    import torch
+
+    gdt = importlib.import_module("dune-gdt_gb300")
+    gdt._build.build()
+    n = args.mesh_n
+    g = gdt.make_cube_grid([0, 0, 0], [1, 1, 1], [n, n, n], simplex=True)
+    cells = gdt.ContinuousLagrangeSpace(g, 1).global_indices().cpu().numpy()
+    t = np.linspace(0.0, 1.0, n + 1)
+    X = np.stack(np.meshgrid(t, t, t, indexing="ij"), -1).transpose(2, 1, 0, 3).reshape(-1, 3)
+    rng = np.random.default_rng(SEED + 8)
+    inner = np.all((X > 0) & (X < 1), axis=1)
+    X[inner] += (0.2 / n) * rng.uniform(-1, 1, (inner.sum(), 3))
+    perm = rng.permutation(X.shape[0])  # new index of old vertex v
+    Xp = np.empty_like(X)
+    Xp[perm] = X
+    cells_p = perm[cells]
+    ne, nv = cells.shape[0], X.shape[0]
+    t0 = time.perf_counter()
+    mesh = gdt.make_simplex_mesh(Xp, cells_p)
+    t_setup = time.perf_counter() - t0
+    kappa = torch.tensor(np.exp(rng.standard_normal(ne)), device="cuda")
+    space = gdt.ContinuousLagrangeSpace(mesh, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    op = gdt.MatrixOperator(mesh, space)
+    torch.cuda.synchronize()
+    t_pattern = time.perf_counter() - t0
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kappa))
+    rhs = torch.zeros(nv, dtype=torch.float64, device="cuda")
+    u = torch.zeros(nv, dtype=torch.float64, device="cuda")
+    opts = {"tol": args.tol}
+
+    def assemble():
+        op.assemble(rhs=rhs, force=1.0, dirichlet=True)
+
+    def step():
+        assemble()
+        u.zero_()
+        op.apply_inverse(rhs, u, opts=opts)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(0).start()
+    ms = event_ms(lambda: [step() for _ in range(args.steps)]) / args.steps
+    clk = clocks.stop()
+    info = dict(op.last_solve_info)
+    ms_asm = event_ms(lambda: [assemble() for _ in range(args.steps)]) / args.steps
+    # the same tetrahedra through the structured Kuhn path (lattice order, no geometry per element)
+    sop = gdt.MatrixOperator(g, gdt.ContinuousLagrangeSpace(g, 1))
+    sop += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kappa))
+    srhs = torch.zeros(nv, dtype=torch.float64, device="cuda")
+    sop.assemble(rhs=srhs, force=1.0, dirichlet=True)
+    ms_asm_s = event_ms(lambda: [sop.assemble(rhs=srhs, force=1.0, dirichlet=True)
+                                 for _ in range(args.steps)]) / args.steps
+    r = (op.apply(u) - rhs).norm().item() / rhs.norm().item()
+    # algorithmic bytes of the assembly: the CSR row written once (8 B value, plus reads of the 4 B
+    # column index of every entry), per row its adjacency (4 B per element), per element visit its
+    # vertex list (16 B) and 4 x 3 coordinates (96 B) and kappa (8 B), the load vector (8 B per row)
+    visits = 4 * ne
+    abytes = op.nnz * 12 + nv * 16 + visits * (4 + 16 + 96 + 8)
+    line = {
+        "metric": "DoF/s assembled+solved on an unstructured tetrahedral mesh (P1)",
+        "value": nv / (ms / 1e3), "unit": "DoF/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (jittered Kuhn tetrahedra of the unit cube, vertices renumbered by a seeded "
+                "permutation; seeded lognormal kappa per element)",
+        "config": {"workload": f"{ne} tetrahedra, {nv} vertices (unstructured mesh), continuous P1 ({op.nnz} nnz), "
+                               f"f=1, Dirichlet 0, CG-Jacobi FP64 to {args.tol:g} rel. residual",
+                   "dofs": nv, "elements": ne, "nnz": op.nnz},
+        "assembly_ms": ms_asm, "assembly_gbs_algorithmic": abytes / (ms_asm / 1e3) / 1e9,
+        "structured_kuhn_assembly_ms": ms_asm_s,
+        "mesh_setup_s": t_setup, "pattern_s": t_pattern,
+        "solve": info, "final_rel_residual": r,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------------ SWIPDG (config 4) ---
 def run_swipdg(args):
     """SWIPDG P1 on n^2 squares split into triangles (theta = 1, omega = kappa, sigma 8 / 14), log kappa
@@ -1143,6 +1229,8 @@ if __name__ == "__main__":
         run_swipdg(a)
     elif a.config == "mapped":
         run_mapped(a)
+    elif a.config == "mesh":
+        run_mesh(a)
     elif a.config == "q2":
         run_q2(a)
     elif a.config == "peaks":
