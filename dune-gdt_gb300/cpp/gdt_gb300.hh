@@ -97,15 +97,29 @@ template <int d>
 using FieldVector = std::array<double, d>;
 
 // ---------------------------------------------------------------------------------- grid ---
+// A grid: make_cube_grid's structured cubes (or their Kuhn simplex split, optionally with moved
+// vertices), or an unstructured simplex mesh (make_simplex_mesh)
 template <int d>
-class CubeGrid {
+class Grid {
  public:
-  CubeGrid(FieldVector<d> lower, FieldVector<d> upper, std::array<int64_t, d> cells, bool simplex = false,
+  Grid(FieldVector<d> lower, FieldVector<d> upper, std::array<int64_t, d> cells, bool simplex = false,
            bool periodic = false)
       : lower_(lower), upper_(upper), cells_(cells), simplex_(simplex) {
     gdt_grid g = nullptr;
     check(gdt_grid_create_cube(d, cells.data(), lower.data(), upper.data(), simplex, periodic, &g), nullptr,
           "make_cube_grid");
+    handle_.reset(g, [](gdt_grid x) { gdt_grid_destroy(x); });
+  }
+  // An unstructured simplex mesh: the leaf view of a DUNE simplex grid (ALUGrid, UGGrid, a gmsh
+  // import) in its index-set order; coords [num_vertices * d], cells [num_elements * (d + 1)] vertex
+  // indices. Continuous order-1 spaces (DoF = vertex index) with the Laplace stiffness, load vector
+  // (data per element or constant) and Dirichlet constraints on the boundary vertices.
+  Grid(const std::vector<double>& coords, const std::vector<int64_t>& cells) : simplex_(true), mapped_(true) {
+    const int64_t nv = int64_t(coords.size() / d), ne = int64_t(cells.size() / (d + 1));
+    if (coords.size() != size_t(nv) * d || cells.size() != size_t(ne) * (d + 1))
+      throw Exception(GDT_ESHAPE, "make_simplex_mesh: coords of d and cells of d + 1 entries each");
+    gdt_grid g = nullptr;
+    check(gdt_grid_create_simplex_mesh(d, nv, coords.data(), ne, cells.data(), &g), nullptr, "make_simplex_mesh");
     handle_.reset(g, [](gdt_grid x) { gdt_grid_destroy(x); });
   }
   gdt_grid handle() const { return handle_.get(); }
@@ -123,7 +137,7 @@ class CubeGrid {
   bool mapped() const { return mapped_; }
   // element barycentre (elements numbered cube * d! + simplex, cubes lexicographic, x fastest)
   FieldVector<d> barycentre(int64_t e) const {
-    if (mapped_) throw Exception(GDT_EUNSUPPORTED, "points of a mapped grid: data per element or constant");
+    if (mapped_) throw Exception(GDT_EUNSUPPORTED, "points of mapped grids and meshes: data per element or constant");
     const int nsub = simplex_ ? (d == 2 ? 2 : d == 3 ? 6 : 1) : 1;
     int64_t c = e / nsub;
     FieldVector<d> x;
@@ -146,7 +160,7 @@ class CubeGrid {
   // J_e the cube's scaling (times the Kuhn simplex's corner matrix: column m is the sum of the unit
   // vectors of the first m + 1 axes of its permutation, permutations in std::next_permutation order)
   FieldVector<d> global(int64_t e, const double* xref) const {
-    if (mapped_) throw Exception(GDT_EUNSUPPORTED, "points of a mapped grid: data per element or constant");
+    if (mapped_) throw Exception(GDT_EUNSUPPORTED, "points of mapped grids and meshes: data per element or constant");
     const int nsub = simplex_ ? (d == 2 ? 2 : d == 3 ? 6 : 1) : 1;
     int64_t c = e / nsub;
     std::array<double, d> loc{};
@@ -170,12 +184,21 @@ class CubeGrid {
   }
 
  private:
-  FieldVector<d> lower_, upper_;
-  std::array<int64_t, d> cells_;
+  FieldVector<d> lower_{}, upper_{};
+  std::array<int64_t, d> cells_{};
   bool simplex_;
   bool mapped_ = false;
   std::shared_ptr<gdt_grid_s> handle_;
 };
+
+template <int d>
+using CubeGrid = Grid<d>;
+
+// an unstructured simplex mesh (see Grid)
+template <int d>
+Grid<d> make_simplex_mesh(const std::vector<double>& coords, const std::vector<int64_t>& cells) {
+  return Grid<d>(coords, cells);
+}
 
 // XT::Grid::make_cube_grid<G>(lower_left, upper_right, num_elements)
 template <int d>
@@ -248,7 +271,10 @@ struct LocalElementProductIntegrand {
   ProductWithAnsatz<d> with_ansatz(const GridFunction<d>& f, int order = 3) const {
     return ProductWithAnsatz<d>{f, 0.0, false, order};
   }
-  ProductWithAnsatz<2> with_ansatz(double c) const { return ProductWithAnsatz<2>{{}, c, true, 0}; }
+  template <int d = 2>
+  ProductWithAnsatz<d> with_ansatz(double c) const {
+    return ProductWithAnsatz<d>{{}, c, true, 0};
+  }
 };
 
 struct LocalElementIntegralBilinearForm {

@@ -90,3 +90,35 @@ def test_facade_mapped_grid_solution_matches_oracle(gdt, oracle, simplex):
     ud = spl.spsolve(A.to_scipy().tocsc(), b)
     assert u.shape == ud.shape
     assert np.abs(u - ud).max() <= 1e-9 * np.abs(ud).max()
+
+
+@pytest.mark.parametrize("dim,n", [(2, 12), (3, 5)])
+def test_facade_mesh_driver_matches_oracle(gdt, oracle, dim, n, tmp_path):
+    # make_simplex_mesh<d>(coords, cells) through the unchanged driver calls on a Delaunay mesh read
+    # from a file: the solution equals a direct solve of the oracle's system on the same mesh
+    import numpy as np
+    import scipy.sparse.linalg as spl
+
+    spatial = pytest.importorskip("scipy.spatial")
+    rng = np.random.default_rng(21 + dim)
+    t = np.linspace(0.0, 1.0, n + 1)
+    X = np.stack(np.meshgrid(*([t] * dim), indexing="ij"), -1).reshape(-1, dim)
+    inner = np.all((X > 0) & (X < 1), axis=1)
+    X[inner] += (0.3 / n) * rng.uniform(-1, 1, (inner.sum(), dim))
+    cells = spatial.Delaunay(X).simplices.astype(np.int64)
+    J = np.stack([X[cells[:, k + 1]] - X[cells[:, 0]] for k in range(dim)], axis=-1)
+    vol = np.abs(np.linalg.det(J))
+    cells = cells[vol > 1e-9 * vol.max()]
+    path = tmp_path / "mesh.txt"
+    with open(path, "w") as f:
+        f.write(f"{dim} {X.shape[0]} {cells.shape[0]}\n")
+        np.savetxt(f, X, fmt="%.17e")
+        np.savetxt(f, cells, fmt="%d")
+    exes = gdt._build.build_examples()
+    exe = [e for e in exes if e.endswith("mesh_heat")][0]
+    out = subprocess.run([exe, str(path)], capture_output=True, text=True, timeout=300, check=True).stdout.split()
+    u = np.array([float(v) for v in out])
+    A, b = oracle.mesh_assemble(X, cells, kappa_const=1.0, force_const=1.0, dirichlet=True)
+    ud = spl.spsolve(A.to_scipy().tocsc(), b)
+    assert u.shape == ud.shape
+    assert np.abs(u - ud).max() <= 1e-9 * np.abs(ud).max()
