@@ -254,7 +254,9 @@ gdt_status gdt_space_create(gdt_grid g, int kind, int order, gdt_space* out) {
   s.kind = kind;
   s.order = order;
   // mapped grids: continuous order-1 spaces only (their assembly forms each element's geometry)
-  if (d.xv && !(kind == GDT_SPACE_CG && order == 1)) return GDT_EUNSUPPORTED;
+  // simplex meshes also: DG order 1 on triangles (SWIPDG)
+  if (d.xv && !(kind == GDT_SPACE_CG && order == 1) && !(d.mesh && kind == GDT_SPACE_DG && order == 1 && d.dim == 2))
+    return GDT_EUNSUPPORTED;
   if (kind == GDT_SPACE_CG) {
     if (order != 1 && order != 2) return GDT_EUNSUPPORTED;
     if (d.periodic) return GDT_EUNSUPPORTED;
@@ -465,11 +467,13 @@ gdt_status gdt_assemble_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_des
   if (m->stencil != GDT_STENCIL_ELEMENT_AND_INTERSECTION)
     return fail(ctx, GDT_ESHAPE, "SWIPDG needs the element_and_intersection stencil");
   m->val_version++;
+  if (m->test.g.mesh) return mesh_swipdg(ctx, m, d, rhs);
   return assemble_swipdg(ctx, m, d, rhs);
 }
 
 gdt_status gdt_dg_face_points(gdt_space dg, double* xy) {
   if (!dg || !xy || dg->kind != GDT_SPACE_DG) return GDT_EINVAL;
+  if (dg->g.mesh) return mesh_dg_face_points(*dg, xy);
   return dg_face_points(*dg, xy);
 }
 
@@ -554,6 +558,7 @@ gdt_status gdt_swipdg_dlogkappa(gdt_context ctx, gdt_space s, const gdt_ipdg_des
                                 const double* lam, double* out) {
   if (!ctx || !s || !d || !d->kappa || !u || !lam || !out) return GDT_EINVAL;
   if (s->kind != GDT_SPACE_DG) return fail(ctx, GDT_ESHAPE, "not a DG space");
+  if (s->g.mesh) return fail(ctx, GDT_EUNSUPPORTED, "SWIPDG log-kappa gradient on simplex meshes");
   return swipdg_dlogkappa(ctx, *s, d, u, lam, out);
 }
 

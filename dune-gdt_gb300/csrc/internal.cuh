@@ -39,6 +39,7 @@ struct GridDesc {
   const int* v2e_ptr = nullptr;
   const int* v2e = nullptr;
   const unsigned char* mbnd = nullptr;
+  const int* mnbr = nullptr;  // element across face k (opposite local vertex k) of element e at e * (dim + 1) + k, or -1
 };
 
 }  // namespace gdt
@@ -158,6 +159,9 @@ gdt_status mesh_dirichlet(gdt_context ctx, gdt_matrix m, double* rhs, const doub
 gdt_status mesh_dlogkappa(gdt_context ctx, const GridDesc& g, const double* kappa, const double* u, const double* lam,
                           double* out);
 gdt_status mesh_global_indices(gdt_context ctx, const GridDesc& g, int64_t* out);
+gdt_status mesh_dg_pattern(gdt_context ctx, gdt_matrix m);
+gdt_status mesh_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs);
+gdt_status mesh_dg_face_points(const gdt_space_s& s, double* xy);
 // assemble_cg.cu
 gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs);
 gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& s, const gdt_diffusion_desc* d, double* rhs);

@@ -33,12 +33,16 @@ struct MeshData {
   int* v2e_ptr = nullptr;
   int* v2e = nullptr;
   unsigned char* bnd = nullptr;
+  int* nbr = nullptr;
+  std::vector<double> hx;   // host copies of the coordinates and element lists (face points)
+  std::vector<int> hcells;
   ~MeshData() {
     cudaFree(xv);
     cudaFree(cells);
     cudaFree(v2e_ptr);
     cudaFree(v2e);
     cudaFree(bnd);
+    cudaFree(nbr);
   }
 };
 
@@ -259,6 +263,302 @@ __global__ void k_mesh_indices(long long n, const int* __restrict__ cells, long 
     out[i] = cells[i];
 }
 
+// --------------------------------------------------------------------- DG P1 / SWIPDG on meshes ---
+// DoF 3 e + i (DiscontinuousMapper, spaces/mapper/discontinuous.hh:102-125); the element-and-intersection
+// pattern couples an element's rows with its own columns and those of its face neighbours, blocks in
+// ascending element order.
+__global__ void k_mesh_dg_pattern(GridDesc g, int* __restrict__ count, const int* __restrict__ rp,
+                                  int* __restrict__ col) {
+  const long long el = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (el >= g.nelem) return;
+  const int e = int(el);
+  int blk[4] = {e, -1, -1, -1};
+  int nb = 1;
+  for (int k = 0; k < 3; ++k) {
+    const int o = g.mnbr[e * 3 + k];
+    if (o < 0) continue;
+    int pos = nb;
+    while (pos > 0 && blk[pos - 1] > o) {
+      blk[pos] = blk[pos - 1];
+      --pos;
+    }
+    blk[pos] = o;
+    ++nb;
+  }
+  for (int i = 0; i < 3; ++i) {
+    const long long row = 3LL * e + i;
+    if (count) count[row] = 3 * nb;
+    if (col) {
+      int p = rp[row];
+      for (int b = 0; b < nb; ++b)
+        for (int j = 0; j < 3; ++j) col[p++] = 3 * blk[b] + j;
+    }
+  }
+}
+
+struct MeshIpdg {
+  double theta, sigma_in, sigma_bd, beta;
+  int weight_is_diffusion;
+  const double* g_face;  // Dirichlet data at the two Gauss points of every face ([element][face][point])
+  double g_const;
+  int rhs_terms;
+};
+
+// a triangle's vertices, coordinates, basis gradients and area
+__device__ __forceinline__ double mesh_tri(const GridDesc& g, int e, int (&w)[3], double (&X)[3][2],
+                                           double (&G)[3][2]) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    w[j] = g.mcells[e * 3 + j];
+    X[j][0] = g.xv[2LL * w[j]];
+    X[j][1] = g.xv[2LL * w[j] + 1];
+  }
+  const double a = X[1][0] - X[0][0], b = X[2][0] - X[0][0], c = X[1][1] - X[0][1], d = X[2][1] - X[0][1];
+  const double det = a * d - b * c;
+  G[1][0] = d / det;
+  G[1][1] = -b / det;
+  G[2][0] = -c / det;
+  G[2][1] = a / det;
+  G[0][0] = -G[1][0] - G[2][0];
+  G[0][1] = -G[1][1] - G[2][1];
+  return 0.5 * fabs(det);
+}
+
+// face k of a triangle: the other two local vertices (ascending), the unit outer normal and the length
+__device__ __forceinline__ double mesh_tri_face(const double (&X)[3][2], int k, int& a, int& b, double (&n)[2]) {
+  a = k == 0 ? 1 : 0;
+  b = k == 2 ? 1 : 2;
+  const double ex = X[b][0] - X[a][0], ey = X[b][1] - X[a][1];
+  const double len = sqrt(ex * ex + ey * ey);
+  n[0] = ey / len;
+  n[1] = -ex / len;
+  if ((X[k][0] - X[a][0]) * n[0] + (X[k][1] - X[a][1]) * n[1] > 0) {
+    n[0] = -n[0];
+    n[1] = -n[1];
+  }
+  return len;
+}
+
+// SWIPDG on a triangle mesh, output-stationary as on the Kuhn grid: one thread owns the 3 rows of one
+// element; its diagonal block is the element Laplace plus the in/in term of each face, its block to
+// a neighbour the in/out term of the shared face, both from the element's own side with the terms of
+// LocalLaplaceIPDGIntegrands::InnerCoupling + LocalIPDGIntegrands::InnerPenalty
+// (local/integrands/laplace-ipdg.hh:107-186, local/integrands/ipdg.hh:113-171), DirichletCoupling +
+// BoundaryPenalty on boundary faces (laplace-ipdg.hh:331-368, ipdg.hh:254-282), h = |I|^beta, the
+// 2-point Gauss rule on every face. On a face the basis of either element is linear along the shared
+// edge, so its values at the face points are the edge parameters of the shared vertices.
+__global__ void __launch_bounds__(128) k_mesh_swipdg_rows(GridDesc g, MeshIpdg p, const int* __restrict__ rp,
+                                                          double* __restrict__ val, double* __restrict__ rhs,
+                                                          const double* __restrict__ kappa, double kappa_const,
+                                                          const double* __restrict__ force, double force_const) {
+  const long long el = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (el >= g.nelem) return;
+  const int e = int(el);
+  int w[3];
+  double X[3][2], G[3][2];
+  const double area = mesh_tri(g, e, w, X, G);
+  const double kin = kappa ? kappa[e] : kappa_const;
+  const double gq = 0.5 / sqrt(3.0);
+  const double xi[2] = {0.5 - gq, 0.5 + gq};
+  double D[3][3], O[3][3][3], b[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    b[i] = (force ? force[e] : force_const) * area / 3.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) D[i][j] = kin * area * (G[i][0] * G[j][0] + G[i][1] * G[j][1]);
+  }
+  int nb[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    int a, bb;
+    double n[2];
+    const double len = mesh_tri_face(X, k, a, bb, n);
+    const double hb = p.beta == 1.0 ? len : pow(len, p.beta);
+    double vin[2][3];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) vin[q][i] = 0.0;
+      vin[q][a] = 1.0 - xi[q];
+      vin[q][bb] = xi[q];
+    }
+    double dn_in[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dn_in[i] = (kin * G[i][0]) * n[0] + (kin * G[i][1]) * n[1];
+    nb[k] = g.mnbr[e * 3 + k];
+    if (nb[k] >= 0) {
+      int wn[3];
+      double Xn[3][2], Gn[3][2];
+      mesh_tri(g, nb[k], wn, Xn, Gn);
+      const double kout = kappa ? kappa[nb[k]] : kappa_const;
+      double vout[2][3];
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) vout[q][j] = wn[j] == w[a] ? 1.0 - xi[q] : (wn[j] == w[bb] ? xi[q] : 0.0);
+      double dn_out[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) dn_out[j] = (kout * Gn[j][0]) * n[0] + (kout * Gn[j][1]) * n[1];
+      const double win = p.weight_is_diffusion ? kin : 1.0, wout = p.weight_is_diffusion ? kout : 1.0;
+      const double delta_plus = wout, delta_minus = win;
+      const double weight_minus = delta_plus / (delta_plus + delta_minus);
+      const double weight_plus = delta_minus / (delta_plus + delta_minus);
+      const double penalty = (p.sigma_in * ((delta_plus * delta_minus) / (delta_plus + delta_minus))) / hb;
+#pragma unroll
+      for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) O[k][ii][jj] = 0.0;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const double fac = 0.5 * len;
+#pragma unroll
+        for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            double v = -1.0 * weight_minus * dn_in[jj] * vin[q][ii];
+            v += -1.0 * p.theta * weight_minus * vin[q][jj] * dn_in[ii];
+            v += penalty * vin[q][jj] * vin[q][ii];
+            D[ii][jj] += v * fac;
+            double u = -1.0 * weight_plus * dn_out[jj] * vin[q][ii];
+            u += p.theta * weight_minus * vout[q][jj] * dn_in[ii];
+            u += -1.0 * penalty * vout[q][jj] * vin[q][ii];
+            O[k][ii][jj] += u * fac;
+          }
+      }
+    } else {
+      const double wb = p.weight_is_diffusion ? kin : 1.0;
+      const double penalty = (p.sigma_bd * wb) / hb;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const double fac = 0.5 * len;
+#pragma unroll
+        for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            double v = -1.0 * dn_in[jj] * vin[q][ii];
+            v += -1.0 * p.theta * vin[q][jj] * dn_in[ii];
+            v += penalty * vin[q][jj] * vin[q][ii];
+            D[ii][jj] += v * fac;
+          }
+        if (rhs && p.rhs_terms) {
+          const double gv = p.g_face ? p.g_face[(3LL * e + k) * 2 + q] : p.g_const;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            double v = 0.0;
+            if (p.rhs_terms & 1) v += -1.0 * p.theta * gv * dn_in[i];
+            if (p.rhs_terms & 2) v += penalty * gv * vin[q][i];
+            b[i] += v * fac;
+          }
+        }
+      }
+    }
+  }
+  if (rhs)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) rhs[3LL * e + i] = b[i];
+  if (!val) return;
+  // blocks in ascending element order: the element itself and its neighbours
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    int pos = rp[3LL * e + i];
+    int last = -1;
+    for (int s = 0; s < 4; ++s) {
+      // the next block: the smallest element id above `last` among e and the neighbours
+      int nxt = 0x7fffffff, kk = -2;
+      if (e > last && e < nxt) {
+        nxt = e;
+        kk = -1;
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (nb[k] > last && nb[k] < nxt) {
+          nxt = nb[k];
+          kk = k;
+        }
+      if (kk == -2) break;
+      last = nxt;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double v = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          if (kk == k) v = O[k][i][j];
+        val[pos++] = kk == -1 ? D[i][j] : v;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+gdt_status mesh_dg_pattern(gdt_context ctx, gdt_matrix m) {
+  const GridDesc& g = m->test.g;
+  if (g.dim != 2 || m->stencil != GDT_STENCIL_ELEMENT_AND_INTERSECTION)
+    return fail(ctx, GDT_EUNSUPPORTED, "DG on meshes: 2D with the element_and_intersection stencil");
+  cudaStream_t s = ctx->stream;
+  const long long rows = m->rows;
+  int* count = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMalloc(&m->rp, sizeof(int) * (rows + 1)));
+  GDT_TRY_CUDA(ctx, cudaMalloc(&count, sizeof(int) * (rows + 1)));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(count + rows, 0, sizeof(int), s));
+  const int bl = grid_blocks(g.nelem, 128);
+  k_mesh_dg_pattern<<<bl, 128, 0, s>>>(g, count, nullptr, nullptr);
+  GDT_CHECK(ctx, check_launch(ctx, "mesh DG pattern count"));
+  size_t tb = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tb, count, m->rp, rows + 1, s);
+  void* tmp = nullptr;
+  GDT_TRY_CUDA(ctx, cudaMalloc(&tmp, tb));
+  cub::DeviceScan::ExclusiveSum(tmp, tb, count, m->rp, rows + 1, s);
+  int nnz = 0;
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&nnz, m->rp + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(s));
+  cudaFree(tmp);
+  cudaFree(count);
+  m->nnz = nnz;
+  m->max_row = 12;
+  GDT_TRY_CUDA(ctx, cudaMalloc(&m->col, sizeof(int) * (nnz + 8)));
+  GDT_TRY_CUDA(ctx, cudaMalloc(&m->val, sizeof(double) * (nnz + 8)));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->val, 0, sizeof(double) * (nnz + 8), s));
+  GDT_TRY_CUDA(ctx, cudaMemsetAsync(m->col, 0, sizeof(int) * (nnz + 8), s));
+  k_mesh_dg_pattern<<<bl, 128, 0, s>>>(g, nullptr, m->rp, m->col);
+  GDT_CHECK(ctx, check_launch(ctx, "mesh DG pattern fill"));
+  m->spmv_sched = 0;
+  m->tuned = 0;
+  return GDT_OK;
+}
+
+gdt_status mesh_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs) {
+  const GridDesc& g = m->test.g;
+  if (d->penalty_beta < 0.0 || (d->dirichlet_rhs & ~3)) return fail(ctx, GDT_EINVAL, "SWIPDG descriptor");
+  const MeshIpdg p{d->symmetry_prefactor, d->sigma_inner, d->sigma_boundary,
+                   d->penalty_beta > 0.0 ? d->penalty_beta : 1.0, d->weight_is_diffusion, d->dirichlet_face,
+                   d->dirichlet_const, d->dirichlet_rhs};
+  k_mesh_swipdg_rows<<<grid_blocks(g.nelem, 128), 128, 0, ctx->stream>>>(g, p, m->rp, m->val, rhs, d->kappa,
+                                                                          d->kappa_const, d->force, d->force_const);
+  return check_launch(ctx, "mesh SWIPDG assembly");
+}
+
+gdt_status mesh_dg_face_points(const gdt_space_s& sp, double* xy) {
+  const auto* md = static_cast<const MeshData*>(sp.mesh_owner.get());
+  if (!md || sp.g.dim != 2) return GDT_EUNSUPPORTED;
+  const double gq = 0.5 / std::sqrt(3.0);
+  const double xi[2] = {0.5 - gq, 0.5 + gq};
+  for (long long e = 0; e < sp.g.nelem; ++e)
+    for (int k = 0; k < 3; ++k) {
+      const int a = k == 0 ? 1 : 0, b = k == 2 ? 1 : 2;
+      const double* xa = &md->hx[2 * size_t(md->hcells[size_t(e) * 3 + a])];
+      const double* xb = &md->hx[2 * size_t(md->hcells[size_t(e) * 3 + b])];
+      for (int q = 0; q < 2; ++q) {
+        double* out = xy + ((e * 3 + k) * 2 + q) * 2;
+        out[0] = xa[0] + xi[q] * (xb[0] - xa[0]);
+        out[1] = xa[1] + xi[q] * (xb[1] - xa[1]);
+      }
+    }
+  return GDT_OK;
+}
+
+namespace {
+
 template <typename T>
 bool upload(T** dst, const std::vector<T>& src) {
   if (cudaMalloc(dst, sizeof(T) * std::max<size_t>(src.size(), 1)) != cudaSuccess) return false;
@@ -398,26 +698,38 @@ extern "C" gdt_status gdt_grid_create_simplex_mesh(int dim, int64_t nvert, const
     }
     if (!std::isfinite(det) || !(std::fabs(det) > 1e-12 * scale)) return GDT_EINVAL;
   }
-  // boundary vertices: those of faces (vertex subsets without one vertex) that belong to one element
-  std::vector<std::array<int, 3>> faces;
+  // faces (an element's vertices without the one at local index k: face k): the boundary vertices are
+  // those of faces that belong to one element, the neighbour across face k the other element of it
+  struct Face {
+    std::array<int, 3> key;
+    int e, k;
+  };
+  std::vector<Face> faces;
   faces.reserve(size_t(nelem) * nl);
   for (int64_t e = 0; e < nelem; ++e)
     for (int skip = 0; skip < nl; ++skip) {
-      std::array<int, 3> f = {-1, -1, -1};
+      Face f{{-1, -1, -1}, int(e), skip};
       int k = 0;
       for (int j = 0; j < nl; ++j)
-        if (j != skip) f[k++] = cells32[size_t(e) * nl + j];
-      std::sort(f.begin(), f.begin() + dim);
+        if (j != skip) f.key[k++] = cells32[size_t(e) * nl + j];
+      std::sort(f.key.begin(), f.key.begin() + dim);
       faces.push_back(f);
     }
-  std::sort(faces.begin(), faces.end());
+  std::sort(faces.begin(), faces.end(), [](const Face& a, const Face& b) {
+    return a.key != b.key ? a.key < b.key : (a.e != b.e ? a.e < b.e : a.k < b.k);
+  });
   std::vector<unsigned char> bnd(size_t(nvert), 0);
+  std::vector<int> nbr(cells32.size(), -1);
   for (size_t i = 0; i < faces.size();) {
     size_t j = i + 1;
-    while (j < faces.size() && faces[j] == faces[i]) ++j;
+    while (j < faces.size() && faces[j].key == faces[i].key) ++j;
     if (j - i > 2) return GDT_EINVAL;  // a face shared by three elements: not a manifold mesh
-    if (j - i == 1)
-      for (int a = 0; a < dim; ++a) bnd[size_t(faces[i][a])] = 1;
+    if (j - i == 1) {
+      for (int a = 0; a < dim; ++a) bnd[size_t(faces[i].key[a])] = 1;
+    } else {
+      nbr[size_t(faces[i].e) * nl + faces[i].k] = faces[i + 1].e;
+      nbr[size_t(faces[i + 1].e) * nl + faces[i + 1].k] = faces[i].e;
+    }
     i = j;
   }
   // vertex -> element adjacency, elements ascending
@@ -431,7 +743,7 @@ extern "C" gdt_status gdt_grid_create_simplex_mesh(int dim, int64_t nvert, const
   if (!md) return GDT_ENOMEM;
   std::shared_ptr<void> owner(md, [](void* p) { delete static_cast<MeshData*>(p); });
   if (!upload(&md->xv, X) || !upload(&md->cells, cells32) || !upload(&md->v2e_ptr, ptr) || !upload(&md->v2e, adj) ||
-      !upload(&md->bnd, bnd)) {
+      !upload(&md->bnd, bnd) || !upload(&md->nbr, nbr)) {
     cudaGetLastError();
     return GDT_ENOMEM;
   }
@@ -452,6 +764,9 @@ extern "C" gdt_status gdt_grid_create_simplex_mesh(int dim, int64_t nvert, const
   d.v2e_ptr = md->v2e_ptr;
   d.v2e = md->v2e;
   d.mbnd = md->bnd;
+  d.mnbr = md->nbr;
+  md->hx = std::move(X);
+  md->hcells = std::move(cells32);
   g->mesh_owner = owner;
   *out = g;
   return GDT_OK;

@@ -109,7 +109,7 @@ __global__ void global_indices_kernel(GridDesc g, int kind, int lsize, long long
 
 gdt_status build_pattern(gdt_context ctx, gdt_matrix m) {
   if (m->test.kind == GDT_SPACE_CG && m->test.order == 2) return ho_build_pattern(ctx, m);
-  if (m->test.g.mesh) return mesh_pattern(ctx, m);
+  if (m->test.g.mesh) return m->test.kind == GDT_SPACE_DG ? mesh_dg_pattern(ctx, m) : mesh_pattern(ctx, m);
   const GridDesc& g = m->test.g;
   cudaStream_t s = ctx->stream;
   const bool dg = m->test.kind == GDT_SPACE_DG;
@@ -171,7 +171,7 @@ gdt_status build_pattern(gdt_context ctx, gdt_matrix m) {
 extern "C" gdt_status gdt_space_global_indices(gdt_context ctx, gdt_space s, int64_t* out) {
   if (!ctx || !s || !out) return GDT_EINVAL;
   if (s->kind == GDT_SPACE_CG && s->order == 2) return gdt::ho_global_indices(ctx, *s, out, nullptr);
-  if (s->g.mesh) return gdt::mesh_global_indices(ctx, s->g, out);
+  if (s->g.mesh && s->kind == GDT_SPACE_CG) return gdt::mesh_global_indices(ctx, s->g, out);
   gdt::global_indices_kernel<<<gdt::grid_blocks(s->g.nelem, 256), 256, 0, ctx->stream>>>(
       s->g, s->kind, s->lsize, reinterpret_cast<long long*>(out));
   return gdt::check_launch(ctx, "global indices");

@@ -155,8 +155,10 @@ gdt_status gdt_grid_set_vertices(gdt_grid grid, const double* coords);
  * to one element. Such a grid takes continuous order-1 spaces (DoF = vertex index, the ContinuousMapper
  * of spaces/mapper/continuous.hh:139-150), their element pattern, the Laplace stiffness and load
  * vector (kappa and source per element or constant, Dirichlet data homogeneous or given values), the
- * log-kappa gradient and everything that works on assembled matrices; other forms return
- * GDT_EUNSUPPORTED. */
+ * log-kappa gradient and everything that works on assembled matrices; on triangle meshes also DG
+ * order-1 spaces (DoF 3 e + i) with the element_and_intersection pattern and the SWIPDG assembly
+ * (face k of an element is the edge opposite its local vertex k, for gdt_dg_face_points and
+ * gdt_ipdg_desc.dirichlet_face); other forms return GDT_EUNSUPPORTED. */
 gdt_status gdt_grid_create_simplex_mesh(int dim, int64_t num_vertices, const double* coords, int64_t num_elements,
                                         const int64_t* cells, gdt_grid* out);
 gdt_status gdt_grid_destroy(gdt_grid grid);

@@ -124,6 +124,9 @@ def lib():
             "orc_mesh_assemble": (C.c_void_p, [C.c_int, C.c_long, dp, C.c_long, lp, dp, C.c_double, dp, C.c_double,
                                                C.c_int, dp]),
             "orc_mesh_boundary": (C.c_long, [C.c_int, C.c_long, C.c_long, lp, lp]),
+            "orc_mesh_assemble_swipdg": (C.c_void_p, [C.c_long, dp, C.c_long, lp, dp, C.c_double, dp, C.c_double,
+                                                      C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
+                                                      C.c_int, C.c_double, C.c_int, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -209,6 +212,22 @@ def mesh_assemble(coords, cells, kappa=None, kappa_const=1.0, force=None, force_
     frc = None if force is None else np.ascontiguousarray(force, dtype=np.float64)
     h = lib().orc_mesh_assemble(x.shape[1], x.shape[0], _dp(x), c.shape[0], _lp(c), _dp(kap), kappa_const, _dp(frc),
                                 force_const, int(dirichlet), _dp(rhs))
+    return CSR(h), rhs
+
+
+def mesh_assemble_swipdg(coords, cells, kappa=None, kappa_const=1.0, force=None, force_const=1.0, theta=1.0,
+                         sigma_inner=8.0, sigma_boundary=14.0, weight_is_diffusion=True, beta=1.0,
+                         dirichlet_fn=DIRICHLET_CONST, dirichlet_const=0.0, dirichlet_rhs=0):
+    """SWIPDG (DG P1) matrix + right-hand side on a triangle mesh (coords [nv, 2], cells [ne, 3])."""
+    x = np.ascontiguousarray(coords, dtype=np.float64)
+    c = np.ascontiguousarray(cells, dtype=np.int64)
+    rhs = np.zeros(3 * c.shape[0])
+    kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+    frc = None if force is None else np.ascontiguousarray(force, dtype=np.float64)
+    h = lib().orc_mesh_assemble_swipdg(x.shape[0], _dp(x), c.shape[0], _lp(c), _dp(kap), kappa_const, _dp(frc),
+                                       force_const, theta, sigma_inner, sigma_boundary, int(weight_is_diffusion),
+                                       float(beta), int(dirichlet_fn), float(dirichlet_const), int(dirichlet_rhs),
+                                       _dp(rhs))
     return CSR(h), rhs
 
 

@@ -1497,3 +1497,119 @@ extern "C" orc_csr* orc_mesh_assemble(int dim, long nv, const double* x, long ne
   if (dirichlet) apply_dirichlet(m, rhs, mesh_boundary(M));
   return m;
 }
+
+// SWIPDG with DG P1 on a triangle mesh: the element Laplace on every element, the coupling terms on
+// every inner intersection once (four blocks), the Dirichlet terms on boundary intersections
+// (test/stationary-eocstudies/diffusion-ipdg.hh:283-326), with the same element and face kernels as the
+// structured restatement. DoF 3 e + i; face k of an element is the edge opposite its local vertex k.
+extern "C" orc_csr* orc_mesh_assemble_swipdg(long nv, const double* x, long ne, const int64_t* cells,
+                                             const double* kappa, double kappa_const, const double* force,
+                                             double force_const, double theta, double sigma_in, double sigma_bd,
+                                             int weight_is_diffusion, double beta, int gfn, double gconst,
+                                             int rhs_terms, double* rhs) {
+  (void)nv;
+  Grid g;
+  g.dim = 2;
+  g.simplex = true;
+  g.nelem = ne;
+  LagrangeFE fe(true, 2, 1);
+  Coeffs c{kappa, kappa_const, force, force_const, ORC_FORCE_DATA, 0};
+  ElementKernel K(g, fe, 2, 1);
+  FaceKernel F(g, fe, 2);
+  FaceParams p{theta, sigma_in, sigma_bd, weight_is_diffusion != 0, beta, gfn, gconst, rhs_terms};
+  // neighbours across the faces (the intersections of the grid view)
+  std::vector<long> nb(size_t(ne) * 3, -1);
+  std::map<std::pair<int64_t, int64_t>, std::pair<long, int>> edges;
+  for (long e = 0; e < ne; ++e)
+    for (int k = 0; k < 3; ++k) {
+      const int a = k == 0 ? 1 : 0, b = k == 2 ? 1 : 2;
+      int64_t u = cells[e * 3 + a], v = cells[e * 3 + b];
+      if (u > v) std::swap(u, v);
+      auto it = edges.find({u, v});
+      if (it == edges.end()) {
+        edges[{u, v}] = {e, k};
+      } else {
+        nb[size_t(e) * 3 + k] = it->second.first;
+        nb[size_t(it->second.first) * 3 + it->second.second] = e;
+      }
+    }
+  auto geometry = [&](long e) {
+    Geometry geo;
+    geo.dim = 2;
+    geo.simplex = true;
+    geo.nv = 3;
+    for (int j = 0; j < 3; ++j) geo.x[j] = {x[cells[e * 3 + j] * 2], x[cells[e * 3 + j] * 2 + 1], 0.0};
+    return geo;
+  };
+  auto intersection = [&](long e, const Geometry& geo, int k) {
+    Intersection I;
+    I.inside = e;
+    I.face_in = k;
+    I.outside = nb[size_t(e) * 3 + k];
+    I.boundary = I.outside < 0;
+    I.nv = 2;
+    const int a = k == 0 ? 1 : 0, b = k == 2 ? 1 : 2;
+    I.corners[0] = geo.x[a];
+    I.corners[1] = geo.x[b];
+    const double tx = geo.x[b][0] - geo.x[a][0], ty = geo.x[b][1] - geo.x[a][1];
+    I.volume = std::sqrt(tx * tx + ty * ty);
+    Vec3 n{ty / I.volume, -tx / I.volume, 0.0};
+    if ((geo.x[k][0] - geo.x[a][0]) * n[0] + (geo.x[k][1] - geo.x[a][1]) * n[1] > 0) n = {-n[0], -n[1], 0.0};
+    I.normal = n;
+    return I;
+  };
+  // element and intersection pattern
+  orc_csr* m = new orc_csr;
+  m->n = 3 * ne;
+  m->rp.assign(size_t(m->n) + 1, 0);
+  for (long e = 0; e < ne; ++e) {
+    std::vector<long> blocks = {e};
+    for (int k = 0; k < 3; ++k)
+      if (nb[size_t(e) * 3 + k] >= 0) blocks.push_back(nb[size_t(e) * 3 + k]);
+    std::sort(blocks.begin(), blocks.end());
+    for (int i = 0; i < 3; ++i) {
+      for (long o : blocks)
+        for (int j = 0; j < 3; ++j) m->col.push_back(int32_t(3 * o + j));
+      m->rp[size_t(3 * e + i) + 1] = int64_t(m->col.size());
+    }
+  }
+  m->val.assign(m->col.size(), 0.0);
+  if (rhs) std::fill(rhs, rhs + 3 * ne, 0.0);
+  double A[9], B1[9], B2[9], B3[9], B4[9], bl[3];
+  auto idx = [](long e, int64_t* out) {
+    for (int i = 0; i < 3; ++i) out[i] = 3 * e + i;
+  };
+  for (long e = 0; e < ne; ++e) {
+    Geometry geo = geometry(e);
+    int64_t ie[3];
+    idx(e, ie);
+    K.laplace(geo, c.k(e), A);
+    scatter(m, ie, ie, 3, A);
+    if (rhs) {
+      K.rhs(geo, c, e, bl);
+      for (int i = 0; i < 3; ++i) rhs[ie[i]] += bl[i];
+    }
+    for (int k = 0; k < 3; ++k) {
+      Intersection I = intersection(e, geo, k);
+      if (I.outside >= 0) {
+        if (!(e < I.outside)) continue;
+        Geometry go = geometry(I.outside);
+        int64_t io[3];
+        idx(I.outside, io);
+        F.inner(I, geo, go, c.k(e), c.k(I.outside), p, B1, B2, B3, B4);
+        scatter(m, ie, ie, 3, B1);
+        scatter(m, ie, io, 3, B2);
+        scatter(m, io, ie, 3, B3);
+        scatter(m, io, io, 3, B4);
+      } else {
+        F.boundary(I, geo, c.k(e), p, B1);
+        scatter(m, ie, ie, 3, B1);
+        if (rhs && p.rhs_terms) {
+          F.boundary_rhs(I, geo, c.k(e), p, bl);
+          for (int i = 0; i < 3; ++i) rhs[ie[i]] += bl[i];
+        }
+      }
+    }
+  }
+  return m;
+}

@@ -69,6 +69,12 @@ orc_csr* orc_assemble_cg(const orc_grid* g, int order, const double* kappa, doub
  * of one element) when dirichlet != 0. */
 orc_csr* orc_mesh_assemble(int dim, long nv, const double* coords, long ne, const int64_t* cells, const double* kappa,
                            double kappa_const, const double* force, double force_const, int dirichlet, double* rhs);
+/* SWIPDG (DG P1) on a triangle mesh, the terms of orc_assemble_swipdg_data; DoF 3 e + i, face k of an
+ * element is the edge opposite its local vertex k */
+orc_csr* orc_mesh_assemble_swipdg(long nv, const double* coords, long ne, const int64_t* cells, const double* kappa,
+                                  double kappa_const, const double* force, double force_const, double theta,
+                                  double sigma_inner, double sigma_boundary, int weight_is_diffusion, double beta,
+                                  int dirichlet_fn, double dirichlet_const, int dirichlet_rhs, double* rhs);
 /* the boundary vertices of such a mesh, ascending; returns the count (out may be NULL) */
 long orc_mesh_boundary(int dim, long nv, long ne, const int64_t* cells, int64_t* out);
 /* the same with a d x d diffusion tensor per element, row-major (local/integrands/laplace.hh:81-102) */

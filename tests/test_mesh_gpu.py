@@ -1,7 +1,8 @@
 """Unstructured simplex meshes (gdt_grid_create_simplex_mesh) on the GPU against the oracle: the pattern
 bit-exact, stiffness, load vector and Dirichlet constraints within 1e-12 on Delaunay meshes of 2D and 3D
 boxes; the Kuhn split of a cube grid handed over as a mesh gives the structured path's system; solves,
-Dirichlet values, the log-kappa gradient and the forms a mesh does not lower."""
+Dirichlet values, the log-kappa gradient, SWIPDG (DG P1) on triangle meshes, and the forms a mesh does
+not lower."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -150,7 +151,9 @@ def test_mesh_log_kappa_gradient(gdt, oracle, dim, n, seed):
 def test_mesh_refusals(gdt):
     X, cells = delaunay_mesh(2, 6, 1)
     mesh = gdt.make_simplex_mesh(X, cells)
-    for make in (lambda: gdt.DiscontinuousLagrangeSpace(mesh, 1), lambda: gdt.ContinuousLagrangeSpace(mesh, 2)):
+    X3, cells3 = delaunay_mesh(3, 3, 1)
+    mesh3 = gdt.make_simplex_mesh(X3, cells3)
+    for make in (lambda: gdt.DiscontinuousLagrangeSpace(mesh3, 1), lambda: gdt.ContinuousLagrangeSpace(mesh, 2)):
         with pytest.raises(gdt.GdtError) as e:
             make()
         assert e.value.status == gdt._capi.EUNSUPPORTED
@@ -171,3 +174,71 @@ def test_mesh_refusals(gdt):
     with pytest.raises(gdt.GdtError) as e:
         op.assemble()
     assert e.value.status == gdt._capi.EUNSUPPORTED
+
+
+def _swipdg(gdt, grid, kappa, force, theta=1.0, dirichlet=None):
+    space = gdt.DiscontinuousLagrangeSpace(grid, 1)
+    op = gdt.MatrixOperator(grid, space, stencil=gdt.Stencil.element_and_intersection)
+    kt = torch.tensor(kappa, device="cuda")
+    op += gdt.LocalElementIntegralBilinearForm(gdt.LocalLaplaceIntegrand(kt))
+    op += gdt.LocalCouplingIntersectionIntegralBilinearForm(
+        gdt.LocalLaplaceIPDGInnerCoupling(theta, kt, kt) + gdt.LocalIPDGInnerPenalty(8.0, kt))
+    coupling = gdt.LocalLaplaceIPDGDirichletCoupling(theta, kt, 0.0 if dirichlet is None else dirichlet)
+    penalty = gdt.LocalIPDGBoundaryPenalty(14.0, kt, dirichlet_data=dirichlet)
+    op += gdt.LocalIntersectionIntegralBilinearForm(coupling + penalty)
+    rhs = torch.zeros(space.num_DoFs, dtype=torch.float64, device="cuda")
+    op.assemble(rhs=rhs, force=torch.tensor(force, device="cuda"))
+    return space, op, rhs
+
+
+@pytest.mark.parametrize("n,seed", [(10, 31), (24, 32)])
+@pytest.mark.parametrize("theta", [1.0, -1.0, 0.0])
+def test_mesh_swipdg_matches_oracle(gdt, oracle, n, seed, theta):
+    X, cells = delaunay_mesh(2, n, seed)
+    mesh = gdt.make_simplex_mesh(X, cells)
+    rng = np.random.default_rng(seed)
+    ne = cells.shape[0]
+    kappa, force = np.exp(rng.standard_normal(ne)), rng.uniform(0.5, 1.5, ne)
+    space, op, rhs = _swipdg(gdt, mesh, kappa, force, theta)
+    A, b = oracle.mesh_assemble_swipdg(X, cells, kappa=kappa, force=force, theta=theta)
+    rp, col, val = op.csr()
+    assert csr_equal_pattern((rp, col, val), A)
+    assert rel_err(val.cpu().numpy(), A.val) < 1e-12
+    assert rel_err(rhs.cpu().numpy(), b) < 1e-12
+    if theta == 1.0:
+        u = op.apply_inverse(rhs, opts={"tol": 1e-13, "max_iter": 200000})
+        assert rel_err(u.cpu().numpy(), spl.spsolve(A.to_scipy().tocsc(), b)) < 1e-9
+
+
+def test_mesh_swipdg_dirichlet_data_matches_oracle(gdt, oracle):
+    # Dirichlet data g = cos(pi x / 2) cos(pi y / 2) + 0.3 x at the face points of the mesh's faces: both
+    # right-hand side terms (unary DirichletCoupling and the penalty's counterpart)
+    X, cells = delaunay_mesh(2, 12, 33)
+    mesh = gdt.make_simplex_mesh(X, cells)
+    rng = np.random.default_rng(33)
+    ne = cells.shape[0]
+    kappa, force = np.exp(rng.standard_normal(ne)), rng.uniform(0.5, 1.5, ne)
+    g = gdt.GridFunction(lambda x: torch.cos(np.pi / 2 * x[..., 0]) * torch.cos(np.pi / 2 * x[..., 1]) + 0.3 * x[..., 0])
+    space, op, rhs = _swipdg(gdt, mesh, kappa, force, 1.0, dirichlet=g)
+    A, b = oracle.mesh_assemble_swipdg(X, cells, kappa=kappa, force=force, dirichlet_fn=oracle.DIRICHLET_TEST,
+                                       dirichlet_rhs=3)
+    assert rel_err(op.csr()[2].cpu().numpy(), A.val) < 1e-12
+    assert rel_err(rhs.cpu().numpy(), b) < 1e-12
+
+
+def test_kuhn_grid_as_mesh_swipdg_equals_structured_path(gdt):
+    n = [9, 7]
+    g = gdt.make_cube_grid([0.0, 0.0], [1.0, 1.0], n, simplex=True)
+    cells = gdt.ContinuousLagrangeSpace(g, 1).global_indices()
+    t = [np.linspace(0.0, 1.0, k + 1) for k in n]
+    X = np.stack(np.meshgrid(*t, indexing="ij"), -1).transpose(1, 0, 2).reshape(-1, 2)
+    mesh = gdt.make_simplex_mesh(X, cells)
+    rng = np.random.default_rng(5)
+    kappa, force = np.exp(rng.standard_normal(g.num_elements)), rng.uniform(0.5, 1.5, g.num_elements)
+    out = []
+    for grid in (g, mesh):
+        _, op, rhs = _swipdg(gdt, grid, kappa, force)
+        out.append([t.cpu().numpy() for t in op.csr()] + [rhs.cpu().numpy()])
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert rel_err(out[1][2], out[0][2]) < 1e-13
+    assert rel_err(out[1][3], out[0][3]) < 1e-13

@@ -60,3 +60,20 @@ def test_delaunay_mesh_patch_test_and_area(oracle, dim, n):
     assert inner.any()
     assert np.abs(r[inner]).max() <= 1e-12 * abs(S).max() * np.abs(u).max()
     assert abs(b.sum() - 1.0) <= 1e-13
+
+
+@pytest.mark.parametrize("n", [[5, 4], [7, 7]])
+@pytest.mark.parametrize("theta,rhs_terms", [(1.0, 0), (1.0, 3), (-1.0, 1)])
+def test_kuhn_grid_as_mesh_swipdg_equals_structured(oracle, n, theta, rhs_terms):
+    # SWIPDG on the Kuhn triangles handed over as a mesh: the structured restatement's system
+    og, coords, cells = kuhn_mesh(oracle, 2, n)
+    rng = np.random.default_rng(9)
+    ne = cells.shape[0]
+    kappa, force = np.exp(rng.standard_normal(ne)), rng.uniform(-1, 2, ne)
+    kw = dict(kappa=kappa, force=force, theta=theta, sigma_inner=8.0, sigma_boundary=14.0, beta=1.0,
+              dirichlet_fn=oracle.DIRICHLET_TEST, dirichlet_rhs=rhs_terms)
+    A, b = oracle.assemble_swipdg(og, 1, **kw)
+    M, bm = oracle.mesh_assemble_swipdg(coords, cells, **kw)
+    assert np.array_equal(M.row_ptr, A.row_ptr) and np.array_equal(M.col, A.col)
+    assert np.abs(M.val - A.val).max() <= 1e-13 * np.abs(A.val).max()
+    assert np.abs(bm - b).max() <= 1e-13 * np.abs(b).max()
