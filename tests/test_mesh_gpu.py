@@ -58,7 +58,6 @@ def test_mesh_assembly_matches_oracle(gdt, oracle, dim, n, seed, dirichlet):
     assert rel_err(rhs.cpu().numpy(), b) < 1e-12
     # the DoF map is the element vertex lists, and the load vector alone matches the fused one
     assert np.array_equal(space.global_indices().cpu().numpy().reshape(ne, dim + 1), cells)
-    rhs2 = torch.zeros_like(rhs)
     fn = gdt.VectorFunctional(mesh, space)
     fn.append(gdt.LocalElementIntegralFunctional(gdt.LocalElementProductIntegrand().with_ansatz(
         torch.tensor(force, device="cuda"))))
@@ -71,7 +70,6 @@ def test_mesh_assembly_matches_oracle(gdt, oracle, dim, n, seed, dirichlet):
             u = op.apply_inverse(rhs, opts={"tol": 1e-12, "precision": precision})
             assert op.last_solve_info["converged"]
             assert rel_err(u.cpu().numpy(), xd) < 1e-9, precision
-    del rhs2
 
 
 @pytest.mark.parametrize("dim,n", [(2, [9, 7]), (3, [4, 5, 3])])

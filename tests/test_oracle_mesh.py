@@ -77,3 +77,14 @@ def test_kuhn_grid_as_mesh_swipdg_equals_structured(oracle, n, theta, rhs_terms)
     assert np.array_equal(M.row_ptr, A.row_ptr) and np.array_equal(M.col, A.col)
     assert np.abs(M.val - A.val).max() <= 1e-13 * np.abs(A.val).max()
     assert np.abs(bm - b).max() <= 1e-13 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("dim,n", [(2, 8), (3, 4)])
+def test_mesh_boundary_is_the_convex_hull(oracle, dim, n):
+    # on a Delaunay mesh of points in a box, the faces of one element are the convex hull's facets
+    X, cells = delaunay_mesh(dim, n, 17)
+    hull = spatial.ConvexHull(X)
+    on_box = np.any((X <= 1e-12) | (X >= 1 - 1e-12), axis=1)
+    bnd = oracle.mesh_boundary(X.shape[0], cells)
+    assert np.array_equal(np.sort(bnd), np.flatnonzero(on_box))
+    assert set(np.unique(hull.simplices)) <= set(bnd.tolist())
