@@ -735,6 +735,9 @@ extern "C" gdt_status gdt_grid_create_simplex_mesh(int dim, int64_t nvert, const
   // vertex -> element adjacency, elements ascending
   std::vector<int> ptr(size_t(nvert) + 1, 0), adj(cells32.size());
   for (int c : cells32) ++ptr[size_t(c) + 1];
+  // every vertex belongs to an element (a vertex of no element would give an empty, singular row)
+  for (int64_t v = 0; v < nvert; ++v)
+    if (ptr[size_t(v) + 1] == 0) return GDT_EINVAL;
   for (int64_t v = 0; v < nvert; ++v) ptr[size_t(v) + 1] += ptr[size_t(v)];
   std::vector<int> fillpos(ptr.begin(), ptr.end() - 1);
   for (int64_t e = 0; e < nelem; ++e)

@@ -149,8 +149,8 @@ gdt_status gdt_grid_set_vertices(gdt_grid grid, const double* coords);
  * make_continuous_lagrange_space, spaces/h1/continuous-lagrange.hh:189-203). dim 2 (triangles) or 3
  * (tetrahedra); coords [num_vertices][dim], cells [num_elements][dim + 1] vertex indices; host or
  * device pointers, copied. Elements must have distinct vertices and a volume above rounding (|det J|
- * above 1e-12 times the product of its edge lengths), and a face may belong to at most two elements
- * (GDT_EINVAL otherwise). Boundary vertices (the Dirichlet DoFs of
+ * above 1e-12 times the product of its edge lengths), every vertex must belong to an element, and a
+ * face may belong to at most two elements (GDT_EINVAL otherwise). Boundary vertices (the Dirichlet DoFs of
  * DirichletConstraints, tools/dirichlet-constraints.hh:153-184) are the vertices of faces that belong
  * to one element. Such a grid takes continuous order-1 spaces (DoF = vertex index, the ContinuousMapper
  * of spaces/mapper/continuous.hh:139-150), their element pattern, the Laplace stiffness and load

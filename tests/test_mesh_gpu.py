@@ -162,7 +162,8 @@ def test_mesh_refusals(gdt):
     bad[1][2, 2] = bad[1][2, 0]        # repeated vertex
     Xf = X.copy()
     Xf[cells[0, 2]] = 0.5 * (Xf[cells[0, 0]] + Xf[cells[0, 1]])  # a flat triangle
-    for Xi, ci in ((X, bad[0]), (X, bad[1]), (Xf, cells)):
+    Xextra = np.vstack([X, [[2.0, 2.0]]])  # a vertex of no element
+    for Xi, ci in ((X, bad[0]), (X, bad[1]), (Xf, cells), (Xextra, cells)):
         with pytest.raises(gdt.GdtError) as e:
             gdt.make_simplex_mesh(Xi, ci)
         assert e.value.status == gdt._capi.EINVAL
