@@ -88,3 +88,35 @@ def test_mesh_boundary_is_the_convex_hull(oracle, dim, n):
     bnd = oracle.mesh_boundary(X.shape[0], cells)
     assert np.array_equal(np.sort(bnd), np.flatnonzero(on_box))
     assert set(np.unique(hull.simplices)) <= set(bnd.tolist())
+
+
+@pytest.mark.parametrize("n,theta", [(9, 1.0), (14, -1.0)])
+def test_mesh_swipdg_reproduces_constants(oracle, n, theta):
+    # SWIPDG is consistent: with f = 0 and Dirichlet data g = c on both right-hand side terms, the
+    # discrete solution is u = c on every DoF, whatever the coefficient
+    import scipy.sparse.linalg as spl
+
+    X, cells = delaunay_mesh(2, n, 41)
+    kappa = np.exp(np.random.default_rng(41).standard_normal(cells.shape[0]) * 2.0)
+    A, b = oracle.mesh_assemble_swipdg(X, cells, kappa=kappa, force_const=0.0, theta=theta,
+                                       dirichlet_const=0.7, dirichlet_rhs=3)
+    u = spl.spsolve(A.to_scipy().tocsc(), b)
+    assert np.abs(u - 0.7).max() <= 1e-10
+
+
+@pytest.mark.parametrize("dim,n", [(2, 10), (3, 5)])
+def test_mesh_p1_reproduces_linear_functions(oracle, dim, n):
+    # P1 on a mesh with f = 0 and Dirichlet values of a linear function: the solution is that function
+    import scipy.sparse.linalg as spl
+
+    X, cells = delaunay_mesh(dim, n, 43)
+    A, _ = oracle.mesh_assemble(X, cells, kappa=np.ones(cells.shape[0]), force_const=0.0, dirichlet=False)
+    lin = 0.2 + X @ np.array([1.0, -0.7, 0.4][:dim])
+    bnd = oracle.mesh_boundary(X.shape[0], cells)
+    inner = np.setdiff1d(np.arange(X.shape[0]), bnd)
+    S = A.to_scipy().tocsr()
+    u = np.zeros(X.shape[0])
+    u[bnd] = lin[bnd]
+    rhs = -S[inner][:, bnd] @ lin[bnd]
+    u[inner] = spl.spsolve(S[inner][:, inner].tocsc(), rhs)
+    assert np.abs(u - lin).max() <= 1e-11
