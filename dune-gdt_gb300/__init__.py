@@ -288,8 +288,14 @@ class _Space:
 
         x, _ = self.quadrature(order)
         g = self.grid
+        if isinstance(g, SimplexMesh):  # the affine map of every element: x_0 + sum_k xi_k (x_{k+1} - x_0)
+            device = device or torch.device("cuda", torch.cuda.current_device())
+            d = g.dimension
+            X = g.vertices.to(device)[g.cells.to(device)]  # [element, d + 1, d]
+            xr = torch.tensor(x[:, :d], device=device)  # [q, d]
+            return X[:, None, 0, :] + torch.einsum("qk,ekd->eqd", xr, X[:, 1:, :] - X[:, None, 0, :])
         if getattr(g, "vertices", None) is not None:
-            raise GdtError(capi.EUNSUPPORTED, "quadrature points of mapped grids and simplex meshes")
+            raise GdtError(capi.EUNSUPPORTED, "quadrature points of mapped grids")
         d = g.dimension
         device = device or torch.device("cuda", torch.cuda.current_device())
         lo = torch.tensor(g.lower_left, dtype=torch.float64, device=device)

@@ -457,6 +457,7 @@ gdt_status gdt_element_error(gdt_context ctx, gdt_space s, int norm, int quad_or
   if (quad_order < 0 || quad_order > 40) return fail(ctx, GDT_EINVAL, "quadrature order out of range");
   if (s->kind == GDT_SPACE_FV || (s->kind == GDT_SPACE_DG && s->order != 1))
     return fail(ctx, GDT_EUNSUPPORTED, "element error of continuous (order 1, 2) and DG (order 1) spaces");
+  if (s->g.mesh) return mesh_element_error(ctx, *s, norm, quad_order, u, ref_qp, eta2, total);
   if (s->g.xv) return fail(ctx, GDT_EUNSUPPORTED, "element error on mapped grids");
   return element_error(ctx, *s, norm, quad_order, u, ref_qp, eta2, total);
 }

@@ -162,6 +162,8 @@ gdt_status mesh_global_indices(gdt_context ctx, const GridDesc& g, int64_t* out)
 gdt_status mesh_dg_pattern(gdt_context ctx, gdt_matrix m);
 gdt_status mesh_swipdg(gdt_context ctx, gdt_matrix m, const gdt_ipdg_desc* d, double* rhs);
 gdt_status mesh_dg_face_points(const gdt_space_s& s, double* xy);
+gdt_status mesh_element_error(gdt_context ctx, const gdt_space_s& s, int norm, int quad_order, const double* u,
+                              const double* ref, double* eta2, double* total);
 // assemble_cg.cu
 gdt_status assemble_cg(gdt_context ctx, gdt_matrix m, const gdt_diffusion_desc* d, double* rhs);
 gdt_status assemble_cg_rhs(gdt_context ctx, const gdt_space_s& s, const gdt_diffusion_desc* d, double* rhs);

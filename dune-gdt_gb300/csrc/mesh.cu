@@ -21,6 +21,7 @@
 #include <new>
 #include <vector>
 
+#include "highorder.cuh"
 #include "internal.cuh"
 
 namespace gdt {
@@ -554,6 +555,112 @@ gdt_status mesh_dg_face_points(const gdt_space_s& sp, double* xy) {
         out[1] = xa[1] + xi[q] * (xb[1] - xa[1]);
       }
     }
+  return GDT_OK;
+}
+
+namespace {
+
+// Element indicators of the EOC studies (test/stationary-eocstudies/base.hh:259-269) on a mesh:
+// eta_e^2 = sum_q w_q |det J_e| |grad u_h - g(x_q)|^2 (norm 0) or (u_h(x_q) - v(x_q))^2 (norm 1), the
+// reference values given at the points of the reference rule mapped by each element's affine map;
+// u_h from the P1 vertex DoFs (continuous) or the element's own DoFs (DG)
+template <int DIM>
+__global__ void k_mesh_element_error(GridDesc g, int dg, int nq, int norm, const double* __restrict__ phi,
+                                     const double* __restrict__ wq, const double* __restrict__ u,
+                                     const double* __restrict__ ref, double* __restrict__ eta2) {
+  for (long long el = blockIdx.x * (long long)blockDim.x + threadIdx.x; el < g.nelem;
+       el += (long long)gridDim.x * blockDim.x) {
+    const int e = int(el);
+    int w[DIM + 1];
+    double G[DIM + 1][DIM];
+    const double adet = mesh_element<DIM>(g, e, w, G) * (DIM == 2 ? 2.0 : 6.0);
+    double ue[DIM + 1], gu[DIM];
+#pragma unroll
+    for (int i = 0; i <= DIM; ++i) ue[i] = u[dg ? (DIM + 1) * el + i : w[i]];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i <= DIM; ++i) s = fma(ue[i], G[i][a], s);
+      gu[a] = s;
+    }
+    double acc = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      double d2 = 0.0;
+      if (norm == 0) {
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+          const double d = gu[a] - ref[(el * nq + q) * DIM + a];
+          d2 = fma(d, d, d2);
+        }
+      } else {
+        double v = 0.0;
+#pragma unroll
+        for (int i = 0; i <= DIM; ++i) v = fma(ue[i], phi[q * (DIM + 1) + i], v);
+        const double d = v - ref[el * nq + q];
+        d2 = d * d;
+      }
+      acc = fma(wq[q] * adet, d2, acc);
+    }
+    eta2[el] = acc;
+  }
+}
+
+}  // namespace
+
+gdt_status mesh_element_error(gdt_context ctx, const gdt_space_s& sp, int norm, int quad_order, const double* u,
+                              const double* ref, double* eta2, double* total) {
+  const GridDesc& g = sp.g;
+  if (sp.order != 1 || !(sp.kind == GDT_SPACE_CG || (sp.kind == GDT_SPACE_DG && g.dim == 2)))
+    return fail(ctx, GDT_EUNSUPPORTED, "element error on meshes: order-1 continuous and DG spaces");
+  cudaStream_t st = ctx->stream;
+  const ho::QuadratureInfo Q = ho::quadrature_info_order(g, quad_order);
+  const int nl = g.dim + 1;
+  // P1 on the reference simplex: phi_0 = 1 - sum xi, phi_k = xi_{k-1}
+  std::vector<double> phi(size_t(Q.nq) * nl);
+  for (int q = 0; q < Q.nq; ++q) {
+    double s = 0.0;
+    for (int k = 0; k < g.dim; ++k) {
+      phi[size_t(q) * nl + k + 1] = Q.x[3 * size_t(q) + k];
+      s += Q.x[3 * size_t(q) + k];
+    }
+    phi[size_t(q) * nl] = 1.0 - s;
+  }
+  double *dphi = nullptr, *dw = nullptr, *sum = nullptr;
+  void* tmp = nullptr;
+  struct Freer {
+    void* p[4];
+    cudaStream_t s;
+    ~Freer() {
+      for (void* q : p)
+        if (q) cudaFreeAsync(q, s);
+    }
+  } freer{{}, st};
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&dphi, sizeof(double) * phi.size(), st));
+  freer.p[0] = dphi;
+  GDT_TRY_CUDA(ctx, cudaMallocAsync(&dw, sizeof(double) * Q.w.size(), st));
+  freer.p[1] = dw;
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(dphi, phi.data(), sizeof(double) * phi.size(), cudaMemcpyHostToDevice, st));
+  GDT_TRY_CUDA(ctx, cudaMemcpyAsync(dw, Q.w.data(), sizeof(double) * Q.w.size(), cudaMemcpyHostToDevice, st));
+  const int bl = std::max(1, std::min(grid_blocks(g.nelem, 128), ctx->num_sms * 8));
+  const int dg = sp.kind == GDT_SPACE_DG ? 1 : 0;
+  if (g.dim == 2) k_mesh_element_error<2><<<bl, 128, 0, st>>>(g, dg, Q.nq, norm, dphi, dw, u, ref, eta2);
+  else k_mesh_element_error<3><<<bl, 128, 0, st>>>(g, dg, Q.nq, norm, dphi, dw, u, ref, eta2);
+  GDT_CHECK(ctx, check_launch(ctx, "mesh element error"));
+  if (total) {
+    GDT_TRY_CUDA(ctx, cudaMallocAsync(&sum, sizeof(double), st));
+    freer.p[2] = sum;
+    size_t tb = 0;
+    cub::DeviceReduce::Sum(nullptr, tb, eta2, sum, int(g.nelem), st);
+    GDT_TRY_CUDA(ctx, cudaMallocAsync(&tmp, std::max<size_t>(tb, 16), st));
+    freer.p[3] = tmp;
+    cub::DeviceReduce::Sum(tmp, tb, eta2, sum, int(g.nelem), st);
+    double h = 0.0;
+    GDT_TRY_CUDA(ctx, cudaMemcpyAsync(&h, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
+    GDT_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    *total = std::sqrt(h);
+  }
+  GDT_TRY_CUDA(ctx, cudaStreamSynchronize(st));  // the host tables outlive the copies
   return GDT_OK;
 }
 

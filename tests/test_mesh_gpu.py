@@ -241,3 +241,40 @@ def test_kuhn_grid_as_mesh_swipdg_equals_structured_path(gdt):
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert rel_err(out[1][2], out[0][2]) < 1e-13
     assert rel_err(out[1][3], out[0][3]) < 1e-13
+
+
+@pytest.mark.parametrize("dim,n,kind", [(2, 9, "cg"), (3, 4, "cg"), (2, 8, "dg")])
+@pytest.mark.parametrize("norm", ["h1_semi", "l2"])
+def test_mesh_element_error_matches_numpy(gdt, dim, n, kind, norm):
+    # the EOC studies' element indicators on a mesh against a numpy restatement at the same points
+    X, cells = delaunay_mesh(dim, n, 51)
+    mesh = gdt.make_simplex_mesh(X, cells)
+    space = gdt.ContinuousLagrangeSpace(mesh, 1) if kind == "cg" else gdt.DiscontinuousLagrangeSpace(mesh, 1)
+    rng = np.random.default_rng(51)
+    u = rng.standard_normal(space.num_DoFs)
+    order = 4
+    xq = space.quadrature_points(order)  # [element, q, dim]
+    xr, wr = space.quadrature(order)
+    if norm == "h1_semi":
+        ref = torch.stack([torch.cos(3 * xq[..., a]) for a in range(dim)], -1)
+    else:
+        ref = torch.sin(2 * xq[..., 0]) + xq[..., 1]
+    eta2, total = gdt.element_error(space, torch.tensor(u, device="cuda"), ref.contiguous(), norm=norm,
+                                    quad_order=order)
+    refn = ref.cpu().numpy()
+    exp = np.empty(cells.shape[0])
+    for e in range(cells.shape[0]):
+        w = cells[e]
+        J = np.stack([X[w[k + 1]] - X[w[0]] for k in range(dim)], axis=1)
+        Gr = np.vstack([-np.ones(dim), np.eye(dim)]) @ np.linalg.inv(J)
+        ue = u[w] if kind == "cg" else u[(dim + 1) * e:(dim + 1) * (e + 1)]
+        wq = wr * abs(np.linalg.det(J))
+        if norm == "h1_semi":
+            d = (ue @ Gr)[None, :] - refn[e]
+            exp[e] = wq @ (d * d).sum(1)
+        else:
+            phi = np.hstack([1.0 - xr[:, :dim].sum(1, keepdims=True), xr[:, :dim]])
+            d = phi @ ue - refn[e]
+            exp[e] = wq @ (d * d)
+    assert rel_err(eta2.cpu().numpy(), exp) < 1e-12
+    assert abs(total - np.sqrt(exp.sum())) <= 1e-12 * np.sqrt(exp.sum())
